@@ -1,0 +1,967 @@
+// capi.cu — host side of libvpmgpu.so: contexts, transfers, work planning,
+// time stepping with CUDA graphs, diagnostics, autotuning.  The C ABI is
+// declared in include/vpm_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "capi_internal.h"
+
+using namespace vpm;
+
+namespace vpm {
+
+thread_local std::string g_last_error;
+
+int set_error(std::string* slot, int code, const std::string& msg) {
+  if (slot) *slot = msg;
+  g_last_error = msg;
+  return code;
+}
+
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+// --------------------------------------------------------- shape choices --
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, Shape> g_tune;  // (device, pass, kernel, prec, bucket)
+
+int size_bucket(int64_t n) {
+  int b = 0;
+  while ((int64_t(1) << (b + 1)) <= n && b < 40) ++b;
+  return b;
+}
+}  // namespace
+
+Shape default_shape(int pass, int precision) {
+  if (precision == VPM_PREC_FP64) return Shape{128, 1};
+  (void)pass;
+  return Shape{128, 2};
+}
+
+Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n,
+                   const Shape* pinned) {
+  if (pinned && pinned->block > 0) return *pinned;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(std::make_tuple(device, pass, kernel, precision, size_bucket(n)));
+  if (it != g_tune.end()) return it->second;
+  return default_shape(pass, precision);
+}
+
+void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[std::make_tuple(device, pass, kernel, precision, size_bucket(n))] = s;
+}
+
+int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int num_sms) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int, int>, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_tuple(device, pass, kernel, precision, s.block, s.tpt);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int per = pair_ctas_per_sm(pass, kernel, precision, s);
+  int r = std::max(1, per) * num_sms;
+  cache[key] = r;
+  return r;
+}
+
+// Source split: choose the number of source chunks so that the grid of
+// n_tb x n_chunk items fills whole waves of resident CTAs, keeping chunks at
+// least two tiles long and preferring fewer chunks at equal efficiency.
+int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out) {
+  int best_c = 1;
+  int64_t best_chunk = std::max<int64_t>(ns, 1);
+  double best = -1.0;
+  for (int c = 1; c <= 128; ++c) {
+    int64_t chunk = round_up(std::max<int64_t>(ceil_div(ns, c), 1), block);
+    if (c > 1 && chunk < 2 * block) break;
+    const int cc = int(std::max<int64_t>(ceil_div(ns, chunk), 1));
+    const int64_t items = n_tb * cc;
+    const int64_t waves = ceil_div(items, resident);
+    const double eff = double(items) / double(waves * resident);
+    const double score = eff - 0.003 * cc;
+    if (score > best + 1e-12) {
+      best = score;
+      best_c = cc;
+      best_chunk = chunk;
+    }
+  }
+  *chunk_out = best_chunk;
+  return best_c;
+}
+
+// Plan and enqueue one pair pass.  `need_part` (elements) is raised to what
+// the launch needs; when dry, nothing is launched.
+cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* pinned,
+                     double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
+                     cudaStream_t st, PairPlan* plan_out) {
+  const int64_t nt = pc.t1 - pc.t0;
+  if (nt <= 0) return cudaSuccess;
+  const Shape sh = lookup_shape(device, pc.pass, pc.kernel, pc.prec, pc.ns, pinned);
+  const int64_t TB = int64_t(sh.block) * sh.tpt;
+  const int64_t n_tb = ceil_div(nt, TB);
+  const int resident = resident_ctas(device, pc.pass, pc.kernel, pc.prec, sh, num_sms);
+  int64_t chunk = 0;
+  int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk);
+  const int nv = pc.pass == PASS_UJ ? kNvalUJ : kNvalZeta;
+  const size_t need = n_chunk > 1 ? size_t(n_chunk) * nv * size_t(ldp) : 0;
+  if (need_part) *need_part = std::max(*need_part, need);
+  if (plan_out) {
+    plan_out->shape = sh;
+    plan_out->n_tb = n_tb;
+    plan_out->n_chunk = n_chunk;
+    plan_out->chunk = chunk;
+  }
+  if (dry) return cudaSuccess;
+  if (need > part_elems) return cudaErrorMemoryAllocation;
+  PairArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.xs = pc.xs; a.gs = pc.gs; a.ss = pc.ss; a.vs = pc.vs; a.lds = pc.lds;
+  a.xt = pc.xt; a.ldt = pc.ldt;
+  a.sigma_scale = pc.sigma_scale;
+  a.t_off = pc.t0; a.nt = nt; a.ns = pc.ns; a.chunk = chunk;
+  a.n_tb = int(n_tb); a.n_chunk = n_chunk;
+  a.items = nullptr; a.n_items = 0; a.counter = nullptr;
+  a.u = pc.u; a.j = pc.j; a.ldo = pc.ldo;
+  a.part = part; a.ldp = ldp;
+  cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
+  if (e != cudaSuccess) return e;
+  if (n_chunk > 1) {
+    e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
+                      pc.u, pc.j, pc.ldo, st);
+  }
+  return e;
+}
+
+}  // namespace vpm
+
+// ====================================================================== ctx ==
+
+namespace {
+
+int ctx_fail(vpm_ctx* c, int code, const std::string& msg) {
+  return set_error(c ? &c->err : nullptr, code, msg);
+}
+
+int cuda_fail(vpm_ctx* c, cudaError_t e, const char* what) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  return ctx_fail(c, VPM_ERR_CUDA, buf);
+}
+
+#define CTX_CK(c, call)                                        \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return cuda_fail((c), e_, #call);  \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+int check_inject(vpm_ctx* c) {
+  if (c->fail_after > 0 && --c->fail_after == 0)
+    return ctx_fail(c, VPM_ERR_INJECTED, "fault injection: launch refused by the debug hook");
+  return VPM_OK;
+}
+
+int ensure_stage(vpm_ctx* c, size_t elems) {
+  if (elems <= c->h_stage_elems) return VPM_OK;
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  c->h_stage = nullptr;
+  c->h_stage_elems = 0;
+  CTX_CK(c, cudaMallocHost(&c->h_stage, elems * sizeof(double)));
+  c->h_stage_elems = elems;
+  return VPM_OK;
+}
+
+int ensure_part(vpm_ctx* c, size_t elems) {
+  if (elems <= c->part_elems) return VPM_OK;
+  if (c->part) cudaFree(c->part);
+  c->part = nullptr;
+  c->part_elems = 0;
+  cudaError_t e = cudaMalloc(&c->part, elems * sizeof(double));
+  if (e != cudaSuccess) return ctx_fail(c, VPM_ERR_NOMEM, "cannot allocate pair-pass scratch");
+  c->part_elems = elems;
+  return VPM_OK;
+}
+
+int ensure_test_filter(vpm_ctx* c) {
+  if (c->Ut) return VPM_OK;
+  const size_t ld = size_t(c->ld);
+  if (cudaMalloc(&c->Ut, 15 * ld * sizeof(double)) != cudaSuccess)
+    return ctx_fail(c, VPM_ERR_NOMEM, "cannot allocate test-filter buffers");
+  c->Jt = c->Ut + 3 * ld;
+  c->Et = c->Jt + 9 * ld;
+  return VPM_OK;
+}
+
+// Host strided AoS -> pinned SoA staging -> device rows [i0, i0+n).
+int upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const double* G,
+           int64_t sg, const double* S, int64_t ss) {
+  if (n == 0) return VPM_OK;
+  int rc = ensure_stage(c, size_t(7) * n);
+  if (rc) return rc;
+  double* h = c->h_stage;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int k = 0; k < 3; ++k) {
+      h[k * n + i] = X[i * sx + k];
+      h[(3 + k) * n + i] = G[i * sg + k];
+    }
+    h[6 * n + i] = S[i * ss];
+  }
+  const size_t w = size_t(n) * sizeof(double), dp = size_t(c->ld) * sizeof(double);
+  CTX_CK(c, cudaMemcpy2DAsync(c->X + i0, dp, h, w, w, 3, cudaMemcpyHostToDevice, c->st));
+  CTX_CK(c, cudaMemcpy2DAsync(c->G + i0, dp, h + 3 * n, w, w, 3, cudaMemcpyHostToDevice, c->st));
+  CTX_CK(c, cudaMemcpyAsync(c->S + i0, h + 6 * n, w, cudaMemcpyHostToDevice, c->st));
+  // Fresh particles start with empty SFS memory.
+  CTX_CK(c, cudaMemset2DAsync(c->C + i0, dp, 0, w, 3, c->st));
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  return VPM_OK;
+}
+
+int validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double* G, int64_t sg,
+                  const double* S, int64_t ss) {
+  if (n < 0) return ctx_fail(c, VPM_ERR_INVALID, "negative particle count");
+  if (n == 0) return VPM_OK;
+  if (!X || !G || !S) return ctx_fail(c, VPM_ERR_INVALID, "null particle array");
+  if (sx < 3 || sg < 3 || ss < 1) return ctx_fail(c, VPM_ERR_INVALID, "stride too small");
+  for (int64_t i = 0; i < n; ++i) {
+    const double s = S[i * ss];
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(X[i * sx + k]) || !std::isfinite(G[i * sg + k]))
+        return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite position or strength in input");
+    if (!std::isfinite(s)) return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite core size in input");
+    if (!(s > 0.0)) return ctx_fail(c, VPM_ERR_INVALID, "core size must be positive");
+  }
+  return VPM_OK;
+}
+
+// Download rows [i0, i0+n) of `rows` consecutive device rows (ld apart) into
+// the host array out[i*stride + k].
+int download_rows(vpm_ctx* c, const double* dev, int rows, int64_t i0, int64_t n, double* out,
+                  int64_t stride) {
+  if (!out || n == 0) return VPM_OK;
+  if (stride < rows) return ctx_fail(c, VPM_ERR_INVALID, "stride too small");
+  int rc = ensure_stage(c, size_t(rows) * n);
+  if (rc) return rc;
+  const size_t w = size_t(n) * sizeof(double), sp = size_t(c->ld) * sizeof(double);
+  CTX_CK(c, cudaMemcpy2DAsync(c->h_stage, w, dev + i0, sp, w, rows, cudaMemcpyDeviceToHost, c->st));
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  const double* h = c->h_stage;
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < rows; ++k) out[i * stride + k] = h[k * n + i];
+  return VPM_OK;
+}
+
+bool valid_kernel(int k) { return k == VPM_KERNEL_WINCKELMANS || k == VPM_KERNEL_GAUSSIANERF; }
+bool valid_prec(int p) { return p == VPM_PREC_FP64 || p == VPM_PREC_FP32 || p == VPM_PREC_FP32C; }
+
+int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
+  if (!s) return ctx_fail(c, VPM_ERR_INVALID, "null scheme");
+  if (!valid_kernel(s->kernel)) return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel");
+  if (!valid_prec(s->precision)) return ctx_fail(c, VPM_ERR_INVALID, "unknown precision");
+  if (s->integration != VPM_INTEGRATION_EULER && s->integration != VPM_INTEGRATION_RK3)
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown integration scheme");
+  if (s->sfs != VPM_SFS_NONE && s->sfs != VPM_SFS_DYNAMIC && s->sfs != VPM_SFS_CONSTANT)
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown SFS model");
+  if (s->relaxation != VPM_RELAX_NONE && s->relaxation != VPM_RELAX_PEDRIZZETTI)
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown relaxation scheme");
+  if (!(s->nu >= 0.0) || !std::isfinite(s->nu)) return ctx_fail(c, VPM_ERR_INVALID, "bad viscosity");
+  // Core spreading is only compatible with the Gaussian basis
+  // (FLOWUnsteady checks kernel/viscous compatibility, src/FLOWUnsteady_simulation.jl:308-314).
+  if (s->nu > 0.0 && s->kernel != VPM_KERNEL_GAUSSIANERF)
+    return ctx_fail(c, VPM_ERR_UNSUPPORTED,
+                    "core spreading requires the Gaussian-erf kernel");
+  if (s->sfs == VPM_SFS_DYNAMIC && !(s->sfs_alpha > 0.0 && s->sfs_alpha != 1.0))
+    return ctx_fail(c, VPM_ERR_INVALID, "dynamic SFS needs 0 < alpha != 1");
+  if (!(1.0 + 3.0 * s->f != 0.0)) return ctx_fail(c, VPM_ERR_INVALID, "bad formulation f");
+  return VPM_OK;
+}
+
+}  // namespace
+
+// Enqueue the pair pass of one context (targets [t0,t1) of its own particles).
+cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int64_t t1,
+                     double scale, const double* vs, double* u, double* j) {
+  if (c->bp) {
+    // Batch: one persistent launch over the flattened (field, target tile,
+    // source chunk) queue, then the fixed-order reduction of split fields.
+    BatchPlan* bp = c->bp;
+    if (bp->kernel != kernel || bp->precision != prec) {
+      if (c->dry) {
+        if (batch_plan(c, kernel, prec) != VPM_OK) return cudaErrorInvalidValue;
+      } else {
+        return cudaErrorInvalidValue;  // plans are built outside capture (dry pass)
+      }
+    }
+    const int nv = pass == PASS_UJ ? kNvalUJ : kNvalZeta;
+    const size_t need = bp->max_chunks > 1 ? size_t(bp->max_chunks) * nv * size_t(c->ld) : 0;
+    c->part_need = std::max(c->part_need, need);
+    if (c->dry) return cudaSuccess;
+    if (need > c->part_elems) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMemsetAsync(bp->d_counter, 0, sizeof(unsigned int), c->st);
+    if (e != cudaSuccess) return e;
+    PairArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.xs = c->X; a.gs = c->G; a.ss = c->S; a.vs = vs; a.lds = c->ld;
+    a.xt = c->X; a.ldt = c->ld;
+    a.sigma_scale = scale;
+    a.items = bp->d_items; a.n_items = bp->n_items; a.counter = bp->d_counter;
+    a.u = u; a.j = j; a.ldo = c->ld;
+    a.part = c->part; a.ldp = c->ld;
+    e = launch_pair(pass, kernel, prec, bp->shape, a, std::min(bp->resident, bp->n_items), c->st);
+    if (e != cudaSuccess) return e;
+    c->launches += 1;
+    if (bp->max_chunks > 1) {
+      e = launch_reduce(pass, kernel, c->part, c->ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
+                        0, c->n, u, j, c->ld, c->st);
+      c->launches += 1;
+    }
+    return e;
+  }
+  PairCall pc;
+  pc.pass = pass; pc.kernel = kernel; pc.prec = prec;
+  pc.t0 = t0; pc.t1 = t1; pc.ns = c->n;
+  pc.xs = c->X; pc.gs = c->G; pc.ss = c->S; pc.vs = vs; pc.lds = c->ld;
+  pc.xt = c->X; pc.ldt = c->ld;
+  pc.sigma_scale = scale;
+  pc.u = u; pc.j = j; pc.ldo = c->ld;
+  const Shape* pinned = &c->pinned[pass][kernel][prec];
+  PairPlan plan;
+  plan.n_chunk = 1;
+  cudaError_t e = run_pair(pc, c->device, c->num_sms, pinned, c->part, c->ld, c->part_elems,
+                           &c->part_need, c->dry, c->st, &plan);
+  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += plan.n_chunk > 1 ? 2 : 1;
+  return e;
+}
+
+#define ENQ(c, call)                                        \
+  do {                                                      \
+    if (!(c)->dry) {                                        \
+      cudaError_t e_ = (call);                              \
+      if (e_ != cudaSuccess) return e_;                     \
+      (c)->launches += 1;                                   \
+    }                                                       \
+  } while (0)
+#define ENQP(c, call)                                       \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return e_;                       \
+  } while (0)
+
+// One stage of a step: U/J, SFS, fused update.
+static cudaError_t enqueue_stage(vpm_ctx* c, const vpm_scheme* s, double dt, double a, double b,
+                                 int stage) {
+  const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
+  const int K = s->kernel, P = s->precision;
+  ENQP(c, ctx_pair(c, PASS_UJ, K, P, 0, n, 1.0, nullptr, c->U, c->J));
+  const bool sfs = s->sfs != VPM_SFS_NONE;
+  if (sfs) {
+    ENQ(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
+    ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
+    ENQ(c, launch_estr_finish(n, ld, c->raw, c->J, s->transposed, c->E, c->st));
+    if (s->sfs == VPM_SFS_CONSTANT) {
+      ENQ(c, launch_sfs_constant(nf, s->sfs_Cd, c->C, c->st));
+    } else if (stage == 0) {
+      const double al = s->sfs_alpha;
+      ENQP(c, ctx_pair(c, PASS_UJ, K, P, 0, n, al, nullptr, c->Ut, c->Jt));
+      ENQ(c, launch_stretch_v(n, ld, c->Jt, c->G, s->transposed, c->V, c->st));
+      ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, al, c->V, c->raw, nullptr));
+      ENQ(c, launch_estr_finish(n, ld, c->raw, c->Jt, s->transposed, c->Et, c->st));
+      SfsParams sp;
+      sp.alpha = al; sp.rlxf = s->sfs_rlxf; sp.minC = s->sfs_minC; sp.maxC = s->sfs_maxC;
+      sp.zeta0 = zeta0_of(K); sp.transposed = s->transposed;
+      sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
+      ENQ(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
+    }
+  }
+  UpdateParams up;
+  up.a = a; up.b = b; up.dt = dt;
+  up.uinf0 = s->uinf[0]; up.uinf1 = s->uinf[1]; up.uinf2 = s->uinf[2];
+  up.zs = (s->f + s->g) / (1.0 + 3.0 * s->f);
+  up.ze = s->f / (1.0 + 3.0 * s->f);
+  up.zeta0 = zeta0_of(K);
+  up.nu = s->nu;
+  up.transposed = s->transposed;
+  up.sfs = sfs ? 1 : 0;
+  up.clip_backscatter = (sfs && (s->sfs_flags & VPM_SFS_CLIP_BACKSCATTER)) ? 1 : 0;
+  ENQ(c, launch_rk_update(nf, ld, c->X, c->G, c->S, c->U, c->J, c->E, c->C, c->Q, up, c->status,
+                          c->st));
+  return cudaSuccess;
+}
+
+static cudaError_t enqueue_step(vpm_ctx* c, const vpm_scheme* s, double dt, bool relax) {
+  static const double A[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0};
+  static const double B[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+  if (s->integration == VPM_INTEGRATION_RK3) {
+    for (int st = 0; st < 3; ++st) ENQP(c, enqueue_stage(c, s, dt, A[st], B[st], st));
+  } else {
+    ENQP(c, enqueue_stage(c, s, dt, 0.0, 1.0, 0));
+  }
+  if (relax) {
+    // Relaxation after the step on a fresh U/J (vpm.pedrizzetti).
+    ENQP(c, ctx_pair(c, PASS_UJ, s->kernel, s->precision, 0, c->n, 1.0, nullptr, c->U, c->J));
+    ENQ(c, launch_relax(c->n - c->n_static, c->ld, c->J, c->G, s->relax_factor, c->st));
+  }
+  return cudaSuccess;
+}
+
+static int check_status(vpm_ctx* c) {
+  int st = 0;
+  CTX_CK(c, cudaMemcpyAsync(&st, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  if (st) {
+    CTX_CK(c, cudaMemsetAsync(c->status, 0, sizeof(int), c->st));
+    CTX_CK(c, cudaStreamSynchronize(c->st));
+    if (st & STATUS_NONFINITE)
+      return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite particle state after the update");
+    return ctx_fail(c, VPM_ERR_CUDA, "device status word set");
+  }
+  return VPM_OK;
+}
+
+int ctx_validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double* G,
+                      int64_t sg, const double* S, int64_t ss) {
+  return validate_host(c, n, X, sx, G, sg, S, ss);
+}
+int ctx_upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const double* G,
+               int64_t sg, const double* S, int64_t ss) {
+  DeviceGuard dg(c->device);
+  return upload(c, i0, n, X, sx, G, sg, S, ss);
+}
+int ctx_download_rows(vpm_ctx* c, const double* dev, int rows, int64_t i0, int64_t n, double* out,
+                      int64_t stride) {
+  DeviceGuard dg(c->device);
+  return download_rows(c, dev, rows, i0, n, out, stride);
+}
+// Size the pair-pass scratch for a UJ pass over all particles.
+int ctx_prepare_scratch(vpm_ctx* c, int kernel, int precision) {
+  DeviceGuard dg(c->device);
+  c->dry = true;
+  c->part_need = 0;
+  cudaError_t e = ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J);
+  c->dry = false;
+  if (e != cudaSuccess) return cuda_fail(c, e, "planning a pair pass");
+  return ensure_part(c, c->part_need);
+}
+
+// ===================================================================== C ABI ==
+extern "C" {
+
+void vpm_scheme_default(vpm_scheme* s) {
+  if (!s) return;
+  std::memset(s, 0, sizeof(*s));
+  s->kernel = VPM_KERNEL_GAUSSIANERF;
+  s->precision = VPM_PREC_FP32C;
+  s->integration = VPM_INTEGRATION_RK3;
+  s->transposed = 1;
+  s->f = 0.0;
+  s->g = 0.2;
+  s->nu = 0.0;
+  s->sfs = VPM_SFS_NONE;
+  s->sfs_flags = VPM_SFS_CLIP_BACKSCATTER;
+  s->sfs_alpha = 0.999;
+  s->sfs_rlxf = 1.0;
+  s->sfs_minC = 0.0;
+  s->sfs_maxC = 1.0;
+  s->sfs_Cd = 0.0;
+  s->relaxation = VPM_RELAX_NONE;
+  s->relax_nsteps = 1;
+  s->relax_factor = 0.3;
+}
+
+int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
+  if (!out) return set_error(nullptr, VPM_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if (capacity < 1) return set_error(nullptr, VPM_ERR_INVALID, "capacity must be >= 1");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return set_error(nullptr, VPM_ERR_CUDA, "no such CUDA device");
+  DeviceGuard dg(device);
+  vpm_ctx* c = new vpm_ctx();
+  c->device = device;
+  c->cap = capacity;
+  c->ld = round_up(capacity, 32);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  std::memset(c->pinned, 0, sizeof(c->pinned));
+  const size_t ld = size_t(c->ld);
+  // State + evaluation rows: X3 G3 S1 C3 Q8 U3 J9 E3 V3 raw6 = 42 rows.
+  const size_t rows = 42;
+  if (cudaMalloc(&c->base, rows * ld * sizeof(double)) != cudaSuccess) {
+    delete c;
+    return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate the particle field");
+  }
+  double* p = c->base;
+  c->X = p; p += 3 * ld;
+  c->G = p; p += 3 * ld;
+  c->S = p; p += ld;
+  c->C = p; p += 3 * ld;
+  c->Q = p; p += 8 * ld;
+  c->U = p; p += 3 * ld;
+  c->J = p; p += 9 * ld;
+  c->E = p; p += 3 * ld;
+  c->V = p; p += 3 * ld;
+  c->raw = p; p += 6 * ld;
+  cudaError_t e = cudaMemset(c->base, 0, rows * ld * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c->status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->status, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->red, (size_t(kRedBlocks) + 1) * kDiagSlots * sizeof(double));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    vpm_ctx_destroy(c);
+    return set_error(nullptr, VPM_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
+  }
+  c->st = c->own;
+  *out = c;
+  return VPM_OK;
+}
+
+int vpm_ctx_destroy(vpm_ctx* c) {
+  if (!c) return VPM_OK;
+  DeviceGuard dg(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  if (c->own) cudaStreamDestroy(c->own);
+  cudaFree(c->base);
+  cudaFree(c->Ut);
+  cudaFree(c->part);
+  cudaFree(c->status);
+  cudaFree(c->red);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  delete c;
+  return VPM_OK;
+}
+
+int vpm_last_error(const vpm_ctx* c, char* buf, int64_t len) {
+  if (!buf || len <= 0) return VPM_ERR_INVALID;
+  const std::string& m = c ? c->err : g_last_error;
+  std::snprintf(buf, size_t(len), "%s", m.c_str());
+  return VPM_OK;
+}
+
+int vpm_ctx_set_stream(vpm_ctx* c, void* stream) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  DeviceGuard dg(c->device);
+  cudaStreamSynchronize(c->st);
+  c->st = stream ? static_cast<cudaStream_t>(stream) : c->own;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return VPM_OK;
+}
+
+int vpm_get_time(const vpm_ctx* c, double* t, int64_t* nt) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (t) *t = c->t;
+  if (nt) *nt = c->nt;
+  return VPM_OK;
+}
+
+int vpm_set_time(vpm_ctx* c, double t, int64_t nt) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  c->t = t;
+  c->nt = nt;
+  return VPM_OK;
+}
+
+int vpm_set_particles(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double* G,
+                      int64_t sg, const double* S, int64_t ss) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n > c->cap) return ctx_fail(c, VPM_ERR_CAPACITY, "particle count above capacity");
+  int rc = validate_host(c, n, X, sx, G, sg, S, ss);
+  if (rc) return rc;
+  DeviceGuard dg(c->device);
+  rc = upload(c, 0, n, X, sx, G, sg, S, ss);
+  if (rc) return rc;
+  c->n = n;
+  c->n_static = 0;
+  c->uj_lo = c->uj_hi = 0;
+  return VPM_OK;
+}
+
+int vpm_append(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double* G, int64_t sg,
+               const double* S, int64_t ss, int is_static) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0) return ctx_fail(c, VPM_ERR_INVALID, "negative particle count");
+  if (c->n + n > c->cap) return ctx_fail(c, VPM_ERR_CAPACITY, "particle count above capacity");
+  if (!is_static && c->n_static > 0 && n > 0)
+    return ctx_fail(c, VPM_ERR_STATE, "free particles cannot follow static particles");
+  int rc = validate_host(c, n, X, sx, G, sg, S, ss);
+  if (rc) return rc;
+  DeviceGuard dg(c->device);
+  rc = upload(c, c->n, n, X, sx, G, sg, S, ss);
+  if (rc) return rc;
+  c->n += n;
+  if (is_static) c->n_static += n;
+  return VPM_OK;
+}
+
+int vpm_truncate(vpm_ctx* c, int64_t n) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0 || n > c->n) return ctx_fail(c, VPM_ERR_INVALID, "truncate beyond particle count");
+  const int64_t removed = c->n - n;
+  c->n_static = std::max<int64_t>(0, c->n_static - removed);
+  c->n = n;
+  c->uj_hi = std::min(c->uj_hi, n);
+  c->uj_lo = std::min(c->uj_lo, c->uj_hi);
+  return VPM_OK;
+}
+
+int vpm_get_np(const vpm_ctx* c, int64_t* n, int64_t* n_static) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n) *n = c->n;
+  if (n_static) *n_static = c->n_static;
+  return VPM_OK;
+}
+
+int vpm_get_state(vpm_ctx* c, int64_t n, double* X, int64_t sx, double* G, int64_t sg, double* S,
+                  int64_t ss) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0 || n > c->n) return ctx_fail(c, VPM_ERR_INVALID, "range beyond particle count");
+  DeviceGuard dg(c->device);
+  int rc = download_rows(c, c->X, 3, 0, n, X, sx);
+  if (!rc) rc = download_rows(c, c->G, 3, 0, n, G, sg);
+  if (!rc) rc = download_rows(c, c->S, 1, 0, n, S, ss);
+  return rc;
+}
+
+int vpm_get_sfs(vpm_ctx* c, int64_t n, double* C, int64_t sc, double* E, int64_t se) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0 || n > c->n) return ctx_fail(c, VPM_ERR_INVALID, "range beyond particle count");
+  DeviceGuard dg(c->device);
+  int rc = download_rows(c, c->C, 3, 0, n, C, sc);
+  if (!rc) rc = download_rows(c, c->E, 3, 0, n, E, se);
+  return rc;
+}
+
+int vpm_eval_UJ_targets(vpm_ctx* c, int kernel, int precision, int64_t t0, int64_t t1) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (!valid_kernel(kernel)) return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel");
+  if (!valid_prec(precision)) return ctx_fail(c, VPM_ERR_INVALID, "unknown precision");
+  if (t0 < 0 || t1 < t0 || t1 > c->n) return ctx_fail(c, VPM_ERR_INVALID, "bad target range");
+  int rc = check_inject(c);
+  if (rc) return rc;
+  DeviceGuard dg(c->device);
+  c->dry = true;
+  c->part_need = 0;
+  ctx_pair(c, PASS_UJ, kernel, precision, t0, t1, 1.0, nullptr, c->U, c->J);
+  c->dry = false;
+  rc = ensure_part(c, c->part_need);
+  if (rc) return rc;
+  CTX_CK(c, ctx_pair(c, PASS_UJ, kernel, precision, t0, t1, 1.0, nullptr, c->U, c->J));
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  c->uj_lo = t0;
+  c->uj_hi = t1;
+  return VPM_OK;
+}
+
+int vpm_eval_UJ(vpm_ctx* c, int kernel, int precision) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  return vpm_eval_UJ_targets(c, kernel, precision, 0, c->n);
+}
+
+int vpm_get_UJ(vpm_ctx* c, int64_t i0, int64_t n, double* U, int64_t su, double* J, int64_t sj) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0 || i0 < 0) return ctx_fail(c, VPM_ERR_INVALID, "bad range");
+  if (n > 0 && (i0 < c->uj_lo || i0 + n > c->uj_hi))
+    return ctx_fail(c, VPM_ERR_STATE, "range not covered by the last U/J evaluation");
+  DeviceGuard dg(c->device);
+  int rc = download_rows(c, c->U, 3, i0, n, U, su);
+  if (!rc) rc = download_rows(c, c->J, 9, i0, n, J, sj);
+  return rc;
+}
+
+int vpm_eval_sfs(vpm_ctx* c, const vpm_scheme* s) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  int rc = validate_scheme(c, s);
+  if (rc) return rc;
+  if (s->sfs == VPM_SFS_NONE) return ctx_fail(c, VPM_ERR_INVALID, "scheme has no SFS model");
+  rc = check_inject(c);
+  if (rc) return rc;
+  DeviceGuard dg(c->device);
+  if (s->sfs == VPM_SFS_DYNAMIC && (rc = ensure_test_filter(c))) return rc;
+  // Same work as the first stage without the update: run the stage in dry
+  // mode to size scratch, then the SFS part for real.
+  const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
+  const int K = s->kernel, P = s->precision;
+  c->dry = true;
+  c->part_need = 0;
+  enqueue_stage(c, s, 0.0, 0.0, 0.0, 0);
+  c->dry = false;
+  if ((rc = ensure_part(c, c->part_need))) return rc;
+  CTX_CK(c, ctx_pair(c, PASS_UJ, K, P, 0, n, 1.0, nullptr, c->U, c->J));
+  CTX_CK(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
+  CTX_CK(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
+  CTX_CK(c, launch_estr_finish(n, ld, c->raw, c->J, s->transposed, c->E, c->st));
+  if (s->sfs == VPM_SFS_CONSTANT) {
+    CTX_CK(c, launch_sfs_constant(nf, s->sfs_Cd, c->C, c->st));
+  } else {
+    const double al = s->sfs_alpha;
+    CTX_CK(c, ctx_pair(c, PASS_UJ, K, P, 0, n, al, nullptr, c->Ut, c->Jt));
+    CTX_CK(c, launch_stretch_v(n, ld, c->Jt, c->G, s->transposed, c->V, c->st));
+    CTX_CK(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, al, c->V, c->raw, nullptr));
+    CTX_CK(c, launch_estr_finish(n, ld, c->raw, c->Jt, s->transposed, c->Et, c->st));
+    SfsParams sp;
+    sp.alpha = al; sp.rlxf = s->sfs_rlxf; sp.minC = s->sfs_minC; sp.maxC = s->sfs_maxC;
+    sp.zeta0 = zeta0_of(K); sp.transposed = s->transposed;
+    sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
+    CTX_CK(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
+  }
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  c->uj_lo = 0;
+  c->uj_hi = n;
+  return VPM_OK;
+}
+
+int vpm_step(vpm_ctx* c, double dt, const vpm_scheme* s, int64_t nsteps, int use_graph) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  int rc = validate_scheme(c, s);
+  if (rc) return rc;
+  if (!std::isfinite(dt)) return ctx_fail(c, VPM_ERR_INVALID, "non-finite time step");
+  if (nsteps < 0) return ctx_fail(c, VPM_ERR_INVALID, "negative step count");
+  if (nsteps == 0 || c->n == 0) {
+    c->t += dt * double(nsteps);
+    c->nt += nsteps;
+    return VPM_OK;
+  }
+  DeviceGuard dg(c->device);
+  if (s->sfs == VPM_SFS_DYNAMIC && (rc = ensure_test_filter(c))) return rc;
+  c->dry = true;
+  c->part_need = 0;
+  enqueue_step(c, s, dt, s->relaxation != VPM_RELAX_NONE);
+  c->dry = false;
+  if ((rc = ensure_part(c, c->part_need))) return rc;
+
+  for (int64_t k = 0; k < nsteps; ++k) {
+    if ((rc = check_inject(c))) return rc;
+    const int64_t step_no = c->nt + 1;
+    const bool relax = s->relaxation != VPM_RELAX_NONE && s->relax_nsteps >= 1 &&
+                       step_no % s->relax_nsteps == 0;
+    if (use_graph) {
+      GraphKey key;
+      key.n = c->n; key.n_static = c->n_static; key.dt = dt; key.relax = relax;
+      key.scheme = *s;
+      cudaGraphExec_t exec = nullptr;
+      for (auto& g : c->graphs)
+        if (std::memcmp(&g.key, &key, sizeof(key)) == 0) exec = g.exec;
+      if (!exec) {
+        cudaGraph_t graph = nullptr;
+        CTX_CK(c, cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        const int64_t before = c->launches;
+        cudaError_t e = enqueue_step(c, s, dt, relax);
+        const int64_t per_step = c->launches - before;
+        c->launches = before;
+        cudaError_t e2 = cudaStreamEndCapture(c->st, &graph);
+        if (e != cudaSuccess) {
+          if (graph) cudaGraphDestroy(graph);
+          return cuda_fail(c, e, "capturing a step");
+        }
+        CTX_CK(c, e2);
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CTX_CK(c, e);
+        if (c->graphs.size() >= 8) {
+          cudaGraphExecDestroy(c->graphs.front().exec);
+          c->graphs.erase(c->graphs.begin());
+        }
+        GraphEntry ge;
+        std::memset(&ge, 0, sizeof(ge));
+        ge.key = key;
+        ge.exec = exec;
+        ge.kernels = per_step;
+        c->graphs.push_back(ge);
+      }
+      int64_t nk = 0;
+      for (auto& g : c->graphs)
+        if (g.exec == exec) nk = g.kernels;
+      CTX_CK(c, cudaGraphLaunch(exec, c->st));
+      c->launches += nk;
+    } else {
+      CTX_CK(c, enqueue_step(c, s, dt, relax));
+    }
+    c->t += dt;
+    c->nt += 1;
+  }
+  c->uj_lo = 0;
+  c->uj_hi = c->n;
+  return check_status(c);
+}
+
+int vpm_diagnostics(vpm_ctx* c, int kernel, int precision, double* out) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (!out) return ctx_fail(c, VPM_ERR_INVALID, "null output");
+  if (!valid_kernel(kernel) || !valid_prec(precision))
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel or precision");
+  int rc = check_inject(c);
+  if (rc) return rc;
+  DeviceGuard dg(c->device);
+  const int64_t n = c->n, nf = n - c->n_static;
+  for (int k = 0; k < VPM_DIAG_COUNT; ++k) out[k] = 0.0;
+  if (n == 0) return VPM_OK;
+  c->dry = true;
+  c->part_need = 0;
+  ctx_pair(c, PASS_ZETA, kernel, precision, 0, n, 1.0, nullptr, c->raw, nullptr);
+  c->dry = false;
+  if ((rc = ensure_part(c, c->part_need))) return rc;
+  CTX_CK(c, ctx_pair(c, PASS_ZETA, kernel, precision, 0, n, 1.0, nullptr, c->raw, nullptr));
+  double* partial = c->red;
+  double* dout = c->red + size_t(kRedBlocks) * kDiagSlots;
+  CTX_CK(c, launch_diagnostics(n, nf, c->ld, c->X, c->G, c->S, c->C, c->raw, zeta0_of(kernel),
+                               partial, dout, c->st));
+  c->launches += 2;
+  double v[kDiagSlots];
+  CTX_CK(c, cudaMemcpyAsync(v, dout, sizeof v, cudaMemcpyDeviceToHost, c->st));
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  out[VPM_DIAG_ENSTROPHY] = v[DS_ENS];
+  out[VPM_DIAG_IMPULSE_X] = v[DS_IX];
+  out[VPM_DIAG_IMPULSE_Y] = v[DS_IY];
+  out[VPM_DIAG_IMPULSE_Z] = v[DS_IZ];
+  out[VPM_DIAG_GAMMA_X] = v[DS_GX];
+  out[VPM_DIAG_GAMMA_Y] = v[DS_GY];
+  out[VPM_DIAG_GAMMA_Z] = v[DS_GZ];
+  if (v[DS_CCNT] > 0) {
+    const double mean = v[DS_CSUM] / v[DS_CCNT];
+    out[VPM_DIAG_CD_MEAN] = mean;
+    out[VPM_DIAG_CD_STD] = std::sqrt(std::max(0.0, v[DS_CSUM2] / v[DS_CCNT] - mean * mean));
+    out[VPM_DIAG_CD_MIN] = v[DS_CMIN];
+    out[VPM_DIAG_CD_MAX] = v[DS_CMAX];
+  }
+  out[VPM_DIAG_CD_ZERO_RATIO] = nf > 0 ? v[DS_CZERO] / double(nf) : 0.0;
+  out[VPM_DIAG_SIGMA_MEAN] = v[DS_SIG] / double(n);
+  out[VPM_DIAG_NONFINITE] = v[DS_NONFIN];
+  return VPM_OK;
+}
+
+int vpm_centroids(vpm_ctx* c, int nranges, const int64_t* starts, const int64_t* ends,
+                  double* out) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (nranges < 0 || (nranges > 0 && (!starts || !ends || !out)))
+    return ctx_fail(c, VPM_ERR_INVALID, "bad centroid ranges");
+  DeviceGuard dg(c->device);
+  double* partial = c->red;
+  double* dout = c->red + size_t(kRedBlocks) * kDiagSlots;
+  for (int r = 0; r < nranges; ++r) {
+    if (starts[r] < 0 || ends[r] < starts[r] || ends[r] > c->n)
+      return ctx_fail(c, VPM_ERR_INVALID, "centroid range beyond particle count");
+    CTX_CK(c, launch_centroid(starts[r], ends[r], c->ld, c->X, c->G, partial, dout, c->st));
+    double v[kDiagSlots];
+    CTX_CK(c, cudaMemcpyAsync(v, dout, sizeof v, cudaMemcpyDeviceToHost, c->st));
+    CTX_CK(c, cudaStreamSynchronize(c->st));
+    for (int k = 0; k < 3; ++k) out[3 * r + k] = v[3] > 0 ? v[k] / v[3] : 0.0;
+  }
+  return VPM_OK;
+}
+
+int vpm_set_tile(vpm_ctx* c, int kernel, int precision, const vpm_tile* t) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (!valid_kernel(kernel) || !valid_prec(precision))
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel or precision");
+  if (!t || t->block == 0) {  // unpin
+    std::memset(&c->pinned[0][kernel][precision], 0, sizeof(Shape));
+    std::memset(&c->pinned[1][kernel][precision], 0, sizeof(Shape));
+    return VPM_OK;
+  }
+  Shape s{t->block, t->tpt};
+  if (!pair_shape_supported(precision, s))
+    return ctx_fail(c, VPM_ERR_UNSUPPORTED, "tile shape not compiled for this precision");
+  c->pinned[0][kernel][precision] = s;
+  c->pinned[1][kernel][precision] = s;
+  return VPM_OK;
+}
+
+int vpm_autotune(vpm_ctx* c, int kernel, int precision, vpm_tile* chosen, double* ms) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (!valid_kernel(kernel) || !valid_prec(precision))
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel or precision");
+  if (c->n == 0) return ctx_fail(c, VPM_ERR_STATE, "autotune needs particles");
+  DeviceGuard dg(c->device);
+  static const Shape cands[] = {{128, 2}, {128, 4}, {256, 2}, {256, 4}, {128, 1}};
+  Shape best{0, 0};
+  double best_ms = 1e30;
+  cudaEvent_t e0, e1;
+  CTX_CK(c, cudaEventCreate(&e0));
+  CTX_CK(c, cudaEventCreate(&e1));
+  const Shape saved = c->pinned[PASS_UJ][kernel][precision];
+  for (const Shape& s : cands) {
+    if (!pair_shape_supported(precision, s)) continue;
+    c->pinned[PASS_UJ][kernel][precision] = s;
+    c->dry = true;
+    c->part_need = 0;
+    ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J);
+    c->dry = false;
+    int rc = ensure_part(c, c->part_need);
+    if (rc) return rc;
+    CTX_CK(c, ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J));
+    float best_rep = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      CTX_CK(c, cudaEventRecord(e0, c->st));
+      CTX_CK(c, ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J));
+      CTX_CK(c, cudaEventRecord(e1, c->st));
+      CTX_CK(c, cudaEventSynchronize(e1));
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      best_rep = std::min(best_rep, t);
+    }
+    if (best_rep < best_ms) {
+      best_ms = best_rep;
+      best = s;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->pinned[PASS_UJ][kernel][precision] = saved;
+  if (best.block == 0) return ctx_fail(c, VPM_ERR_UNSUPPORTED, "no tile shape compiled");
+  store_shape(c->device, PASS_UJ, kernel, precision, c->n, best);
+  store_shape(c->device, PASS_ZETA, kernel, precision, c->n, best);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  c->uj_lo = 0;
+  c->uj_hi = c->n;
+  if (chosen) {
+    chosen->block = best.block;
+    chosen->tpt = best.tpt;
+    chosen->chunk = 0;
+    chosen->reserved = 0;
+  }
+  if (ms) *ms = best_ms;
+  return VPM_OK;
+}
+
+int vpm_debug_fail_after(vpm_ctx* c, int64_t k) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (k < 0) return ctx_fail(c, VPM_ERR_INVALID, "negative count");
+  c->fail_after = k;
+  return VPM_OK;
+}
+
+int vpm_get_launch_count(const vpm_ctx* c, int64_t* count) {
+  if (!c || !count) return set_error(nullptr, VPM_ERR_INVALID, "null argument");
+  *count = c->launches;
+  return VPM_OK;
+}
+
+const char* vpm_build_info(void) {
+  static char buf[160];
+  std::snprintf(buf, sizeof buf, "libvpmgpu abi=%d arch=sm_103a nvcc=%d.%d", VPM_ABI_VERSION,
+                __CUDACC_VER_MAJOR__, __CUDACC_VER_MINOR__);
+  return buf;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// capi_internal.h — host-side structures shared by capi.cu, batch.cu and device_api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "update.h"
+#include "vpm_device.cuh"
+
+namespace vpm {
+
+extern thread_local std::string g_last_error;
+int set_error(std::string* slot, int code, const std::string& msg);
+int64_t ceil_div(int64_t a, int64_t b);
+int64_t round_up(int64_t a, int64_t b);
+
+// One pair pass over targets [t0, t1) of xt against sources [0, ns).
+struct PairCall {
+  int pass, kernel, prec;
+  int64_t t0, t1, ns;
+  const double *xs, *gs, *ss, *vs;
+  int64_t lds;
+  const double* xt;
+  int64_t ldt;
+  double sigma_scale;
+  double *u, *j;
+  int64_t ldo;
+};
+
+struct PairPlan {
+  Shape shape;
+  int64_t n_tb;
+  int n_chunk;
+  int64_t chunk;
+};
+
+Shape default_shape(int pass, int precision);
+Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n, const Shape* pinned);
+void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s);
+int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int num_sms);
+int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out);
+cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* pinned,
+                     double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
+                     cudaStream_t st, PairPlan* plan_out);
+
+struct GraphKey {
+  int64_t n, n_static;
+  double dt;
+  int64_t relax;
+  vpm_scheme scheme;
+};
+
+struct GraphEntry {
+  GraphKey key;
+  cudaGraphExec_t exec;
+  int64_t kernels;   // kernel nodes of one replay
+};
+
+// Flattened work queue of a batch of independent fields (see batch.cu).
+struct BatchPlan {
+  Shape shape;
+  PairItem* d_items = nullptr;
+  int n_items = 0;
+  int64_t* d_foff = nullptr;
+  int32_t* d_fchunks = nullptr;
+  int nfields = 0;
+  int max_chunks = 1;
+  unsigned int* d_counter = nullptr;
+  int resident = 1;
+  int kernel = -1, precision = -1;   // plan built for this pair
+  std::vector<int64_t> h_off, h_n;   // field offsets and sizes
+};
+
+}  // namespace vpm
+
+struct vpm_ctx {
+  int device = 0;
+  int num_sms = 0;
+  int64_t cap = 0, ld = 0;
+  int64_t n = 0, n_static = 0;
+  double t = 0.0;
+  int64_t nt = 0;
+  cudaStream_t own = nullptr, st = nullptr;
+  double* base = nullptr;
+  double *X = nullptr, *G = nullptr, *S = nullptr, *C = nullptr, *Q = nullptr;
+  double *U = nullptr, *J = nullptr, *E = nullptr, *V = nullptr, *raw = nullptr;
+  double *Ut = nullptr, *Jt = nullptr, *Et = nullptr;
+  double* part = nullptr;
+  size_t part_elems = 0;
+  size_t part_need = 0;
+  bool dry = false;
+  double* red = nullptr;
+  int* status = nullptr;
+  int64_t uj_lo = 0, uj_hi = 0;
+  double* h_stage = nullptr;
+  size_t h_stage_elems = 0;
+  vpm::Shape pinned[2][2][3];
+  std::vector<vpm::GraphEntry> graphs;
+  int64_t fail_after = 0;
+  std::string err;
+  vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
+  int64_t launches = 0;           // kernels enqueued (graph replays add their kernel count)
+  int64_t step_launches = 0;      // kernels of one captured step (counted while enqueuing)
+};
+
+// Pair pass of a context over targets [t0, t1) of its own particles (queue form
+// when the context backs a batch).
+cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int64_t t1,
+                     double scale, const double* vs, double* u, double* j);
+// Build (or rebuild for another kernel/precision) the batch queue.
+int batch_plan(vpm_ctx* c, int kernel, int precision);
+// Host transfer helpers of capi.cu, reused by batches.
+int ctx_validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double* G,
+                      int64_t sg, const double* S, int64_t ss);
+int ctx_upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const double* G,
+               int64_t sg, const double* S, int64_t ss);
+int ctx_download_rows(vpm_ctx* c, const double* dev, int rows, int64_t i0, int64_t n, double* out,
+                      int64_t stride);
+int ctx_prepare_scratch(vpm_ctx* c, int kernel, int precision);

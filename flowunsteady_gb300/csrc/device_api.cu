@@ -1,0 +1,56 @@
+// device_api.cu — stateless U/J on caller-owned device arrays
+// (vpm_uj_device_async), for hosts that keep the particle field in their own
+// CUDA memory (e.g. CUDA.jl arrays passed through ccall).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "capi_internal.h"
+
+using namespace vpm;
+
+extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const double* Xs,
+                                   const double* Gs, const double* Ss, int64_t ld_s, int64_t nt,
+                                   const double* Xt, int64_t ld_t, double* U, double* J,
+                                   int64_t ld_o, void* cuda_stream) {
+  if (kernel != VPM_KERNEL_WINCKELMANS && kernel != VPM_KERNEL_GAUSSIANERF)
+    return set_error(nullptr, VPM_ERR_INVALID, "unknown kernel");
+  if (precision != VPM_PREC_FP64 && precision != VPM_PREC_FP32 && precision != VPM_PREC_FP32C)
+    return set_error(nullptr, VPM_ERR_INVALID, "unknown precision");
+  if (ns < 0 || nt < 0) return set_error(nullptr, VPM_ERR_INVALID, "negative count");
+  if (nt == 0) return VPM_OK;
+  if ((ns > 0 && (!Xs || !Gs || !Ss)) || !U || !J)
+    return set_error(nullptr, VPM_ERR_INVALID, "null device array");
+  if (ld_s < ns || ld_o < nt) return set_error(nullptr, VPM_ERR_INVALID, "leading dimension too small");
+  if (!Xt) {
+    if (nt > ns) return set_error(nullptr, VPM_ERR_INVALID, "targets exceed sources");
+    Xt = Xs;
+    ld_t = ld_s;
+  } else if (ld_t < nt) {
+    return set_error(nullptr, VPM_ERR_INVALID, "leading dimension too small");
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  PairCall pc;
+  pc.pass = PASS_UJ; pc.kernel = kernel; pc.prec = precision;
+  pc.t0 = 0; pc.t1 = nt; pc.ns = ns;
+  pc.xs = Xs; pc.gs = Gs; pc.ss = Ss; pc.vs = nullptr; pc.lds = ld_s;
+  pc.xt = Xt; pc.ldt = ld_t;
+  pc.sigma_scale = 1.0;
+  pc.u = U; pc.j = J; pc.ldo = ld_o;
+  size_t need = 0;
+  run_pair(pc, dev, sms, nullptr, nullptr, nt, 0, &need, true, st, nullptr);
+  double* part = nullptr;
+  if (need > 0) {
+    cudaError_t e = cudaMallocAsync(&part, need * sizeof(double), st);
+    if (e != cudaSuccess) return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate scratch");
+  }
+  cudaError_t e = run_pair(pc, dev, sms, nullptr, part, nt, need, nullptr, false, st, nullptr);
+  if (part) cudaFreeAsync(part, st);
+  if (e != cudaSuccess)
+    return set_error(nullptr, VPM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  return VPM_OK;
+}

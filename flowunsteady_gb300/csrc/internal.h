@@ -1,0 +1,79 @@
+// internal.h — declarations shared by the translation units of libvpmgpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vpm_gpu.h"
+
+namespace vpm {
+
+// Pair passes.
+enum PairPass { PASS_UJ = 0, PASS_ZETA = 1 };
+constexpr int kNvalUJ = 15;    // Uacc(3), Aacc(9), Wacc(3)
+constexpr int kNvalZeta = 6;   // Ω(3) = Σ ζ Γ_q, V(3) = Σ ζ v_q
+
+// One work item: targets [t0, t1) against sources [s0, s1).  slot < 0 means the
+// item covers all sources of its targets and writes final values; otherwise it
+// writes raw sums into partial slot `slot`.
+struct PairItem {
+  int64_t t0, t1, s0, s1;
+  int32_t slot;
+  int32_t field;
+};
+
+struct PairArgs {
+  // Sources: FP64 SoA rows of leading dimension lds.
+  const double* xs;
+  const double* gs;
+  const double* ss;
+  const double* vs;   // PASS_ZETA: per-source S(J_q, Γ_q), 3 rows (may be null)
+  int64_t lds;
+  // Target positions: FP64 SoA of leading dimension ldt.
+  const double* xt;
+  int64_t ldt;
+  double sigma_scale;
+  // Decomposition without a table: targets [t_off, t_off+nt) x sources [0, ns).
+  int64_t t_off, nt, ns, chunk;
+  int32_t n_tb, n_chunk;
+  // Decomposition from a table (batches): n_items entries, dynamic queue when
+  // counter != null.
+  const PairItem* items;
+  int32_t n_items;
+  unsigned int* counter;
+  // Outputs.  Final: UJ -> U rows 0..2 of `u` (ld ldo), J rows 0..8 of `j`;
+  // ZETA -> raw Ω, V rows 0..5 of `u`.  Partials: part[(slot*nval + k)*ldp + i].
+  double* u;
+  double* j;
+  int64_t ldo;
+  double* part;
+  int64_t ldp;
+};
+
+// Tile shape of a launch.
+struct Shape {
+  int block;   // threads per CTA
+  int tpt;     // targets per thread
+};
+
+// Launch one pair pass (grid chosen by the caller through args/n_items).
+cudaError_t launch_pair(int pass, int kernel, int precision, Shape shape, const PairArgs& a,
+                        int grid, cudaStream_t st);
+// Dynamic shared memory of a shape (bytes).
+size_t pair_smem_bytes(int pass, int precision, Shape shape);
+// Max resident CTAs per SM of a shape.
+int pair_ctas_per_sm(int pass, int kernel, int precision, Shape shape);
+// Whether a shape is compiled.
+bool pair_shape_supported(int precision, Shape shape);
+
+// Sum partial slots in fixed order and write the final values.
+//   UJ: U = -Uacc/(4π), J = -(Aacc·KP + ε·Wacc)/(4π); ZETA: raw sums.
+// Targets are [t_begin, t_end); the slot count of target i is scalar_chunks
+// when foff is null, else found from the device field table (foff[f] <= i,
+// fchunks[f]); targets whose count is 1 are skipped (already final).
+cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
+                          const int64_t* foff, const int32_t* fchunks, int nfields,
+                          int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
+                          double* j, int64_t ldo, cudaStream_t st);
+
+}  // namespace vpm

@@ -1,0 +1,406 @@
+"""FLOWVPM-shaped host API over libvpmgpu.so.
+
+The names follow the FLOWVPM symbols that FLOWUnsteady passes around
+(src/FLOWUnsteady_simulation.jl:107-253 of byuflowlab/FLOWUnsteady):
+
+    pfield = ParticleField(max_particles; formulation=rVPM, viscous=Inviscid(),
+                           kernel=gaussianerf, UJ=UJ_gpu, SFS=noSFS,
+                           integration=rungekutta3, transposed=True,
+                           relaxation=norelaxation, Uinf=...)
+    add_particle(pfield, X, Gamma, sigma; static=False)     (:455-489, :572)
+    remove_particle(pfield, i)            (tail removal,     :360-365, :550-552)
+    get_np(pfield)
+    pfield.UJ(pfield)                     (probe / force evaluation, :544)
+    nextstep(pfield, dt; relax=False)     (:358)
+    monitor_enstrophy(pfield), monitor_Cd(pfield)   (src/FLOWUnsteady_monitors.jl:614,697)
+
+Everything computes on the GPU through the C ABI; particle data lives in
+device memory owned by the library.  Appends are buffered on the host and
+uploaded before the next device call.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+# ------------------------------------------------------------------ kernels --
+
+
+@dataclass(frozen=True)
+class Kernel:
+    """Regularising kernel (FLOWVPM's vpm.Kernel)."""
+    name: str
+    id: int
+
+    def zeta0(self) -> float:
+        return 15.0 / (8.0 * np.pi) if self.id == L.KERNEL_WINCKELMANS else (2 * np.pi) ** -1.5
+
+
+winckelmans = Kernel("winckelmans", L.KERNEL_WINCKELMANS)
+gaussianerf = Kernel("gaussianerf", L.KERNEL_GAUSSIANERF)
+
+# -------------------------------------------------------------- formulation --
+
+
+@dataclass(frozen=True)
+class Formulation:
+    """rVPM constants f, g (docs/src/theory/rvpm.md:196-237)."""
+    f: float
+    g: float
+
+
+rVPM = Formulation(0.0, 0.2)
+cVPM = Formulation(0.0, 0.0)
+
+# ------------------------------------------------------------------ viscous --
+
+
+@dataclass
+class Inviscid:
+    nu: float = 0.0
+
+
+@dataclass
+class CoreSpreading:
+    """Viscous core spreading d(σ²)/dt = 2ν (vpm.CoreSpreading(nu, sgm0, zeta)).
+
+    The RBF re-initialisation when σ outgrows beta·sgm0 is not provided."""
+    nu: float
+    sgm0: Optional[float] = None
+    beta: float = 1.5
+
+
+# ---------------------------------------------------------------------- SFS --
+
+
+@dataclass
+class NoSFS:
+    pass
+
+
+noSFS = NoSFS()
+SFS_none = noSFS
+
+
+def Estr_direct():
+    """Marker of the direct E_str pair pass (vpm.Estr_direct)."""
+    return "Estr_direct"
+
+
+clipping_backscatter = "clipping_backscatter"
+pseudo3level = "pseudo3level"
+pseudo3level_positive = "pseudo3level_positive"
+
+
+@dataclass
+class DynamicSFS:
+    """vpm.DynamicSFS(Estr_direct, procedure; alpha, rlxf, minC, maxC, clippings)."""
+    model: object = Estr_direct
+    procedure: str = pseudo3level_positive
+    alpha: float = 0.999
+    rlxf: float = 1.0
+    minC: float = 0.0
+    maxC: float = 1.0
+    clippings: Sequence[str] = (clipping_backscatter,)
+
+
+@dataclass
+class ConstantSFS:
+    """E_str with a prescribed coefficient C_d."""
+    Cd: float
+    clippings: Sequence[str] = (clipping_backscatter,)
+
+
+# -------------------------------------------------------------- integration --
+euler = "euler"
+rungekutta3 = "rungekutta3"
+
+
+@dataclass
+class Relaxation:
+    """Pedrizzetti relaxation (vpm.pedrizzetti): factor rlxf every nsteps_relax steps."""
+    rlxf: float = 0.3
+    nsteps_relax: int = 1
+
+
+norelaxation = None
+pedrizzetti = Relaxation()
+
+# ----------------------------------------------------------------------- UJ --
+
+
+def _uj(precision: int) -> Callable:
+    def UJ(pfield: "ParticleField"):
+        pfield._flush()
+        L.check(L.lib().vpm_eval_UJ(pfield._ctx, pfield.kernel.id, precision), pfield._ctx)
+        pfield._uj_valid = True
+    UJ.precision = precision
+    return UJ
+
+
+UJ_direct = _uj(L.PREC_FP64)         # plain FP64 direct sum (the parity form)
+UJ_gpu = _uj(L.PREC_FP32C)           # FP32 tile-relative compensated direct sum
+UJ_gpu_fp32 = _uj(L.PREC_FP32)       # naive FP32 (precision studies only)
+
+# -------------------------------------------------------------- the field --
+
+
+class ParticleField:
+    """Device-resident particle field (FLOWVPM's vpm.ParticleField)."""
+
+    def __init__(self, maxparticles: int, *, formulation: Formulation = rVPM,
+                 viscous=None, kernel: Kernel = gaussianerf, UJ: Callable = UJ_gpu,
+                 SFS=noSFS, integration: str = rungekutta3, transposed: bool = True,
+                 relaxation: Optional[Relaxation] = norelaxation,
+                 Uinf: Sequence[float] = (0.0, 0.0, 0.0), device: int = 0):
+        self.maxparticles = int(maxparticles)
+        self.formulation = formulation
+        self.viscous = viscous if viscous is not None else Inviscid()
+        self.kernel = kernel
+        self.UJ = UJ
+        self.SFS = SFS
+        self.integration = integration
+        self.transposed = transposed
+        self.relaxation = relaxation
+        self.Uinf = tuple(float(u) for u in Uinf)
+        ptr = ctypes.c_void_p()
+        L.check(L.lib().vpm_ctx_create(int(device), self.maxparticles, ctypes.byref(ptr)))
+        self._ctx = ptr
+        self._pend: List[tuple] = []
+        self._uj_valid = False
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_ctx", None):
+            L.lib().vpm_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- scheme
+    def scheme(self, precision: Optional[int] = None) -> L.Scheme:
+        s = L.default_scheme()
+        s.kernel = self.kernel.id
+        s.precision = getattr(self.UJ, "precision", L.PREC_FP32C) if precision is None else precision
+        s.integration = L.INTEGRATION_RK3 if self.integration == rungekutta3 else L.INTEGRATION_EULER
+        s.transposed = 1 if self.transposed else 0
+        s.f, s.g = self.formulation.f, self.formulation.g
+        for k in range(3):
+            s.uinf[k] = self.Uinf[k]
+        s.nu = float(getattr(self.viscous, "nu", 0.0) or 0.0)
+        if isinstance(self.SFS, DynamicSFS):
+            s.sfs = L.SFS_DYNAMIC
+            s.sfs_alpha, s.sfs_rlxf = self.SFS.alpha, self.SFS.rlxf
+            s.sfs_minC, s.sfs_maxC = self.SFS.minC, self.SFS.maxC
+            flags = L.SFS_CLIP_BACKSCATTER if clipping_backscatter in self.SFS.clippings else 0
+            if self.SFS.procedure == pseudo3level_positive:
+                flags |= L.SFS_FORCE_POSITIVE
+            s.sfs_flags = flags
+        elif isinstance(self.SFS, ConstantSFS):
+            s.sfs = L.SFS_CONSTANT
+            s.sfs_Cd = self.SFS.Cd
+            s.sfs_flags = L.SFS_CLIP_BACKSCATTER if clipping_backscatter in self.SFS.clippings else 0
+        else:
+            s.sfs = L.SFS_NONE
+        if self.relaxation is not None:
+            s.relaxation = L.RELAX_PEDRIZZETTI
+            s.relax_factor = self.relaxation.rlxf
+            s.relax_nsteps = self.relaxation.nsteps_relax
+        return s
+
+    # -- particles
+    def _flush(self):
+        if not self._pend:
+            return
+        groups = []
+        for X, G, S, static in self._pend:
+            if groups and groups[-1][3] == static:
+                groups[-1][0].append(X); groups[-1][1].append(G); groups[-1][2].append(S)
+            else:
+                groups.append(([X], [G], [S], static))
+        self._pend = []
+        for Xs, Gs, Ss, static in groups:
+            X = np.ascontiguousarray(np.concatenate(Xs), dtype=np.float64)
+            G = np.ascontiguousarray(np.concatenate(Gs), dtype=np.float64)
+            S = np.ascontiguousarray(np.concatenate(Ss), dtype=np.float64)
+            L.check(L.lib().vpm_append(self._ctx, X.shape[0], L.dptr(X), 3, L.dptr(G), 3,
+                                       L.dptr(S), 1, 1 if static else 0), self._ctx)
+        self._uj_valid = False
+
+    def set_particles(self, X, Gamma, sigma):
+        self._pend = []
+        X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, 3)
+        G = np.ascontiguousarray(Gamma, dtype=np.float64).reshape(-1, 3)
+        S = np.ascontiguousarray(sigma, dtype=np.float64).reshape(-1)
+        L.check(L.lib().vpm_set_particles(self._ctx, X.shape[0], L.dptr(X), 3, L.dptr(G), 3,
+                                          L.dptr(S), 1), self._ctx)
+        self._uj_valid = False
+
+    def get_np(self) -> int:
+        self._flush()
+        n = ctypes.c_int64()
+        ns = ctypes.c_int64()
+        L.check(L.lib().vpm_get_np(self._ctx, ctypes.byref(n), ctypes.byref(ns)), self._ctx)
+        return int(n.value)
+
+    def get_nstatic(self) -> int:
+        self._flush()
+        n = ctypes.c_int64()
+        ns = ctypes.c_int64()
+        L.check(L.lib().vpm_get_np(self._ctx, ctypes.byref(n), ctypes.byref(ns)), self._ctx)
+        return int(ns.value)
+
+    def state(self):
+        """(X, Gamma, sigma) of every particle as host arrays."""
+        n = self.get_np()
+        X, G, S = np.empty((n, 3)), np.empty((n, 3)), np.empty(n)
+        L.check(L.lib().vpm_get_state(self._ctx, n, L.dptr(X), 3, L.dptr(G), 3, L.dptr(S), 1),
+                self._ctx)
+        return X, G, S
+
+    def get_X(self):
+        return self.state()[0]
+
+    def get_Gamma(self):
+        return self.state()[1]
+
+    def get_sigma(self):
+        return self.state()[2]
+
+    def get_UJ(self, i0: int = 0, n: Optional[int] = None):
+        """U (n,3) and J (n,3,3) of particles [i0, i0+n) from the last evaluation."""
+        if n is None:
+            n = self.get_np() - i0
+        U, J = np.empty((n, 3)), np.empty((n, 3, 3))
+        L.check(L.lib().vpm_get_UJ(self._ctx, i0, n, L.dptr(U), 3, L.dptr(J), 9), self._ctx)
+        return U, J
+
+    def get_U(self):
+        return self.get_UJ()[0]
+
+    def get_J(self):
+        return self.get_UJ()[1]
+
+    def get_C(self):
+        n = self.get_np()
+        C, E = np.empty((n, 3)), np.empty((n, 3))
+        L.check(L.lib().vpm_get_sfs(self._ctx, n, L.dptr(C), 3, L.dptr(E), 3), self._ctx)
+        return C
+
+    def get_SFS(self):
+        n = self.get_np()
+        C, E = np.empty((n, 3)), np.empty((n, 3))
+        L.check(L.lib().vpm_get_sfs(self._ctx, n, L.dptr(C), 3, L.dptr(E), 3), self._ctx)
+        return E
+
+    @property
+    def t(self) -> float:
+        t = ctypes.c_double()
+        nt = ctypes.c_int64()
+        L.check(L.lib().vpm_get_time(self._ctx, ctypes.byref(t), ctypes.byref(nt)), self._ctx)
+        return t.value
+
+    @property
+    def nt(self) -> int:
+        t = ctypes.c_double()
+        nt = ctypes.c_int64()
+        L.check(L.lib().vpm_get_time(self._ctx, ctypes.byref(t), ctypes.byref(nt)), self._ctx)
+        return int(nt.value)
+
+    def eval_UJ_targets(self, t0: int, t1: int, precision: Optional[int] = None):
+        """U/J at particles [t0, t1) only (probe evaluation)."""
+        self._flush()
+        prec = getattr(self.UJ, "precision", L.PREC_FP32C) if precision is None else precision
+        L.check(L.lib().vpm_eval_UJ_targets(self._ctx, self.kernel.id, prec, t0, t1), self._ctx)
+
+    def diagnostics(self, precision: Optional[int] = None) -> dict:
+        self._flush()
+        prec = getattr(self.UJ, "precision", L.PREC_FP32C) if precision is None else precision
+        out = np.zeros(L.DIAG_COUNT)
+        L.check(L.lib().vpm_diagnostics(self._ctx, self.kernel.id, prec, L.dptr(out)), self._ctx)
+        return dict(zip(L.DIAG_NAMES, out.tolist()))
+
+    def centroids(self, ranges):
+        self._flush()
+        st = (ctypes.c_int64 * len(ranges))(*[r[0] for r in ranges])
+        en = (ctypes.c_int64 * len(ranges))(*[r[1] for r in ranges])
+        out = np.zeros((len(ranges), 3))
+        L.check(L.lib().vpm_centroids(self._ctx, len(ranges), st, en, L.dptr(out)), self._ctx)
+        return out
+
+
+def add_particle(pfield: ParticleField, X, Gamma, sigma, *, static: bool = False):
+    """Append one particle or an (n,3)/(n,3)/(n,) batch (vpm.add_particle)."""
+    X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    G = np.asarray(Gamma, dtype=np.float64).reshape(-1, 3)
+    S = np.broadcast_to(np.asarray(sigma, dtype=np.float64).reshape(-1), (X.shape[0],))
+    pfield._pend.append((X, G, np.array(S), bool(static)))
+
+
+def add_probe(pfield: ParticleField, X):
+    """Probe particle: Γ = 0, σ = 1e-6, static (add_probe, src/FLOWUnsteady_simulation.jl:572)."""
+    X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    add_particle(pfield, X, np.zeros_like(X), 1e-6, static=True)
+
+
+def remove_particle(pfield: ParticleField, i: int):
+    """Remove particle i (0-based); only the last particle can be removed."""
+    n = pfield.get_np()
+    if i != n - 1:
+        raise ValueError("only tail removal is supported (FLOWUnsteady removes from the tail)")
+    L.check(L.lib().vpm_truncate(pfield._ctx, n - 1), pfield._ctx)
+
+
+def get_np(pfield: ParticleField) -> int:
+    return pfield.get_np()
+
+
+def nextstep(pfield: ParticleField, dt: float, *, relax: bool = False, nsteps: int = 1,
+             use_graph: bool = True):
+    """Advance the free particles by nsteps steps (vpm.nextstep)."""
+    pfield._flush()
+    s = pfield.scheme()
+    if not relax:
+        s.relaxation = L.RELAX_NONE
+    L.check(L.lib().vpm_step(pfield._ctx, float(dt), ctypes.byref(s), int(nsteps),
+                             1 if use_graph else 0), pfield._ctx)
+
+
+def Vvpm_on_Xs(pfield: ParticleField, Xs) -> np.ndarray:
+    """Velocity of the field at points Xs: probes appended, U/J evaluated at the
+    probes only, probes removed (Vvpm_on_Xs, src/FLOWUnsteady_simulation.jl:494-570)."""
+    Xs = np.asarray(Xs, dtype=np.float64).reshape(-1, 3)
+    if Xs.shape[0] == 0:
+        return np.zeros((0, 3))
+    n0 = pfield.get_np()
+    add_probe(pfield, Xs)
+    pfield.eval_UJ_targets(n0, n0 + Xs.shape[0])
+    U, _ = pfield.get_UJ(n0, Xs.shape[0])
+    L.check(L.lib().vpm_truncate(pfield._ctx, n0), pfield._ctx)
+    return U
+
+
+def monitor_enstrophy(pfield: ParticleField) -> float:
+    """½ Σ Γ_p·ω(x_p) (src/FLOWUnsteady_monitors.jl:573-574)."""
+    return pfield.diagnostics()["enstrophy"]
+
+
+def monitor_Cd(pfield: ParticleField) -> dict:
+    d = pfield.diagnostics()
+    return {k: d[k] for k in ("cd_mean", "cd_std", "cd_zero_ratio", "cd_min", "cd_max")}
+
+
+def measure_fma_peaks(device: int = 0):
+    f32, f64, mhz = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    L.check(L.lib().vpm_measure_fma_peaks(device, ctypes.byref(f32), ctypes.byref(f64),
+                                          ctypes.byref(mhz)))
+    return f32.value, f64.value, mhz.value

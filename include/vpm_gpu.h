@@ -1,0 +1,300 @@
+/*
+ * vpm_gpu.h — C ABI of libvpmgpu.so, a GB300 (sm_103a) implementation of the
+ * reformulated vortex particle method (rVPM) particle-field evaluation that
+ * FLOWUnsteady drives through FLOWVPM:
+ *
+ *   - all-pairs regularised Biot–Savart velocity U and gradient J = ∇U
+ *     (FLOWVPM's UJ_direct, Winckelmans and Gaussian-erf kernels),
+ *   - the stretching term and the dynamic subfilter-scale (SFS) pass,
+ *   - the low-storage RK3 (or Euler) update of x, Γ and σ with viscous core
+ *     spreading,
+ *   - FP64 diagnostics (enstrophy, impulse, centroids, C_d statistics).
+ *
+ * Reference interface this replaces (paths inside byuflowlab/FLOWUnsteady):
+ *   run_simulation(...; vpm_UJ=..., vpm_kernel=..., vpm_SFS=..., vpm_integration=...,
+ *                  vpm_transposed=..., vpm_viscous=...)      src/FLOWUnsteady_simulation.jl:107-191
+ *   vpm.ParticleField(max_particles; UJ=vpm_UJ, kernel=..., SFS=..., ...)
+ *                                                              src/FLOWUnsteady_simulation.jl:239-244
+ *   pfield.UJ(pfield)   (probe evaluation)                     src/FLOWUnsteady_simulation.jl:544
+ *   pfield.UJ(pfield)   (vortex-sheet forces)                  src/FLOWUnsteady_processing_force.jl:238
+ *   vpm.nextstep(pfield, dt; relax, custom_UJ)                 src/FLOWUnsteady_simulation.jl:358
+ *   vpm.monitor_enstrophy / vpm.monitor_Cd                      src/FLOWUnsteady_monitors.jl:614,697
+ *
+ * Conventions
+ *   - Every call returns an int status: VPM_OK (0) or a negative VPM_ERR_* code.
+ *     vpm_last_error() gives the message of the last failing call on a context.
+ *   - Host arrays are strided "array of structs": component k of particle i sits at
+ *     ptr[i*stride + k], with a stride per array.  stride = 3 for an (n,3)
+ *     row-major array and 1 for an (n,) array; Julia's FLOWVPM particle matrix
+ *     (one column per particle) is passed with every stride = number of rows and
+ *     each pointer offset to its row.
+ *   - J is row-major per particle: J[i*stride + 3*a + b] = dU_a/dx_b.
+ *   - The caller owns host memory; the library never retains a host pointer.
+ *     The library owns device memory.  There are no callbacks.
+ *   - A context is thread-compatible (one host thread at a time).  All work is
+ *     issued on the context's stream; calls are synchronous at the ABI unless the
+ *     name ends in _async.
+ *   - Pair sums skip coincident pairs (r == 0), as FLOWVPM's direct sums do
+ *     (src/FLOWUnsteady_processing_force.jl:895); pair counts in throughput
+ *     figures still count N_targets x N_sources.
+ */
+#ifndef VPM_GPU_H
+#define VPM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VPM_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status -- */
+enum {
+  VPM_OK = 0,
+  VPM_ERR_INVALID = -1,      /* bad argument (null pointer, bad enum, n < 0, ...) */
+  VPM_ERR_CAPACITY = -2,     /* particle count above the context's capacity      */
+  VPM_ERR_CUDA = -3,         /* CUDA runtime error                               */
+  VPM_ERR_NONFINITE = -4,    /* NaN/Inf in an input or in the evolved state      */
+  VPM_ERR_NOMEM = -5,        /* device allocation failed                         */
+  VPM_ERR_UNSUPPORTED = -6,  /* e.g. core spreading with a non-Gaussian kernel   */
+  VPM_ERR_STATE = -7,        /* call out of order (e.g. get_UJ before eval)      */
+  VPM_ERR_INJECTED = -8      /* host-side fault-injection hook fired             */
+};
+
+/* --------------------------------------------------------------- choices -- */
+/* Regularising kernels (FLOWVPM's vpm.winckelmans / vpm.gaussianerf,
+ * src/FLOWUnsteady_simulation.jl:128). */
+enum { VPM_KERNEL_WINCKELMANS = 0, VPM_KERNEL_GAUSSIANERF = 1 };
+
+/* Arithmetic of the O(N^2) pair passes.  State, updates and reductions are
+ * always FP64. */
+enum {
+  VPM_PREC_FP64 = 0,   /* plain FP64 pair sum (the parity form)                    */
+  VPM_PREC_FP32 = 1,   /* naive FP32: absolute coordinates, one FP32 accumulator   */
+  VPM_PREC_FP32C = 2   /* FP32 on tile-relative coordinates, per-tile FP32 partial  *
+                        * sums folded into FP64 accumulators (compensated)          */
+};
+
+/* Time integration (FLOWVPM's vpm.euler / vpm.rungekutta3,
+ * src/FLOWUnsteady_simulation.jl:131). */
+enum { VPM_INTEGRATION_EULER = 0, VPM_INTEGRATION_RK3 = 1 };
+
+/* Subfilter-scale model (FLOWVPM's vpm.SFS_none / vpm.DynamicSFS(vpm.Estr_direct, ...)). */
+enum {
+  VPM_SFS_NONE = 0,
+  VPM_SFS_DYNAMIC = 1,   /* E_str pair pass + pseudo-three-level dynamic C_d          */
+  VPM_SFS_CONSTANT = 2   /* E_str pair pass with a prescribed C_d (sfs_Cd)            */
+};
+
+/* sfs_flags bits */
+#define VPM_SFS_CLIP_BACKSCATTER 1u   /* vpm.clipping_backscatter: C_d = 0 where C_d Γ·E_str < 0 */
+#define VPM_SFS_FORCE_POSITIVE 2u     /* the "_positive" procedure: C_d = |C_d|                    */
+
+/* Relaxation of Γ towards the local vorticity (FLOWVPM's vpm.pedrizzetti). */
+enum { VPM_RELAX_NONE = 0, VPM_RELAX_PEDRIZZETTI = 1 };
+
+/* The scheme of one time step.  Fill with vpm_scheme_default() and edit. */
+typedef struct vpm_scheme {
+  int32_t kernel;        /* VPM_KERNEL_*                                            */
+  int32_t precision;     /* VPM_PREC_* used by every pair pass of the step          */
+  int32_t integration;   /* VPM_INTEGRATION_*                                       */
+  int32_t transposed;    /* 1: S = (Γ·∇ᵀ)u = Jᵀ Γ (FLOWUnsteady default), 0: S = J Γ */
+  double f;              /* rVPM formulation constants: rVPM f=0, g=1/5; cVPM f=g=0 */
+  double g;
+  double uinf[3];        /* freestream velocity added to dx/dt                      */
+  double nu;             /* core-spreading viscosity, d(σ²)/dt = 2ν; 0 = inviscid   */
+  int32_t sfs;           /* VPM_SFS_*                                               */
+  uint32_t sfs_flags;    /* VPM_SFS_CLIP_BACKSCATTER | VPM_SFS_FORCE_POSITIVE       */
+  double sfs_alpha;      /* test-filter ratio of the dynamic procedure (0.999)      */
+  double sfs_rlxf;       /* Lagrangian-average relaxation factor (1 = no averaging) */
+  double sfs_minC;       /* |C_d| floor (0 = none)                                  */
+  double sfs_maxC;       /* |C_d| ceiling (0 = none)                                */
+  double sfs_Cd;         /* prescribed coefficient for VPM_SFS_CONSTANT             */
+  int32_t relaxation;    /* VPM_RELAX_*                                             */
+  int32_t relax_nsteps;  /* relax every this many steps                             */
+  double relax_factor;   /* Pedrizzetti relaxation factor                           */
+} vpm_scheme;
+
+/* Defaults: Gaussian-erf, FP32C, RK3, transposed, rVPM (f=0, g=1/5), inviscid,
+ * no SFS (alpha=0.999, rlxf=1, minC=0, maxC=1 preset for the dynamic model),
+ * no relaxation. */
+void vpm_scheme_default(vpm_scheme* s);
+
+/* ----------------------------------------------------------- diagnostics -- */
+/* vpm_diagnostics() output layout (all FP64). */
+enum {
+  VPM_DIAG_ENSTROPHY = 0,   /* ½ Σ_p Γ_p·ω(x_p), ω(x) = Σ_q Γ_q ζ_σq(x − x_q) (incl. self) */
+  VPM_DIAG_IMPULSE_X = 1,   /* ½ Σ_p x_p × Γ_p                                               */
+  VPM_DIAG_IMPULSE_Y = 2,
+  VPM_DIAG_IMPULSE_Z = 3,
+  VPM_DIAG_GAMMA_X = 4,     /* Σ_p Γ_p                                                       */
+  VPM_DIAG_GAMMA_Y = 5,
+  VPM_DIAG_GAMMA_Z = 6,
+  VPM_DIAG_CD_MEAN = 7,     /* C_d statistics over particles with C_d != 0 (vpm.monitor_Cd) */
+  VPM_DIAG_CD_STD = 8,
+  VPM_DIAG_CD_ZERO_RATIO = 9,
+  VPM_DIAG_CD_MIN = 10,
+  VPM_DIAG_CD_MAX = 11,
+  VPM_DIAG_SIGMA_MEAN = 12,
+  VPM_DIAG_NONFINITE = 13,  /* number of particles whose state holds a NaN/Inf            */
+  VPM_DIAG_COUNT = 14
+};
+
+/* --------------------------------------------------------------- context -- */
+typedef struct vpm_ctx vpm_ctx;
+
+/* Create a context on CUDA device `device` holding up to `capacity` particles.
+ * Replaces vpm.ParticleField(max_particles, Float64; ...)
+ * (src/FLOWUnsteady_simulation.jl:239-244): the device SoA buffers, the stream,
+ * the CUDA graphs and the tile-shape choices live here. */
+int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out);
+int vpm_ctx_destroy(vpm_ctx* ctx);
+
+/* Copy the message of the last error on `ctx` (or the last global error when
+ * ctx is NULL) into buf (NUL-terminated, at most len bytes). */
+int vpm_last_error(const vpm_ctx* ctx, char* buf, int64_t len);
+
+/* Issue the context's work on a caller-owned cudaStream_t (NULL restores the
+ * context's own stream).  The stream must belong to the context's device. */
+int vpm_ctx_set_stream(vpm_ctx* ctx, void* cuda_stream);
+
+/* Simulation time and step counter (pfield.t, pfield.nt). */
+int vpm_get_time(const vpm_ctx* ctx, double* t, int64_t* nt);
+int vpm_set_time(vpm_ctx* ctx, double t, int64_t nt);
+
+/* ------------------------------------------------------------ particles -- */
+/* Replace the particle set with n particles from host arrays: component k of
+ * particle i is X[i*stride_x + k], Gamma[i*stride_g + k], sigma[i*stride_s].
+ * SFS memory (C_d and its Lagrangian averages) of every particle is reset to 0.
+ * Rejects n > capacity (VPM_ERR_CAPACITY), σ <= 0 (VPM_ERR_INVALID) and
+ * non-finite values (VPM_ERR_NONFINITE) without touching the state.
+ * Replaces the vpm.add_particle loop that fills a ParticleField. */
+int vpm_set_particles(vpm_ctx* ctx, int64_t n, const double* X, int64_t stride_x,
+                      const double* Gamma, int64_t stride_g, const double* sigma,
+                      int64_t stride_s);
+
+/* Append n particles at the tail (vpm.add_particle, src/FLOWUnsteady_simulation.jl:455-489,
+ * and add_probe, :572).  The appended particles are counted as static (sources
+ * only, not advanced by vpm_step) when is_static != 0.  Static particles must
+ * stay at the tail: appending a free particle after a static one is VPM_ERR_STATE. */
+int vpm_append(vpm_ctx* ctx, int64_t n, const double* X, int64_t stride_x, const double* Gamma,
+               int64_t stride_g, const double* sigma, int64_t stride_s, int is_static);
+
+/* Keep the first n particles (vpm.remove_particle from the tail,
+ * src/FLOWUnsteady_simulation.jl:360-365, :550-552). */
+int vpm_truncate(vpm_ctx* ctx, int64_t n);
+
+/* Number of particles (vpm.get_np) and of static particles at the tail. */
+int vpm_get_np(const vpm_ctx* ctx, int64_t* n, int64_t* n_static);
+
+/* Download the state of the first n particles (any pointer may be NULL). */
+int vpm_get_state(vpm_ctx* ctx, int64_t n, double* X, int64_t stride_x, double* Gamma,
+                  int64_t stride_g, double* sigma, int64_t stride_s);
+
+/* Download SFS memory: C (C_d, ⟨Γ·L⟩, ⟨Γ·m⟩) with stride_c, and E_str with stride_e
+ * (either may be NULL). */
+int vpm_get_sfs(vpm_ctx* ctx, int64_t n, double* C, int64_t stride_c, double* Estr,
+                int64_t stride_e);
+
+/* --------------------------------------------------------------- compute -- */
+/* U and J at every particle from every particle (pfield.UJ(pfield) with
+ * vpm.UJ_direct, src/FLOWUnsteady_simulation.jl:544).  Results stay on the
+ * device until vpm_get_UJ. */
+int vpm_eval_UJ(vpm_ctx* ctx, int kernel, int precision);
+
+/* U and J at the targets [t0, t1) only, from all particles (the probe form of
+ * Vvpm_on_Xs, src/FLOWUnsteady_simulation.jl:494-570). */
+int vpm_eval_UJ_targets(vpm_ctx* ctx, int kernel, int precision, int64_t t0, int64_t t1);
+
+/* Download U (stride_u) and J (stride_j) of particles [i0, i0+n) from the last
+ * evaluation (either pointer may be NULL).  The range must lie inside the
+ * targets of the last vpm_eval_UJ / vpm_eval_UJ_targets / vpm_step. */
+int vpm_get_UJ(vpm_ctx* ctx, int64_t i0, int64_t n, double* U, int64_t stride_u, double* J,
+               int64_t stride_j);
+
+/* SFS pass on the current state: U/J, E_str and (for VPM_SFS_DYNAMIC) the
+ * dynamic coefficient with its clippings, as the first stage of a step does. */
+int vpm_eval_sfs(vpm_ctx* ctx, const vpm_scheme* s);
+
+/* Advance the free particles by `nsteps` time steps of size dt
+ * (vpm.nextstep, src/FLOWUnsteady_simulation.jl:358).  Static particles act as
+ * sources but are not advanced.  When use_graph != 0 each step is a replay of
+ * one CUDA graph captured on first use for this (n, scheme). */
+int vpm_step(vpm_ctx* ctx, double dt, const vpm_scheme* s, int64_t nsteps, int use_graph);
+
+/* FP64 diagnostics of the current state into out[VPM_DIAG_COUNT]
+ * (vpm.monitor_enstrophy, vpm.monitor_Cd).  The enstrophy pair pass uses the
+ * given kernel and precision. */
+int vpm_diagnostics(vpm_ctx* ctx, int kernel, int precision, double* out);
+
+/* Σ|Γ|-weighted centroids of index ranges: for r in [0, nranges) particles
+ * [starts[r], ends[r]) -> centroid out[3r..3r+2]. */
+int vpm_centroids(vpm_ctx* ctx, int nranges, const int64_t* starts, const int64_t* ends,
+                  double* out);
+
+/* ------------------------------------------------------- device pointers -- */
+/* Stateless U/J on caller-owned device memory (for callers that hold the
+ * particle field in their own CUDA arrays, e.g. CUDA.jl CuArrays).  Device
+ * arrays are SoA: X[k*ld + i], k = 0..2; J[(3a+b)*ld + i].  Targets are the
+ * sources [0, nt) when Xt == NULL.  Runs on `cuda_stream` (NULL = legacy
+ * default stream) and returns after the work is enqueued. Scratch, if the
+ * launch shape needs it, is allocated by the library. */
+int vpm_uj_device_async(int kernel, int precision, int64_t ns, const double* Xs,
+                        const double* Gs, const double* Ss, int64_t ld_s, int64_t nt,
+                        const double* Xt, int64_t ld_t, double* U, double* J, int64_t ld_o,
+                        void* cuda_stream);
+
+/* --------------------------------------------------------------- batches -- */
+typedef struct vpm_batch vpm_batch;
+
+/* Many independent particle fields of uneven size advanced together: every
+ * pair pass of a stage is one persistent launch over a flattened
+ * (field, target tile, source chunk) work queue. */
+int vpm_batch_create(int device, int nfields, const int64_t* n, vpm_batch** out);
+int vpm_batch_destroy(vpm_batch* b);
+int vpm_batch_last_error(const vpm_batch* b, char* buf, int64_t len);
+int vpm_batch_set_stream(vpm_batch* b, void* cuda_stream);
+int vpm_batch_set_field(vpm_batch* b, int field, const double* X, int64_t stride_x,
+                        const double* Gamma, int64_t stride_g, const double* sigma,
+                        int64_t stride_s);
+int vpm_batch_get_field(vpm_batch* b, int field, double* X, int64_t stride_x, double* Gamma,
+                        int64_t stride_g, double* sigma, int64_t stride_s);
+int vpm_batch_eval_UJ(vpm_batch* b, int kernel, int precision);
+int vpm_batch_get_UJ(vpm_batch* b, int field, double* U, int64_t stride_u, double* J,
+                     int64_t stride_j);
+int vpm_batch_step(vpm_batch* b, double dt, const vpm_scheme* s, int64_t nsteps, int use_graph);
+
+/* ----------------------------------------------------------- utilities -- */
+/* Tile shape of the FP32 pair kernels: block size, targets per thread and
+ * source chunk length.  The autotuner picks one per size bucket on first use
+ * (per device, mutex-guarded); these calls expose and pin that choice. */
+typedef struct vpm_tile {
+  int32_t block;        /* threads per CTA                         */
+  int32_t tpt;          /* targets per thread (register blocking)  */
+  int32_t chunk;        /* sources per work item (0 = all)         */
+  int32_t reserved;
+} vpm_tile;
+int vpm_autotune(vpm_ctx* ctx, int kernel, int precision, vpm_tile* chosen, double* ms);
+int vpm_set_tile(vpm_ctx* ctx, int kernel, int precision, const vpm_tile* t);
+
+/* Measured FP32 and FP64 FMA throughput of the device (TFLOP/s, FMA = 2 flops),
+ * from an all-SM independent-chain microbenchmark. */
+int vpm_measure_fma_peaks(int device, double* fp32_tflops, double* fp64_tflops, double* sm_mhz);
+
+/* Host fault-injection hook for tests: the next k-th launch-issuing call on the
+ * context fails with VPM_ERR_INJECTED before it launches anything (0 disables). */
+int vpm_debug_fail_after(vpm_ctx* ctx, int64_t k);
+
+/* Number of kernels the context has enqueued since creation (pair passes,
+ * reductions and updates; a graph replay counts its kernels). */
+int vpm_get_launch_count(const vpm_ctx* ctx, int64_t* count);
+
+/* Library build information ("sm_103a ..."). */
+const char* vpm_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VPM_GPU_H */

@@ -1,0 +1,157 @@
+"""GPU parity of the U/∇U pair pass (and the ζ pass behind E_str and the
+enstrophy) against the CPU FP64 oracle, through the C ABI.
+
+Tolerances: FP64 pair sums ≤ 1e-12 relative L2 (and ≤ 1e-11 relative max) of
+the oracle; FP32C ≤ 1e-5 relative L2 (the target precision)."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from flowunsteady_gb300 import _lib as L
+from flowunsteady_gb300.workloads import helical_wake, uniform_box
+from tests.helpers import Ctx, rel_l2, rel_max, scheme
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+KERNELS = [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF]
+
+
+def stretching(J, G):
+    return np.einsum("iba,ib->ia", J, G)
+
+
+@pytest.mark.parametrize("k", KERNELS)
+def test_fp64_matches_oracle_uniform_4096(oracle, k):
+    X, G, S = uniform_box(4096)
+    U0, J0 = oracle.uj_direct(k, X, G, S)
+    with Ctx(4096) as c:
+        c.set(X, G, S)
+        U, J = c.uj(k, L.PREC_FP64)
+    assert rel_l2(U, U0) <= 1e-12 and rel_l2(J, J0) <= 1e-12
+    assert rel_max(U, U0) <= 1e-11 and rel_max(J, J0) <= 1e-11
+
+
+@pytest.mark.parametrize("k", KERNELS)
+def test_fp32c_within_1e5_of_oracle(oracle, k):
+    X, G, S = uniform_box(4096)
+    U0, J0 = oracle.uj_direct(k, X, G, S)
+    with Ctx(4096) as c:
+        c.set(X, G, S)
+        U, J = c.uj(k, L.PREC_FP32C)
+        Un, Jn = c.uj(k, L.PREC_FP32)
+    assert rel_l2(U, U0) <= 1e-5 and rel_l2(J, J0) <= 1e-5
+    assert rel_l2(stretching(J, G), stretching(J0, G)) <= 1e-5
+    # naive FP32 is reported, not bounded tightly
+    assert rel_l2(Un, U0) < 1e-3
+
+
+@pytest.mark.parametrize("k", KERNELS)
+def test_fp32c_helical_wake_sample(oracle, k):
+    # 16,384-particle helical wake: dense near field (σ=0.03 with 0.01 jitter).
+    X, G, S = helical_wake(16384)
+    rng = np.random.default_rng(5)
+    idx = np.sort(rng.choice(X.shape[0], 512, replace=False))
+    U0, J0 = oracle.uj_direct(k, X, G, S, Xt=X[idx])
+    with Ctx(X.shape[0]) as c:
+        c.set(X, G, S)
+        U, J = c.uj(k, L.PREC_FP32C)
+        U64, J64 = c.uj(k, L.PREC_FP64)
+    assert rel_l2(U64[idx], U0) <= 1e-12 and rel_l2(J64[idx], J0) <= 1e-12
+    assert rel_l2(U[idx], U0) <= 1e-5 and rel_l2(J[idx], J0) <= 1e-5
+
+
+@pytest.mark.parametrize("name,k", [("winckelmans", 0), ("gaussianerf", 1)])
+def test_golden_vectors_on_gpu(name, k):
+    d = np.load(os.path.join(GOLD, f"uj_{name}_n160.npz"))
+    with Ctx(200) as c:
+        c.set(d["X"], d["G"], d["S"])
+        U, J = c.uj(k, L.PREC_FP64)
+        assert rel_max(U, d["U"]) <= 1e-12 and rel_max(J, d["J"]) <= 1e-12
+        U, J = c.uj(k, L.PREC_FP32C)
+        assert rel_l2(U, d["U"]) <= 1e-5 and rel_l2(J, d["J"]) <= 1e-5
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 257, 1000])
+@pytest.mark.parametrize("k", KERNELS)
+def test_ragged_sizes(oracle, n, k):
+    X, G, S = uniform_box(n, seed_index=40 + n)
+    S = S * 4
+    U0, J0 = oracle.uj_direct(k, X, G, S)
+    with Ctx(n + 5) as c:
+        c.set(X, G, S)
+        for prec, tol in ((L.PREC_FP64, 1e-12), (L.PREC_FP32C, 1e-5), (L.PREC_FP32, 1e-4)):
+            U, J = c.uj(k, prec)
+            if n == 1:
+                assert np.all(U == 0) and np.all(J == 0)
+            else:
+                assert rel_l2(U, U0) <= tol and rel_l2(J, J0) <= tol, prec
+
+
+def test_target_subset_equals_full_rows():
+    X, G, S = uniform_box(3000, seed_index=50)
+    with Ctx(3000) as c:
+        c.set(X, G, S)
+        for prec in (L.PREC_FP64, L.PREC_FP32C):
+            U, J = c.uj(1, prec)
+            Us, Js = c.uj(1, prec, 2900, 3000)
+            assert rel_max(Us, U[2900:]) < 1e-6 and rel_max(Js, J[2900:]) < 1e-6
+            if prec == L.PREC_FP64:
+                assert rel_max(Us, U[2900:]) < 1e-13
+
+
+def test_repeatable_bitwise():
+    X, G, S = helical_wake(20000)
+    with Ctx(20000) as c:
+        c.set(X, G, S)
+        a = c.uj(1, L.PREC_FP32C)
+        b = c.uj(1, L.PREC_FP32C)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_device_pointer_entry_point():
+    torch = pytest.importorskip("torch")
+    X, G, S = uniform_box(2000, seed_index=60)
+    with Ctx(2000) as c:
+        c.set(X, G, S)
+        U0, J0 = c.uj(0, L.PREC_FP32C)
+    dev = torch.device("cuda:0")
+    Xd = torch.tensor(X.T.copy(), device=dev)
+    Gd = torch.tensor(G.T.copy(), device=dev)
+    Sd = torch.tensor(S, device=dev)
+    Ud = torch.zeros((3, 2000), dtype=torch.float64, device=dev)
+    Jd = torch.zeros((9, 2000), dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    rc = L.lib().vpm_uj_device_async(0, L.PREC_FP32C, 2000, Xd.data_ptr(), Gd.data_ptr(),
+                                     Sd.data_ptr(), 2000, 2000, None, 2000, Ud.data_ptr(),
+                                     Jd.data_ptr(), 2000, ctypes.c_void_p(st))
+    assert rc == 0, L.last_error()
+    torch.cuda.synchronize()
+    U = Ud.cpu().numpy().T
+    J = Jd.cpu().numpy().T.reshape(2000, 3, 3)
+    assert rel_max(U, U0) < 1e-12 and rel_max(J, J0) < 1e-12
+
+
+@pytest.mark.parametrize("k", KERNELS)
+def test_estr_and_enstrophy_match_oracle(oracle, k):
+    X, G, S = uniform_box(1500, seed_index=70)
+    S = S * 3
+    U0, J0 = oracle.uj_direct(k, X, G, S)
+    E0, om0 = oracle.estr_direct(k, X, G, S, J0, transposed=True)
+    d0 = oracle.diagnostics(k, X, G, S)
+    sc = scheme(kernel=k, prec=L.PREC_FP64, sfs=L.SFS_CONSTANT, flags=0)
+    with Ctx(1500) as c:
+        c.set(X, G, S)
+        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
+        _, E = c.sfs()
+        assert rel_l2(E, E0) <= 1e-11
+        d = c.diag(k, L.PREC_FP64)
+        assert abs(d[0] - d0[0]) <= 1e-12 * abs(d0[0])
+        assert np.allclose(d[1:7], d0[1:7], rtol=1e-12, atol=1e-18)
+        sc.precision = L.PREC_FP32C
+        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
+        _, E = c.sfs()
+        assert rel_l2(E, E0) <= 1e-5
+        d = c.diag(k, L.PREC_FP32C)
+        assert abs(d[0] - d0[0]) <= 1e-6 * abs(d0[0])
