@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import glob
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -17,8 +18,23 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", platform.machine())
 LIB = os.path.join(HERE, "libvpmgpu.so")
+
+_ELF_MACHINE = {"x86_64": 0x3E, "aarch64": 0xB7, "arm64": 0xB7}
+
+
+def elf_matches_host(path: str) -> bool:
+    """True when `path` is an ELF file built for this machine's architecture."""
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    if len(head) < 20 or head[:4] != b"\x7fELF":
+        return False
+    want = _ELF_MACHINE.get(platform.machine())
+    return want is None or int.from_bytes(head[18:20], "little") == want
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -49,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
 
     def compile_one(src):
         obj = obj_of(src)
-        if (not force and os.path.exists(obj)
+        if (not force and os.path.exists(obj) and elf_matches_host(obj)
                 and os.path.getmtime(obj) >= max(os.path.getmtime(src), hdr_t)):
             return obj, None
         cmd = [cc] + ARCH + flags + ["-c", src, "-o", obj]
@@ -67,7 +83,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
     newest = max(os.path.getmtime(o) for o in objs)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+    if (force or not os.path.exists(LIB) or not elf_matches_host(LIB)
+            or os.path.getmtime(LIB) < newest):
         cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

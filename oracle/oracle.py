@@ -29,11 +29,26 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _i64 = ctypes.c_int64
 
 
+def _elf_matches_host(path: str) -> bool:
+    import platform
+    want = {"x86_64": 0x3E, "aarch64": 0xB7, "arm64": 0xB7}.get(platform.machine())
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    if len(head) < 20 or head[:4] != b"\x7fELF":
+        return False
+    return want is None or int.from_bytes(head[18:20], "little") == want
+
+
 def build(force: bool = False) -> str:
     """Compile liboracle.so with the committed Makefile (g++ + OpenMP)."""
     src = os.path.join(_HERE, "vpm_oracle.cpp")
-    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
-        subprocess.check_call(["make", "-s", "-C", _HERE, "-B" if force else "liboracle.so"])
+    stale = (not os.path.exists(_LIB) or not _elf_matches_host(_LIB)
+             or os.path.getmtime(_LIB) < os.path.getmtime(src))
+    if force or stale:
+        subprocess.check_call(["make", "-s", "-B", "-C", _HERE, "liboracle.so"])
     return _LIB
 
 
