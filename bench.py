@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--n", type=int, default=262144)
     p.add_argument("--sample-targets", type=int, default=8192)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp32", "fp64"])
+    p.add_argument("--timed-only", action="store_true",
+                   help="run only the warm-up and timed evaluations (for profiler captures)")
     return p.parse_args()
 
 
@@ -225,15 +228,16 @@ def run_ours(args, world, rank, local, dist):
     f32 = ctypes.c_double()
     f64 = ctypes.c_double()
     mhz = ctypes.c_double()
-    L.check(lib.vpm_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64),
-                                      ctypes.byref(mhz)))
+    if not args.timed_only:
+        L.check(lib.vpm_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64),
+                                          ctypes.byref(mhz)))
 
     ctx = ctypes.c_void_p()
     L.check(lib.vpm_ctx_create(local, n, ctypes.byref(ctx)))
     stream = torch.cuda.current_stream(dev)
     L.check(lib.vpm_ctx_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
     L.check(lib.vpm_set_particles(ctx, n, L.dptr(X), 3, L.dptr(G), 3, L.dptr(S), 1), ctx)
-    prec = L.PREC_FP32C
+    prec = {"fp32c": L.PREC_FP32C, "fp32": L.PREC_FP32, "fp64": L.PREC_FP64}[args.precision]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     for _ in range(args.warmup):
@@ -268,6 +272,13 @@ def run_ours(args, world, rank, local, dist):
     value = world * args.steps * pairs / total_s
     ms_per_step = 1e3 * total_s / args.steps
     launches = int(l1.value - l0.value)
+    if args.timed_only:
+        if rank == 0:
+            print(json.dumps({"timed_only": True, "ms_per_step": ms_per_step,
+                              "pairs_per_s": value, "gpu_launches": launches,
+                              "kernel": args.kernel, "precision": args.precision, "n": n}))
+        lib.vpm_ctx_destroy(ctx)
+        return None
 
     # ---- end to end through the C ABI with host buffers ------------------------
     U = np.empty((n, 3))
