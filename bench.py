@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--sample-targets", type=int, default=8192)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp32", "fp64"])
+    p.add_argument("--tile", default=None,
+                   help="pin the pair-kernel tile shape, e.g. 128x4 (default: autotuner/default)")
     p.add_argument("--timed-only", action="store_true",
                    help="run only the warm-up and timed evaluations (for profiler captures)")
     return p.parse_args()
@@ -237,6 +239,12 @@ def run_ours(args, world, rank, local, dist):
     stream = torch.cuda.current_stream(dev)
     L.check(lib.vpm_ctx_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)), ctx)
     L.check(lib.vpm_set_particles(ctx, n, L.dptr(X), 3, L.dptr(G), 3, L.dptr(S), 1), ctx)
+    if args.tile:
+        b_, t_ = (int(v) for v in args.tile.lower().split("x"))
+        tile = L.Tile(b_, t_, 0, 0)
+        L.check(lib.vpm_set_tile(ctx, kernel, {"fp32c": L.PREC_FP32C, "fp32": L.PREC_FP32,
+                                               "fp64": L.PREC_FP64}[args.precision],
+                                 ctypes.byref(tile)), ctx)
     prec = {"fp32c": L.PREC_FP32C, "fp32": L.PREC_FP32, "fp64": L.PREC_FP64}[args.precision]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -275,7 +283,7 @@ def run_ours(args, world, rank, local, dist):
     if args.timed_only:
         if rank == 0:
             print(json.dumps({"timed_only": True, "ms_per_step": ms_per_step,
-                              "pairs_per_s": value, "gpu_launches": launches,
+                              "pairs_per_s": value, "gpu_launches": launches, "tile": args.tile,
                               "kernel": args.kernel, "precision": args.precision, "n": n}))
         lib.vpm_ctx_destroy(ctx)
         return None

@@ -892,7 +892,7 @@ int vpm_autotune(vpm_ctx* c, int kernel, int precision, vpm_tile* chosen, double
     return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel or precision");
   if (c->n == 0) return ctx_fail(c, VPM_ERR_STATE, "autotune needs particles");
   DeviceGuard dg(c->device);
-  static const Shape cands[] = {{128, 2}, {128, 4}, {256, 2}, {256, 4}, {128, 1}};
+  static const Shape cands[] = {{128, 2}, {128, 4}, {256, 2}, {128, 1}};
   Shape best{0, 0};
   double best_ms = 1e30;
   cudaEvent_t e0, e1;

@@ -48,13 +48,28 @@ __host__ __device__ constexpr size_t smem_bytes(int block, int tpt) {
   return src + fold;
 }
 
+// Minimum resident CTAs requested from the compiler: caps the FP32 U/J kernels
+// at 128 (T=4) or 96 (T=2) registers per thread.
+template <int PASS, int PREC, int BLOCK, int T>
+constexpr int min_blocks() {
+  return (PASS == PASS_UJ && PREC != VPM_PREC_FP64)
+             ? (65536 / (BLOCK * (T >= 4 ? 128 : 96)) > 0 ? 65536 / (BLOCK * (T >= 4 ? 128 : 96)) : 1)
+             : 1;
+}
+
+// Sources summed in FP32 between two folds into the compensated (hi, lo) pairs.
+constexpr int kFoldSources = 256;
+
 template <int PASS, int KERNEL, int PREC, int BLOCK, int T>
-__global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
+__global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
+    pair_kernel(const PairArgs a) {
   using Tr = PairTraits<PASS, PREC>;
   using R = typename Tr::R;
   constexpr bool COMP = Tr::kComp;
   constexpr int NV = Tr::kNval;
   constexpr int TB = BLOCK * T;
+  constexpr int FOLD_TILES = kFoldSources / BLOCK > 0 ? kFoldSources / BLOCK : 1;
+  constexpr bool F32 = sizeof(R) == sizeof(float);
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Quad<R>* tileA = reinterpret_cast<Quad<R>*>(smem_raw);
@@ -126,6 +141,7 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
         }
     }
 
+    int tiles = 0;
     for (int64_t tile0 = s0; tile0 < s1; tile0 += BLOCK) {
       // ---- stage one tile of sources -------------------------------------
       __syncthreads();  // previous tile fully consumed
@@ -164,11 +180,22 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
 
       // ---- all pairs of the tile ------------------------------------------
       const int cnt = int(min(int64_t(BLOCK), s1 - tile0));
+      if constexpr (PASS == PASS_UJ && F32) {
+        const float4* ta = reinterpret_cast<const float4*>(tileA);
+        const float4* tb = reinterpret_cast<const float4*>(tileB);
+#pragma unroll 2
+        for (int js = 0; js < cnt; ++js) {
+          const float4 sa = ta[js];
+          const float4 sb = tb[js];
+          if (KERNEL == VPM_KERNEL_WINCKELMANS) uj_source_winck<T>(sa, sb, tx, ty, tz, acc);
+          else uj_source_gauss<T>(sa, sb, tx, ty, tz, acc);
+        }
+      } else {
 #pragma unroll 2
       for (int js = 0; js < cnt; ++js) {
         const Quad<R> sa = tileA[js];
         const Quad<R> sb = tileB[js];
-        if (PASS == PASS_UJ) {
+        if constexpr (PASS == PASS_UJ && !F32) {
 #pragma unroll
           for (int k = 0; k < T; ++k) {
             const R dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
@@ -197,9 +224,10 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
           }
         }
       }
+      }
 
-      if (COMP) {
-        // Fold this tile's FP32 sums into the (hi, lo) pairs.
+      if (COMP && (++tiles % FOLD_TILES == 0 || tile0 + BLOCK >= s1)) {
+        // Fold the FP32 sums of the last kFoldSources sources into the (hi, lo) pairs.
 #pragma unroll
         for (int k = 0; k < T; ++k)
 #pragma unroll
@@ -229,6 +257,8 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
           v[w] = double(acc[k][w]);
         }
       }
+      // FP32 U/J passes do not accumulate A22 (trace-free pairs): rebuild it.
+      if (PASS == PASS_UJ && F32) v[11] = -(v[3] + v[7]);
       if (slot >= 0) {
 #pragma unroll
         for (int w = 0; w < NV; ++w) a.part[(int64_t(slot) * NV + w) * a.ldp + i] = v[w];
@@ -327,7 +357,7 @@ PairFn fn_ready() {
   return pair_kernel<PASS, KERNEL, PREC, BLOCK, T>;
 }
 
-// Compiled shapes: FP64 {128x1}; FP32 and FP32C {128x2, 128x4, 256x2, 256x4}.
+// Compiled shapes: FP64 {128x1}; FP32 and FP32C {128x2, 128x4, 256x2}.
 template <int PASS, int KERNEL, int PREC>
 PairFn pick(Shape s) {
   if constexpr (PREC == VPM_PREC_FP64) {
@@ -337,7 +367,6 @@ PairFn pick(Shape s) {
     if (s.block == 128 && s.tpt == 2) return fn_ready<PASS, KERNEL, PREC, 128, 2>();
     if (s.block == 128 && s.tpt == 4) return fn_ready<PASS, KERNEL, PREC, 128, 4>();
     if (s.block == 256 && s.tpt == 2) return fn_ready<PASS, KERNEL, PREC, 256, 2>();
-    if (s.block == 256 && s.tpt == 4) return fn_ready<PASS, KERNEL, PREC, 256, 4>();
     return nullptr;
   }
 }
@@ -365,7 +394,7 @@ PairFn pick_all(int pass, int kernel, int prec, Shape s) {
 
 bool pair_shape_supported(int precision, Shape s) {
   if (precision == VPM_PREC_FP64) return s.block == 128 && s.tpt == 1;
-  return (s.block == 128 || s.block == 256) && (s.tpt == 2 || s.tpt == 4);
+  return (s.block == 128 && (s.tpt == 2 || s.tpt == 4)) || (s.block == 256 && s.tpt == 2);
 }
 
 size_t pair_smem_bytes(int pass, int precision, Shape s) {

@@ -35,8 +35,7 @@ constexpr double kLog2e = 1.44269504088896340736;
 constexpr double kZeta0Winck = 15.0 / (8.0 * kPi);
 constexpr double kZeta0Gauss = 0.06349363593424096978;  // (2π)^{-3/2}
 
-// ρ² below which the Gaussian-erf series replaces the direct forms.
-constexpr float kSeriesRho2F = 0.5f;
+// ρ² below which the FP64 Gaussian-erf series replaces the direct forms.
 constexpr double kSeriesRho2D = 0.25;
 
 __host__ __device__ inline double zeta0_of(int kernel) {
@@ -88,53 +87,23 @@ struct GaussSeries {
 // the tile is staged).
 //   Winckelmans:  a = σ²,   b = 5/2 σ² (so r²+σ²+b·... forms below)
 //   Gaussian-erf: a = 1/σ², b = 1/σ
+//   (FP32 Gaussian-erf: a = -log2(e)/(2σ²), the exponent scale of e^{-ρ²/2})
 template <int KERNEL, typename R>
 __device__ inline void source_consts(double sig, R& a, R& b) {
   if (KERNEL == VPM_KERNEL_WINCKELMANS) {
     a = R(sig * sig);
     b = R(1.5 * sig * sig);
+  } else if (sizeof(R) == sizeof(float)) {
+    a = R(-0.5 * kLog2e / (sig * sig));
+    b = R(1.0 / sig);
   } else {
     a = R(1.0 / (sig * sig));
     b = R(1.0 / sig);
   }
 }
 
-// (q, p) of one pair from r² and the source constants; the pair is dropped
-// (q = p = 0) when r² == 0.
-__device__ inline void pair_qp_f32_winck(float r2, float s2, float k15, float& q, float& p) {
-  const float s = r2 + s2;
-  const float rs = rsqrtf(s);
-  const float rs2 = rs * rs;
-  const float rs3 = rs2 * rs;
-  const float rs5 = rs3 * rs2;
-  const float rs7 = rs5 * rs2;
-  q = fmaf(k15, rs5, rs3);             // (s + 3/2σ²)/s^{5/2} = (r²+5/2σ²)/s^{5/2}
-  p = fmaf(k15 + s2, rs7, rs5);        // (s + 5/2σ²)/s^{7/2} = (r²+7/2σ²)/s^{7/2}
-  q = r2 > 0.f ? q : 0.f;
-}
-
-__device__ inline void pair_qp_f32_gauss(float r2, float is2, float is1, float& q, float& p) {
-  const float rho2 = r2 * is2;
-  if (rho2 < kSeriesRho2F) {
-    float h1, h2;
-    GaussSeries<float, 8>::eval(rho2, h1, h2);
-    const float is3 = is2 * is1;
-    q = h1 * is3;
-    p = h2 * is3 * is2;
-    q = r2 > 0.f ? q : 0.f;
-    p = r2 > 0.f ? p : 0.f;
-  } else {
-    const float ri = rsqrtf(r2);
-    const float rho = r2 * ri * is1;
-    const float e = exp2f(rho2 * float(-0.5 * kLog2e));
-    const float g = erff(rho * float(kInvSqrt2)) - float(kSqrt2overPi) * rho * e;
-    const float ri2 = ri * ri;
-    const float ri3 = ri2 * ri;
-    q = g * ri3;
-    p = fmaf(float(kSqrt2overPi) * rho * rho2, e, -3.f * g) * ri3 * ri2;
-  }
-}
-
+// (q, p) of one FP64 pair from r² and the source constants; the pair is
+// dropped (q = p = 0) when r² == 0.
 __device__ inline void pair_qp_f64_winck(double r2, double s2, double k15, double& q, double& p) {
   const double s = r2 + s2;
   const double rs = rsqrt(s);
@@ -169,11 +138,6 @@ __device__ inline void pair_qp_f64_gauss(double r2, double is2, double is1, doub
 }
 
 template <int KERNEL>
-__device__ inline void pair_qp(float r2, float a, float b, float& q, float& p) {
-  if (KERNEL == VPM_KERNEL_WINCKELMANS) pair_qp_f32_winck(r2, a, b, q, p);
-  else pair_qp_f32_gauss(r2, a, b, q, p);
-}
-template <int KERNEL>
 __device__ inline void pair_qp(double r2, double a, double b, double& q, double& p) {
   if (KERNEL == VPM_KERNEL_WINCKELMANS) pair_qp_f64_winck(r2, a, b, q, p);
   else pair_qp_f64_gauss(r2, a, b, q, p);
@@ -199,16 +163,19 @@ __device__ inline void zeta_consts(double sig, R& a, R& b) {
   }
 }
 
+__device__ __forceinline__ float rsqrt_ftz(float x);
+__device__ __forceinline__ float ex2_ftz(float x);
+
 template <int KERNEL>
 __device__ inline float pair_zeta(float r2, float a, float b) {
   float z;
   if (KERNEL == VPM_KERNEL_WINCKELMANS) {
-    const float rs = rsqrtf(fmaf(r2, a, 1.f));
+    const float rs = rsqrt_ftz(fmaf(r2, a, 1.f));
     const float rs2 = rs * rs;
     const float rs4 = rs2 * rs2;
     z = b * rs4 * rs2 * rs;
   } else {
-    z = b * exp2f(r2 * a);
+    z = b * ex2_ftz(r2 * a);
   }
   return r2 > 0.f ? z : 0.f;
 }
@@ -232,6 +199,143 @@ __device__ inline void two_sum(float a, float b, float& s, float& e) {
   const float bp = __fadd_rn(s, -a);
   const float ap = __fadd_rn(s, -bp);
   e = __fadd_rn(__fadd_rn(a, -ap), __fadd_rn(b, -bp));
+}
+
+}  // namespace vpm
+
+// ------------------------------------------------------------------------------
+// FP32 pair routines of the U/∇U pass: one staged source against the T targets
+// a thread holds.  They use the hardware approximations of the PTX ISA
+// (rsqrt/ex2/rcp .approx.ftz) directly, one SFU instruction each.
+namespace vpm {
+
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Gaussian-erf for ρ² >= 3/2, without erf:
+//   g(ρ) = erf(x) - √(2/π) ρ e^{-x²} = 1 - e^{-x²} (erfcx(x) + √(2/π) ρ),  x = ρ/√2,
+// with erfcx(x) = e^{x²} erfc(x) ≈ t (a1 + t (a2 + t (a3 + t a4))), t = 1/(1 + P x).
+// This is the structure of Hastings' approximation (Abramowitz & Stegun 7.1.26);
+// P and a1..a4 were fitted for this code by Lawson-reweighted least squares to
+// minimise the relative error of g over ρ in [1, 9] (max 7.5e-8; beyond ρ = 9
+// the e^{-x²} factor is below 2e-18).  For ρ² < 3/2 the power series is used
+// (10 terms); in FP32 the worst pair errors are then 4.4e-7 in q and 1.8e-6 in
+// q'/r, both at the switch point where ρg' - 3g cancels.
+constexpr float kErfcxP = 0.47729708f;  // P/√2: t = 1/(1 + kErfcxP ρ)
+constexpr float kErfcxA1 = 0.39182437f;
+constexpr float kErfcxA2 = 0.28743228f;
+constexpr float kErfcxA3 = 0.59069124f;
+constexpr float kErfcxA4 = -0.27144525f;
+// ρ² = 3/2 expressed in the exponent argument r²·(-log2(e)/(2σ²)).
+constexpr float kArgSeries = float(-0.5 * kLog2e * 1.5);
+constexpr float kArgToRho2 = float(-2.0 / kLog2e);
+
+// Accumulate one pair into the 14 FP32 sums of a target (A22 is not kept:
+// J is trace-free pair by pair, c·Δx = 0, and the epilogue sets
+// A22 = -(A00 + A11)).  acc: U 0..2, A 3..11 (11 unused), W 12..14.
+__device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float q, float p,
+                                           float gx, float gy, float gz, float* acc) {
+  const float c0 = dy * gz - dz * gy;
+  const float c1 = dz * gx - dx * gz;
+  const float c2 = dx * gy - dy * gx;
+  acc[0] = fmaf(q, c0, acc[0]);
+  acc[1] = fmaf(q, c1, acc[1]);
+  acc[2] = fmaf(q, c2, acc[2]);
+  const float p0 = p * c0, p1 = p * c1, p2 = p * c2;
+  acc[3] = fmaf(p0, dx, acc[3]);
+  acc[4] = fmaf(p0, dy, acc[4]);
+  acc[5] = fmaf(p0, dz, acc[5]);
+  acc[6] = fmaf(p1, dx, acc[6]);
+  acc[7] = fmaf(p1, dy, acc[7]);
+  acc[8] = fmaf(p1, dz, acc[8]);
+  acc[9] = fmaf(p2, dx, acc[9]);
+  acc[10] = fmaf(p2, dy, acc[10]);
+  acc[12] = fmaf(q, gx, acc[12]);
+  acc[13] = fmaf(q, gy, acc[13]);
+  acc[14] = fmaf(q, gz, acc[14]);
+}
+
+// Winckelmans: source quads (x, y, z, σ²) and (Γx, Γy, Γz, 3/2 σ²).
+template <int T>
+__device__ __forceinline__ void uj_source_winck(const float4 sa, const float4 sb,
+                                                const float (&tx)[T], const float (&ty)[T],
+                                                const float (&tz)[T], float (&acc)[T][15]) {
+  const float s2 = sa.w, k15 = sb.w, k25 = sa.w + sb.w;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float rs = rsqrt_ftz(r2 + s2);
+    const float rs2 = rs * rs;
+    const float rs3 = rs2 * rs;
+    const float rs5 = rs3 * rs2;
+    const float rs7 = rs5 * rs2;
+    float q = fmaf(k15, rs5, rs3);
+    q = r2 > 0.f ? q : 0.f;
+    const float p = fmaf(k25, rs7, rs5);
+    accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
+  }
+}
+
+// Gaussian-erf: source quads (x, y, z, -log2(e)/(2σ²)) and (Γx, Γy, Γz, 1/σ).
+// All T targets take the erf-free form; one warp vote per source sends the
+// rare warps holding a pair with ρ² < 3/2 (or the self pair) through the series.
+template <int T>
+__device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb,
+                                                const float (&tx)[T], const float (&ty)[T],
+                                                const float (&tz)[T], float (&acc)[T][15]) {
+  const float ea = sa.w, is1 = sb.w;
+  const float kt = kErfcxP * is1;                      // t = 1/(1 + kt r)
+  const float kc = float(kSqrt2overPi) * is1;          // √(2/π) ρ = kc r
+  const float k3 = float(kSqrt2overPi) * is1 * is1 * is1;
+  float dx[T], dy[T], dz[T], arg[T], q[T], p[T];
+  float amax = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    dx[k] = tx[k] - sa.x;
+    dy[k] = ty[k] - sa.y;
+    dz[k] = tz[k] - sa.z;
+    const float r2 = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
+    arg[k] = r2 * ea;
+    amax = fmaxf(amax, arg[k]);
+    const float ri = rsqrt_ftz(r2);
+    const float r = r2 * ri;
+    const float e = ex2_ftz(arg[k]);
+    const float t = rcp_ftz(fmaf(kt, r, 1.f));
+    const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
+    const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
+    const float ri2 = ri * ri;
+    q[k] = g * (ri2 * ri);
+    p[k] = fmaf(-3.f, q[k], k3 * e) * ri2;
+  }
+  if (__any_sync(0xffffffffu, amax > kArgSeries)) {
+    const float is2 = is1 * is1, is3 = is2 * is1, is5 = is3 * is2;
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      if (arg[k] > kArgSeries) {
+        float h1, h2;
+        GaussSeries<float, 10>::eval(arg[k] * kArgToRho2, h1, h2);
+        const bool self = arg[k] == 0.f;   // r² == 0 (the exponent argument is r²·(<0))
+        q[k] = self ? 0.f : h1 * is3;
+        p[k] = self ? 0.f : h2 * is5;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < T; ++k) accum_pair(dx[k], dy[k], dz[k], q[k], p[k], sb.x, sb.y, sb.z, acc[k]);
 }
 
 }  // namespace vpm
