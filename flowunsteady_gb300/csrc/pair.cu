@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 
   const int tid = threadIdx.x;
   const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
+  const bool same_arrays = a.xt == a.xs && a.ldt == a.lds;
 
   int item;
   if (a.counter) {
@@ -183,12 +184,20 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       if constexpr (PASS == PASS_UJ && F32) {
         const float4* ta = reinterpret_cast<const float4*>(tileA);
         const float4* tb = reinterpret_cast<const float4*>(tileB);
+        // Coincident pairs can only occur in tiles that overlap the CTA's own
+        // targets (or anywhere when the targets are a separate array).
+        const bool own = !same_arrays || (tile0 < t1 && tile0 + BLOCK > t0);
+        if (KERNEL == VPM_KERNEL_WINCKELMANS && !own) {
 #pragma unroll 2
-        for (int js = 0; js < cnt; ++js) {
-          const float4 sa = ta[js];
-          const float4 sb = tb[js];
-          if (KERNEL == VPM_KERNEL_WINCKELMANS) uj_source_winck<T>(sa, sb, tx, ty, tz, acc);
-          else uj_source_gauss<T>(sa, sb, tx, ty, tz, acc);
+          for (int js = 0; js < cnt; ++js)
+            uj_source_winck<T, false>(ta[js], tb[js], tx, ty, tz, acc);
+        } else if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+#pragma unroll 2
+          for (int js = 0; js < cnt; ++js)
+            uj_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
+        } else {
+#pragma unroll 2
+          for (int js = 0; js < cnt; ++js) uj_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc);
         }
       } else {
 #pragma unroll 2

@@ -268,8 +268,11 @@ __device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float q
   acc[14] = fmaf(q, gz, acc[14]);
 }
 
-// Winckelmans: source quads (x, y, z, σ²) and (Γx, Γy, Γz, 3/2 σ²).
-template <int T>
+// Winckelmans: source quads (x, y, z, σ²) and (Γx, Γy, Γz, 3/2 σ²).  MASK drops
+// coincident pairs; the kernel sets it only for source tiles that can hold a
+// target's own particle (the kernel is finite at r = 0, so an unmasked
+// coincident pair adds the core term q(0) ε·Γ to J and nothing to U).
+template <int T, bool MASK>
 __device__ __forceinline__ void uj_source_winck(const float4 sa, const float4 sb,
                                                 const float (&tx)[T], const float (&ty)[T],
                                                 const float (&tz)[T], float (&acc)[T][15]) {
@@ -284,7 +287,7 @@ __device__ __forceinline__ void uj_source_winck(const float4 sa, const float4 sb
     const float rs5 = rs3 * rs2;
     const float rs7 = rs5 * rs2;
     float q = fmaf(k15, rs5, rs3);
-    q = r2 > 0.f ? q : 0.f;
+    if (MASK) q = r2 > 0.f ? q : 0.f;
     const float p = fmaf(k25, rs7, rs5);
     accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
   }
