@@ -78,11 +78,13 @@ int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int 
 // Source split: choose the number of source chunks so that the grid of
 // n_tb x n_chunk items fills whole waves of resident CTAs, keeping chunks at
 // least two tiles long and preferring fewer chunks at equal efficiency.
-int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out) {
+int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out,
+                int max_chunks) {
   int best_c = 1;
   int64_t best_chunk = std::max<int64_t>(ns, 1);
   double best = -1.0;
-  for (int c = 1; c <= 128; ++c) {
+  const int cmax = max_chunks > 0 ? std::min(max_chunks, 128) : 128;
+  for (int c = 1; c <= cmax; ++c) {
     int64_t chunk = round_up(std::max<int64_t>(ceil_div(ns, c), 1), block);
     if (c > 1 && chunk < 2 * block) break;
     const int cc = int(std::max<int64_t>(ceil_div(ns, chunk), 1));
@@ -112,7 +114,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   const int64_t n_tb = ceil_div(nt, TB);
   const int resident = resident_ctas(device, pc.pass, pc.kernel, pc.prec, sh, num_sms);
   int64_t chunk = 0;
-  int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk);
+  int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
   const int nv = pc.pass == PASS_UJ ? kNvalUJ : kNvalZeta;
   const size_t need = n_chunk > 1 ? size_t(n_chunk) * nv * size_t(ldp) : 0;
   if (need_part) *need_part = std::max(*need_part, need);

@@ -28,6 +28,7 @@ struct PairCall {
   double sigma_scale;
   double *u, *j;
   int64_t ldo;
+  int max_chunks = 0;   // upper bound on source chunks (0 = planner's choice)
 };
 
 struct PairPlan {
@@ -41,7 +42,8 @@ Shape default_shape(int pass, int precision);
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n, const Shape* pinned);
 void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s);
 int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int num_sms);
-int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out);
+int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out,
+                int max_chunks = 0);
 cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* pinned,
                      double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
                      cudaStream_t st, PairPlan* plan_out);

@@ -245,6 +245,27 @@ int vpm_uj_device_async(int kernel, int precision, int64_t ns, const double* Xs,
                         const double* Xt, int64_t ld_t, double* U, double* J, int64_t ld_o,
                         void* cuda_stream);
 
+/* The same evaluation as vpm_uj_device_async, for callers that cannot let the
+ * library allocate device memory: a loop that must not allocate once it runs,
+ * a host whose device memory is entirely held by its own pool allocator, or
+ * work being captured into a CUDA graph.  It has no counterpart in the
+ * reference.  It calls no cudaMalloc, cudaFree or other allocating routine:
+ * the scratch for split source ranges is a fixed 4 MiB array that every GPU
+ * loading the library holds until the process exits.
+ *   - nt may be at most 16384 targets; larger calls return VPM_ERR_CAPACITY
+ *     without launching (use vpm_uj_device_async for them).
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     outside any stream capture.
+ *   - All calls share the one array and leave their partial sums in it; every
+ *     slot a call uses is written before it is read.  Calls whose work
+ *     overlaps on the GPU (different streams, or host threads) race on the
+ *     array: serialise them. */
+int vpm_uj_device_noalloc(int kernel, int precision, int64_t ns, const double* Xs,
+                          const double* Gs, const double* Ss, int64_t ld_s, int64_t nt,
+                          const double* Xt, int64_t ld_t, double* U, double* J, int64_t ld_o,
+                          void* cuda_stream);
+
 /* --------------------------------------------------------------- batches -- */
 typedef struct vpm_batch vpm_batch;
 
