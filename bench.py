@@ -43,6 +43,9 @@ PAIR_FLOP = 60          # algorithmic flop per U+∇U pair (FMA = 2)
 BYTES_H2D = 56          # X, Γ, σ per particle (FP64)
 BYTES_D2H = 96          # U (3) and J (9) per particle (FP64)
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) of one pair-kernel launch of the default workload,
+# from an ncu capture (profiles/launches_bench_helical_n262144.md).
+PAIR_KERNEL_TRAFFIC = {262144: 25233408 + 194519296}
 
 
 def parse():
@@ -343,7 +346,8 @@ def run_ours(args, world, rank, local, dist):
     achieved = PAIR_FLOP * pairs / (ms_per_step / 1e3) / 1e12
     roof = {"bound": "fp32_fma", "achieved": achieved, "peak": f32.value, "unit": "TFLOP/s",
             "frac": achieved / f32.value if f32.value > 0 else None,
-            "traffic": None,
+            "traffic": PAIR_KERNEL_TRAFFIC.get(n),
+            "traffic_unit": "bytes per launch (ncu dram__bytes_read + dram__bytes_write)",
             "peak_source": "in-repo FFMA microbenchmark (vpm_measure_fma_peaks) in this run",
             "fp64_peak_tflops": f64.value, "microbench_sm_mhz": mhz.value,
             "flop_per_pair": PAIR_FLOP}
