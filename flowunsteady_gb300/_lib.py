@@ -37,6 +37,7 @@ SFS_DYNAMIC = 1
 SFS_CONSTANT = 2
 SFS_CLIP_BACKSCATTER = 1
 SFS_FORCE_POSITIVE = 2
+SFS_ANALYTIC_DSIGMA = 4
 RELAX_NONE = 0
 RELAX_PEDRIZZETTI = 1
 

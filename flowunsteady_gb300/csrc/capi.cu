@@ -115,7 +115,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   const int resident = resident_ctas(device, pc.pass, pc.kernel, pc.prec, sh, num_sms);
   int64_t chunk = 0;
   int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
-  const int nv = pc.pass == PASS_UJ ? kNvalUJ : kNvalZeta;
+  const int nv = nval_of(pc.pass);
   const size_t need = n_chunk > 1 ? size_t(n_chunk) * nv * size_t(ldp) : 0;
   if (need_part) *need_part = std::max(*need_part, need);
   if (plan_out) {
@@ -128,9 +128,10 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   if (need > part_elems) return cudaErrorMemoryAllocation;
   PairArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.xs = pc.xs; a.gs = pc.gs; a.ss = pc.ss; a.vs = pc.vs; a.lds = pc.lds;
+  a.xs = pc.xs; a.gs = pc.gs; a.ss = pc.ss; a.vs = pc.vs; a.ws = pc.ws; a.lds = pc.lds;
   a.xt = pc.xt; a.ldt = pc.ldt;
   a.sigma_scale = pc.sigma_scale;
+  a.dj = pc.dj;
   a.t_off = pc.t0; a.nt = nt; a.ns = pc.ns; a.chunk = chunk;
   a.n_tb = int(n_tb); a.n_chunk = n_chunk;
   a.items = nullptr; a.n_items = 0; a.counter = nullptr;
@@ -140,7 +141,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   if (e != cudaSuccess) return e;
   if (n_chunk > 1) {
     e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
-                      pc.u, pc.j, pc.ldo, st);
+                      pc.u, pc.j, pc.dj, pc.ldo, st);
   }
   return e;
 }
@@ -302,7 +303,8 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
 
 // Enqueue the pair pass of one context (targets [t0,t1) of its own particles).
 cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int64_t t1,
-                     double scale, const double* vs, double* u, double* j) {
+                     double scale, const double* vs, double* u, double* j, const double* ws,
+                     double* dj) {
   if (c->bp) {
     // Batch: one persistent launch over the flattened (field, target tile,
     // source chunk) queue, then the fixed-order reduction of split fields.
@@ -314,7 +316,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
         return cudaErrorInvalidValue;  // plans are built outside capture (dry pass)
       }
     }
-    const int nv = pass == PASS_UJ ? kNvalUJ : kNvalZeta;
+    const int nv = nval_of(pass);
     const size_t need = bp->max_chunks > 1 ? size_t(bp->max_chunks) * nv * size_t(c->ld) : 0;
     c->part_need = std::max(c->part_need, need);
     if (c->dry) return cudaSuccess;
@@ -323,9 +325,10 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     if (e != cudaSuccess) return e;
     PairArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.xs = c->X; a.gs = c->G; a.ss = c->S; a.vs = vs; a.lds = c->ld;
+    a.xs = c->X; a.gs = c->G; a.ss = c->S; a.vs = vs; a.ws = ws; a.lds = c->ld;
     a.xt = c->X; a.ldt = c->ld;
     a.sigma_scale = scale;
+    a.dj = dj;
     a.items = bp->d_items; a.n_items = bp->n_items; a.counter = bp->d_counter;
     a.u = u; a.j = j; a.ldo = c->ld;
     a.part = c->part; a.ldp = c->ld;
@@ -334,7 +337,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     c->launches += 1;
     if (bp->max_chunks > 1) {
       e = launch_reduce(pass, kernel, c->part, c->ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
-                        0, c->n, u, j, c->ld, c->st);
+                        0, c->n, u, j, dj, c->ld, c->st);
       c->launches += 1;
     }
     return e;
@@ -346,7 +349,8 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   pc.xt = c->X; pc.ldt = c->ld;
   pc.sigma_scale = scale;
   pc.u = u; pc.j = j; pc.ldo = c->ld;
-  const Shape* pinned = &c->pinned[pass][kernel][prec];
+  pc.ws = ws; pc.dj = dj;
+  const Shape* pinned = &c->pinned[pass & 1][kernel][prec];  // D passes share their plain pass's pin
   PairPlan plan;
   plan.n_chunk = 1;
   cudaError_t e = run_pair(pc, c->device, c->num_sms, pinned, c->part, c->ld, c->part_elems,
@@ -369,32 +373,58 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     if (e_ != cudaSuccess) return e_;                       \
   } while (0)
 
-// One stage of a step: U/J, SFS, fused update.
-static cudaError_t enqueue_stage(vpm_ctx* c, const vpm_scheme* s, double dt, double a, double b,
-                                 int stage) {
+// U/J and the SFS pass of a stage (the first stage of a dynamic step also
+// computes C_d).  In the analytic form the first stage runs the α-derivative
+// passes (U/J + DJ, then ζ + Dζ) instead of separate passes at σ and ασ.
+static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
   const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
   const int K = s->kernel, P = s->precision;
-  ENQP(c, ctx_pair(c, PASS_UJ, K, P, 0, n, 1.0, nullptr, c->U, c->J));
   const bool sfs = s->sfs != VPM_SFS_NONE;
-  if (sfs) {
-    ENQ(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
-    ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
-    ENQ(c, launch_estr_finish(n, ld, c->raw, c->J, s->transposed, c->E, c->st));
-    if (s->sfs == VPM_SFS_CONSTANT) {
-      ENQ(c, launch_sfs_constant(nf, s->sfs_Cd, c->C, c->st));
-    } else if (stage == 0) {
-      const double al = s->sfs_alpha;
+  const bool dyn0 = s->sfs == VPM_SFS_DYNAMIC && stage == 0;
+  const bool analytic = dyn0 && (s->sfs_flags & VPM_SFS_ANALYTIC_DSIGMA);
+  double* W = c->V + 3 * ld;
+  if (analytic) {
+    // Jt := DJ, Et := DE.
+    ENQP(c, ctx_pair(c, PASS_UJD, K, P, 0, n, 1.0, nullptr, c->U, c->J, nullptr, c->Jt));
+    ENQ(c, launch_stretch_vw(n, ld, c->J, c->Jt, c->G, s->transposed, c->V, W, c->st));
+    ENQP(c, ctx_pair(c, PASS_ZETAD, K, P, 0, n, 1.0, c->V, c->raw, nullptr, W, nullptr));
+    ENQ(c, launch_estr_finish_d(n, ld, c->raw, c->J, c->Jt, s->transposed, c->E, c->Et, c->st));
+  } else {
+    ENQP(c, ctx_pair(c, PASS_UJ, K, P, 0, n, 1.0, nullptr, c->U, c->J));
+    if (sfs) {
+      ENQ(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
+      ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
+      ENQ(c, launch_estr_finish(n, ld, c->raw, c->J, s->transposed, c->E, c->st));
+    }
+  }
+  if (s->sfs == VPM_SFS_CONSTANT) {
+    ENQ(c, launch_sfs_constant(nf, s->sfs_Cd, c->C, c->st));
+  } else if (dyn0) {
+    const double al = s->sfs_alpha;
+    if (!analytic) {
       ENQP(c, ctx_pair(c, PASS_UJ, K, P, 0, n, al, nullptr, c->Ut, c->Jt));
       ENQ(c, launch_stretch_v(n, ld, c->Jt, c->G, s->transposed, c->V, c->st));
       ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, al, c->V, c->raw, nullptr));
       ENQ(c, launch_estr_finish(n, ld, c->raw, c->Jt, s->transposed, c->Et, c->st));
-      SfsParams sp;
-      sp.alpha = al; sp.rlxf = s->sfs_rlxf; sp.minC = s->sfs_minC; sp.maxC = s->sfs_maxC;
-      sp.zeta0 = zeta0_of(K); sp.transposed = s->transposed;
-      sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
-      ENQ(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
     }
+    SfsParams sp;
+    sp.alpha = al; sp.rlxf = s->sfs_rlxf; sp.minC = s->sfs_minC; sp.maxC = s->sfs_maxC;
+    sp.zeta0 = zeta0_of(K); sp.transposed = s->transposed;
+    sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
+    sp.analytic = analytic ? 1 : 0;
+    ENQ(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
   }
+  return cudaSuccess;
+}
+
+// One stage of a step: U/J, SFS, fused update.
+static cudaError_t enqueue_stage(vpm_ctx* c, const vpm_scheme* s, double dt, double a, double b,
+                                 int stage) {
+  const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
+  const int K = s->kernel;
+  const bool sfs = s->sfs != VPM_SFS_NONE;
+  (void)n;
+  ENQP(c, enqueue_uj_sfs(c, s, stage));
   UpdateParams up;
   up.a = a; up.b = b; up.dt = dt;
   up.uinf0 = s->uinf[0]; up.uinf1 = s->uinf[1]; up.uinf2 = s->uinf[2];
@@ -505,8 +535,8 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   std::memset(c->pinned, 0, sizeof(c->pinned));
   const size_t ld = size_t(c->ld);
-  // State + evaluation rows: X3 G3 S1 C3 Q8 U3 J9 E3 V3 raw6 = 42 rows.
-  const size_t rows = 42;
+  // State + evaluation rows: X3 G3 S1 C3 Q8 U3 J9 E3 V6 raw12 = 51 rows.
+  const size_t rows = 51;
   if (cudaMalloc(&c->base, rows * ld * sizeof(double)) != cudaSuccess) {
     delete c;
     return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate the particle field");
@@ -520,8 +550,8 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   c->U = p; p += 3 * ld;
   c->J = p; p += 9 * ld;
   c->E = p; p += 3 * ld;
-  c->V = p; p += 3 * ld;
-  c->raw = p; p += 6 * ld;
+  c->V = p; p += 6 * ld;      // v rows 0..2, w rows 3..5
+  c->raw = p; p += 12 * ld;   // raw ζ sums (12 rows for the α-derivative pass)
   cudaError_t e = cudaMemset(c->base, 0, rows * ld * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c->status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(c->status, 0, sizeof(int));
@@ -699,36 +729,17 @@ int vpm_eval_sfs(vpm_ctx* c, const vpm_scheme* s) {
   if (rc) return rc;
   DeviceGuard dg(c->device);
   if (s->sfs == VPM_SFS_DYNAMIC && (rc = ensure_test_filter(c))) return rc;
-  // Same work as the first stage without the update: run the stage in dry
-  // mode to size scratch, then the SFS part for real.
-  const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
-  const int K = s->kernel, P = s->precision;
+  // The work of a step's first stage without the update: a dry pass sizes the
+  // scratch, then the same sequence is enqueued for real.
   c->dry = true;
   c->part_need = 0;
-  enqueue_stage(c, s, 0.0, 0.0, 0.0, 0);
+  enqueue_uj_sfs(c, s, 0);
   c->dry = false;
   if ((rc = ensure_part(c, c->part_need))) return rc;
-  CTX_CK(c, ctx_pair(c, PASS_UJ, K, P, 0, n, 1.0, nullptr, c->U, c->J));
-  CTX_CK(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
-  CTX_CK(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
-  CTX_CK(c, launch_estr_finish(n, ld, c->raw, c->J, s->transposed, c->E, c->st));
-  if (s->sfs == VPM_SFS_CONSTANT) {
-    CTX_CK(c, launch_sfs_constant(nf, s->sfs_Cd, c->C, c->st));
-  } else {
-    const double al = s->sfs_alpha;
-    CTX_CK(c, ctx_pair(c, PASS_UJ, K, P, 0, n, al, nullptr, c->Ut, c->Jt));
-    CTX_CK(c, launch_stretch_v(n, ld, c->Jt, c->G, s->transposed, c->V, c->st));
-    CTX_CK(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, al, c->V, c->raw, nullptr));
-    CTX_CK(c, launch_estr_finish(n, ld, c->raw, c->Jt, s->transposed, c->Et, c->st));
-    SfsParams sp;
-    sp.alpha = al; sp.rlxf = s->sfs_rlxf; sp.minC = s->sfs_minC; sp.maxC = s->sfs_maxC;
-    sp.zeta0 = zeta0_of(K); sp.transposed = s->transposed;
-    sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
-    CTX_CK(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
-  }
+  CTX_CK(c, enqueue_uj_sfs(c, s, 0));
   CTX_CK(c, cudaStreamSynchronize(c->st));
   c->uj_lo = 0;
-  c->uj_hi = n;
+  c->uj_hi = c->n;
   return VPM_OK;
 }
 

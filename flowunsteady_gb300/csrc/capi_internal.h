@@ -22,11 +22,13 @@ struct PairCall {
   int pass, kernel, prec;
   int64_t t0, t1, ns;
   const double *xs, *gs, *ss, *vs;
+  const double* ws = nullptr;   // PASS_ZETAD: w_q rows
   int64_t lds;
   const double* xt;
   int64_t ldt;
   double sigma_scale;
   double *u, *j;
+  double* dj = nullptr;         // PASS_UJD: DJ rows
   int64_t ldo;
   int max_chunks = 0;   // upper bound on source chunks (0 = planner's choice)
 };
@@ -111,7 +113,8 @@ struct vpm_ctx {
 // Pair pass of a context over targets [t0, t1) of its own particles (queue form
 // when the context backs a batch).
 cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int64_t t1,
-                     double scale, const double* vs, double* u, double* j);
+                     double scale, const double* vs, double* u, double* j,
+                     const double* ws = nullptr, double* dj = nullptr);
 // Build (or rebuild for another kernel/precision) the batch queue.
 int batch_plan(vpm_ctx* c, int kernel, int precision);
 // Host transfer helpers of capi.cu, reused by batches.

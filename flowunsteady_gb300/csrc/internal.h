@@ -8,10 +8,21 @@
 
 namespace vpm {
 
-// Pair passes.
-enum PairPass { PASS_UJ = 0, PASS_ZETA = 1 };
-constexpr int kNvalUJ = 15;    // Uacc(3), Aacc(9), Wacc(3)
-constexpr int kNvalZeta = 6;   // Ω(3) = Σ ζ Γ_q, V(3) = Σ ζ v_q
+// Pair passes.  The D forms also accumulate the derivative with respect to a
+// common scale α of every core size (d/dα at α = 1), for the analytic dynamic
+// SFS procedure.
+enum PairPass { PASS_UJ = 0, PASS_ZETA = 1, PASS_UJD = 2, PASS_ZETAD = 3 };
+constexpr int kNvalUJ = 15;     // Uacc(3), Aacc(9), Wacc(3)
+constexpr int kNvalZeta = 6;    // Ω(3) = Σ ζ Γ_q, V(3) = Σ ζ v_q
+constexpr int kNvalUJD = 27;    // UJ values, then DAacc(9), DWacc(3)
+constexpr int kNvalZetaD = 12;  // Ω, V, DΩ = Σ Dζ Γ_q, DV = Σ (Dζ v_q + ζ w_q)
+
+__host__ __device__ constexpr int nval_of(int pass) {
+  return pass == PASS_UJ ? kNvalUJ
+         : pass == PASS_ZETA ? kNvalZeta
+         : pass == PASS_UJD ? kNvalUJD
+                            : kNvalZetaD;
+}
 
 // One work item: targets [t0, t1) against sources [s0, s1).  slot < 0 means the
 // item covers all sources of its targets and writes final values; otherwise it
@@ -27,7 +38,8 @@ struct PairArgs {
   const double* xs;
   const double* gs;
   const double* ss;
-  const double* vs;   // PASS_ZETA: per-source S(J_q, Γ_q), 3 rows (may be null)
+  const double* vs;   // PASS_ZETA(D): per-source v_q = S(J_q, Γ_q), 3 rows (may be null)
+  const double* ws;   // PASS_ZETAD: per-source w_q = S(DJ_q, Γ_q), 3 rows
   int64_t lds;
   // Target positions: FP64 SoA of leading dimension ldt.
   const double* xt;
@@ -41,10 +53,12 @@ struct PairArgs {
   const PairItem* items;
   int32_t n_items;
   unsigned int* counter;
-  // Outputs.  Final: UJ -> U rows 0..2 of `u` (ld ldo), J rows 0..8 of `j`;
-  // ZETA -> raw Ω, V rows 0..5 of `u`.  Partials: part[(slot*nval + k)*ldp + i].
+  // Outputs.  Final: UJ -> U rows 0..2 of `u` (ld ldo), J rows 0..8 of `j`
+  // (UJD also DJ rows 0..8 of `dj`); ZETA(D) -> raw rows 0..5 (0..11) of `u`.
+  // Partials: part[(slot*nval + k)*ldp + i].
   double* u;
   double* j;
+  double* dj;
   int64_t ldo;
   double* part;
   int64_t ldp;
@@ -74,6 +88,17 @@ bool pair_shape_supported(int precision, Shape shape);
 cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
-                          double* j, int64_t ldo, cudaStream_t st);
+                          double* j, double* dj, int64_t ldo, cudaStream_t st);
+
+// The D passes live in pair_d.cu; launch_pair/launch_reduce/pair_ctas_per_sm/
+// pair_smem_bytes forward to these for PASS_UJD and PASS_ZETAD.
+cudaError_t launch_pair_d(int pass, int kernel, int precision, Shape shape, const PairArgs& a,
+                          int grid, cudaStream_t st);
+cudaError_t launch_reduce_d(int pass, int kernel, const double* part, int64_t ldp,
+                            const int64_t* foff, const int32_t* fchunks, int nfields,
+                            int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
+                            double* j, double* dj, int64_t ldo, cudaStream_t st);
+size_t pair_smem_bytes_d(int pass, int precision, Shape shape);
+int pair_ctas_per_sm_d(int pass, int kernel, int precision, Shape shape);
 
 }  // namespace vpm

@@ -57,6 +57,40 @@ __global__ void estr_finish_kernel(int64_t n, int64_t ld, const double* __restri
   E[2 * ld + i] = s2 - raw[5 * ld + i];
 }
 
+// v = S(J, Γ) and w = S(DJ, Γ) (per-source terms of the α-derivative ζ pass).
+__global__ void stretch_vw_kernel(int64_t n, int64_t ld, const double* __restrict__ J,
+                                  const double* __restrict__ DJ, const double* __restrict__ G,
+                                  int transposed, double* V, double* W) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double g0 = G[i], g1 = G[ld + i], g2 = G[2 * ld + i];
+  double s0, s1, s2;
+  stretch_dev(J, ld, i, g0, g1, g2, transposed, s0, s1, s2);
+  V[i] = s0; V[ld + i] = s1; V[2 * ld + i] = s2;
+  stretch_dev(DJ, ld, i, g0, g1, g2, transposed, s0, s1, s2);
+  W[i] = s0; W[ld + i] = s1; W[2 * ld + i] = s2;
+}
+
+// E = S(J, Ω) - V and DE = S(DJ, Ω) + S(J, DΩ) - DV from the raw sums of the
+// α-derivative ζ pass (rows 0..2 Ω, 3..5 V, 6..8 DΩ, 9..11 DV).
+__global__ void estr_finish_d_kernel(int64_t n, int64_t ld, const double* __restrict__ raw,
+                                     const double* __restrict__ J, const double* __restrict__ DJ,
+                                     int transposed, double* E, double* DE) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double o0 = raw[i], o1 = raw[ld + i], o2 = raw[2 * ld + i];
+  double s0, s1, s2, t0, t1, t2;
+  stretch_dev(J, ld, i, o0, o1, o2, transposed, s0, s1, s2);
+  E[i] = s0 - raw[3 * ld + i];
+  E[ld + i] = s1 - raw[4 * ld + i];
+  E[2 * ld + i] = s2 - raw[5 * ld + i];
+  stretch_dev(DJ, ld, i, o0, o1, o2, transposed, s0, s1, s2);
+  stretch_dev(J, ld, i, raw[6 * ld + i], raw[7 * ld + i], raw[8 * ld + i], transposed, t0, t1, t2);
+  DE[i] = s0 + t0 - raw[9 * ld + i];
+  DE[ld + i] = s1 + t1 - raw[10 * ld + i];
+  DE[2 * ld + i] = s2 + t2 - raw[11 * ld + i];
+}
+
 // Pseudo-three-level dynamic coefficient (once per step, first RK stage):
 //   nume = (3α-2) Γ·[S(J(ασ)) - S(J(σ))],  deno = σ³/ζ(0) Γ·[E(ασ) - E(σ)],
 //   Lagrangian average with rlxf, C_d = nume/deno, |C_d| forced/limited.
@@ -68,11 +102,20 @@ __global__ void sfs_dynamic_kernel(int64_t nf, int64_t ld, const double* __restr
   if (i >= nf) return;
   const double g0 = G[i], g1 = G[ld + i], g2 = G[2 * ld + i];
   double a0, a1, a2, b0, b1, b2;
-  stretch_dev(Jt, ld, i, g0, g1, g2, p.transposed, a0, a1, a2);
-  stretch_dev(J, ld, i, g0, g1, g2, p.transposed, b0, b1, b2);
-  double nume = g0 * (a0 - b0) + g1 * (a1 - b1) + g2 * (a2 - b2);
-  double deno = g0 * (Et[i] - E[i]) + g1 * (Et[ld + i] - E[ld + i]) +
-                g2 * (Et[2 * ld + i] - E[2 * ld + i]);
+  double nume, deno;
+  if (p.analytic) {
+    // Jt = DJ, Et = DE: the test-filter differences are (α-1)·D to first order.
+    const double h = p.alpha - 1.0;
+    stretch_dev(Jt, ld, i, g0, g1, g2, p.transposed, a0, a1, a2);
+    nume = h * (g0 * a0 + g1 * a1 + g2 * a2);
+    deno = h * (g0 * Et[i] + g1 * Et[ld + i] + g2 * Et[2 * ld + i]);
+  } else {
+    stretch_dev(Jt, ld, i, g0, g1, g2, p.transposed, a0, a1, a2);
+    stretch_dev(J, ld, i, g0, g1, g2, p.transposed, b0, b1, b2);
+    nume = g0 * (a0 - b0) + g1 * (a1 - b1) + g2 * (a2 - b2);
+    deno = g0 * (Et[i] - E[i]) + g1 * (Et[ld + i] - E[ld + i]) +
+           g2 * (Et[2 * ld + i] - E[2 * ld + i]);
+  }
   const double sg = S[i];
   nume *= 3.0 * p.alpha - 2.0;
   deno *= sg * sg * sg / p.zeta0;
@@ -310,6 +353,22 @@ cudaError_t launch_estr_finish(int64_t n, int64_t ld, const double* raw, const d
                                int transposed, double* E, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   estr_finish_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, ld, raw, J, transposed, E);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stretch_vw(int64_t n, int64_t ld, const double* J, const double* DJ,
+                              const double* G, int transposed, double* V, double* W,
+                              cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  stretch_vw_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, ld, J, DJ, G, transposed, V, W);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_estr_finish_d(int64_t n, int64_t ld, const double* raw, const double* J,
+                                 const double* DJ, int transposed, double* E, double* DE,
+                                 cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  estr_finish_d_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, ld, raw, J, DJ, transposed, E, DE);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@ struct SfsParams {
   double alpha, rlxf, minC, maxC, zeta0;
   int transposed;
   int force_positive;
+  int analytic;   // Jt, Et hold DJ, DE (analytic α-derivatives)
 };
 
 struct UpdateParams {
@@ -38,6 +39,12 @@ cudaError_t launch_stretch_v(int64_t n, int64_t ld, const double* J, const doubl
                              int transposed, double* V, cudaStream_t st);
 cudaError_t launch_estr_finish(int64_t n, int64_t ld, const double* raw, const double* J,
                                int transposed, double* E, cudaStream_t st);
+cudaError_t launch_stretch_vw(int64_t n, int64_t ld, const double* J, const double* DJ,
+                              const double* G, int transposed, double* V, double* W,
+                              cudaStream_t st);
+cudaError_t launch_estr_finish_d(int64_t n, int64_t ld, const double* raw, const double* J,
+                                 const double* DJ, int transposed, double* E, double* DE,
+                                 cudaStream_t st);
 cudaError_t launch_sfs_dynamic(int64_t nf, int64_t ld, const double* G, const double* S,
                                const double* J, const double* Jt, const double* E,
                                const double* Et, double* C, const SfsParams& p, cudaStream_t st);

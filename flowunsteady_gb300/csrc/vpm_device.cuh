@@ -342,3 +342,189 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
 }
 
 }  // namespace vpm
+
+// ------------------------------------------------------------------------------
+// α-derivative forms (d/dα at α = 1 of the sums with every σ scaled by α):
+//   D q = -ρ g'(ρ)/r³,  D(q'/r) = (2ρg' - ρ²g'')/r⁵, which reduce to
+//   Winckelmans:  D q = -15/2 σ⁴ s^{-7/2},  D p = D(q'/r)/KP = -35/2 σ⁴ s^{-9/2}
+//   Gaussian-erf: D q = -√(2/π) e/σ³,      D p = D(q'/r)     = √(2/π) e/σ⁵
+// (no cancellation in either), and D ζ_σ = ζ_σ (4 - 7/(ρ²+1)) or ζ_σ (ρ² - 3).
+namespace vpm {
+
+// 27 sums: U 0..2, A 3..11 (11 unused), W 12..14, DA 15..23 (23 unused), DW 24..26.
+__device__ __forceinline__ void accum_pair_d(float dx, float dy, float dz, float q, float p,
+                                             float dq, float dp, float gx, float gy, float gz,
+                                             float* acc) {
+  const float c0 = dy * gz - dz * gy;
+  const float c1 = dz * gx - dx * gz;
+  const float c2 = dx * gy - dy * gx;
+  acc[0] = fmaf(q, c0, acc[0]);
+  acc[1] = fmaf(q, c1, acc[1]);
+  acc[2] = fmaf(q, c2, acc[2]);
+  float a0 = p * c0, a1 = p * c1, a2 = p * c2;
+  acc[3] = fmaf(a0, dx, acc[3]);
+  acc[4] = fmaf(a0, dy, acc[4]);
+  acc[5] = fmaf(a0, dz, acc[5]);
+  acc[6] = fmaf(a1, dx, acc[6]);
+  acc[7] = fmaf(a1, dy, acc[7]);
+  acc[8] = fmaf(a1, dz, acc[8]);
+  acc[9] = fmaf(a2, dx, acc[9]);
+  acc[10] = fmaf(a2, dy, acc[10]);
+  acc[12] = fmaf(q, gx, acc[12]);
+  acc[13] = fmaf(q, gy, acc[13]);
+  acc[14] = fmaf(q, gz, acc[14]);
+  a0 = dp * c0; a1 = dp * c1; a2 = dp * c2;
+  acc[15] = fmaf(a0, dx, acc[15]);
+  acc[16] = fmaf(a0, dy, acc[16]);
+  acc[17] = fmaf(a0, dz, acc[17]);
+  acc[18] = fmaf(a1, dx, acc[18]);
+  acc[19] = fmaf(a1, dy, acc[19]);
+  acc[20] = fmaf(a1, dz, acc[20]);
+  acc[21] = fmaf(a2, dx, acc[21]);
+  acc[22] = fmaf(a2, dy, acc[22]);
+  acc[24] = fmaf(dq, gx, acc[24]);
+  acc[25] = fmaf(dq, gy, acc[25]);
+  acc[26] = fmaf(dq, gz, acc[26]);
+}
+
+template <int T, bool MASK>
+__device__ __forceinline__ void ujd_source_winck(const float4 sa, const float4 sb,
+                                                 const float (&tx)[T], const float (&ty)[T],
+                                                 const float (&tz)[T], float (&acc)[T][27]) {
+  const float s2 = sa.w, k15 = sb.w, k25 = sa.w + sb.w;
+  const float c75 = -7.5f * s2 * s2, c175 = -17.5f * s2 * s2;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float rs = rsqrt_ftz(r2 + s2);
+    const float rs2 = rs * rs;
+    const float rs3 = rs2 * rs;
+    const float rs5 = rs3 * rs2;
+    const float rs7 = rs5 * rs2;
+    float q = fmaf(k15, rs5, rs3);
+    float dq = c75 * rs7;
+    if (MASK) {
+      q = r2 > 0.f ? q : 0.f;
+      dq = r2 > 0.f ? dq : 0.f;
+    }
+    const float p = fmaf(k25, rs7, rs5);
+    const float dp = c175 * (rs7 * rs2);
+    accum_pair_d(dx, dy, dz, q, p, dq, dp, sb.x, sb.y, sb.z, acc[k]);
+  }
+}
+
+template <int T>
+__device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 sb,
+                                                 const float (&tx)[T], const float (&ty)[T],
+                                                 const float (&tz)[T], float (&acc)[T][27]) {
+  const float ea = sa.w, is1 = sb.w;
+  const float kt = kErfcxP * is1;
+  const float kc = float(kSqrt2overPi) * is1;
+  const float is2 = is1 * is1;
+  const float k3 = float(kSqrt2overPi) * is2 * is1;
+  float dx[T], dy[T], dz[T], arg[T], q[T], p[T], dq[T], dp[T];
+  float amax = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    dx[k] = tx[k] - sa.x;
+    dy[k] = ty[k] - sa.y;
+    dz[k] = tz[k] - sa.z;
+    const float r2 = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
+    arg[k] = r2 * ea;
+    amax = fmaxf(amax, arg[k]);
+    const float ri = rsqrt_ftz(r2);
+    const float r = r2 * ri;
+    const float e = ex2_ftz(arg[k]);
+    const float t = rcp_ftz(fmaf(kt, r, 1.f));
+    const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
+    const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
+    const float ri2 = ri * ri;
+    const float k3e = k3 * e;
+    q[k] = g * (ri2 * ri);
+    p[k] = fmaf(-3.f, q[k], k3e) * ri2;
+    dq[k] = -k3e;
+    dp[k] = k3e * is2;
+  }
+  if (__any_sync(0xffffffffu, amax > kArgSeries)) {
+    const float is3 = is2 * is1, is5 = is3 * is2;
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      if (arg[k] > kArgSeries) {
+        float h1, h2;
+        GaussSeries<float, 10>::eval(arg[k] * kArgToRho2, h1, h2);
+        const bool self = arg[k] == 0.f;
+        q[k] = self ? 0.f : h1 * is3;
+        p[k] = self ? 0.f : h2 * is5;
+        dq[k] = self ? 0.f : dq[k];
+        dp[k] = self ? 0.f : dp[k];
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < T; ++k)
+    accum_pair_d(dx[k], dy[k], dz[k], q[k], p[k], dq[k], dp[k], sb.x, sb.y, sb.z, acc[k]);
+}
+
+// FP64 α-derivatives of one pair (zero when r² == 0).
+//   Winckelmans: a = σ², b = 3/2 σ²;  Gaussian-erf: a = 1/σ², b = 1/σ.
+template <int KERNEL>
+__device__ inline void pair_dqp_f64(double r2, double a, double b, double& dq, double& dp) {
+  if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+    const double s = r2 + a;
+    const double rs = rsqrt(s);
+    const double rs2 = rs * rs;
+    const double rs7 = rs2 * rs2 * rs2 * rs;
+    dq = -7.5 * a * a * rs7;
+    dp = -17.5 * a * a * rs7 * rs2;
+  } else {
+    const double e = exp(-0.5 * r2 * a);
+    const double k3 = kSqrt2overPi * b * b * b;
+    dq = -k3 * e;
+    dp = k3 * e * a;
+  }
+  if (!(r2 > 0.0)) {
+    dq = 0.0;
+    dp = 0.0;
+  }
+}
+
+// ζ_σ and D ζ_σ of one pair from the ζ source constants (zero when r² == 0):
+//   Winckelmans a = 1/σ², b = 15/(8π)/σ³;  Gaussian-erf a = -log2(e)/(2σ²), b = (2π)^{-3/2}/σ³.
+template <int KERNEL>
+__device__ inline void pair_zeta_d(float r2, float a, float b, float& z, float& dz) {
+  if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+    const float rs = rsqrt_ftz(fmaf(r2, a, 1.f));
+    const float rs2 = rs * rs;
+    z = b * (rs2 * rs2) * (rs2 * rs);
+    dz = z * fmaf(-7.f, rs2, 4.f);
+  } else {
+    const float x = r2 * a;
+    z = b * ex2_ftz(x);
+    dz = z * fmaf(x, kArgToRho2, -3.f);
+  }
+  if (!(r2 > 0.f)) {
+    z = 0.f;
+    dz = 0.f;
+  }
+}
+template <int KERNEL>
+__device__ inline void pair_zeta_d(double r2, double a, double b, double& z, double& dz) {
+  if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+    const double s = fma(r2, a, 1.0);
+    const double rs = rsqrt(s);
+    const double rs2 = rs * rs;
+    z = b * rs2 * rs2 * rs2 * rs;
+    dz = z * (4.0 - 7.0 * rs2);
+  } else {
+    const double x = r2 * a;
+    z = b * exp2(x);
+    dz = z * (x * (-2.0 / kLog2e) - 3.0);
+  }
+  if (!(r2 > 0.0)) {
+    z = 0.0;
+    dz = 0.0;
+  }
+}
+
+}  // namespace vpm

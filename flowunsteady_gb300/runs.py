@@ -82,11 +82,13 @@ def stretching(J, G):
     return np.einsum("iba,ib->ia", J, G)
 
 
-def scheme_for(kernel, prec, sfs=L.SFS_DYNAMIC, nu=1e-4, rlxf=1.0):
+def scheme_for(kernel, prec, sfs=L.SFS_DYNAMIC, nu=1e-4, rlxf=1.0, analytic=True):
     s = L.default_scheme()
     s.kernel, s.precision = kernel, prec
     s.sfs = sfs
     s.sfs_flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE
+    if analytic:
+        s.sfs_flags |= L.SFS_ANALYTIC_DSIGMA
     s.sfs_alpha, s.sfs_rlxf, s.sfs_minC, s.sfs_maxC = 0.999, rlxf, 0.0, 1.0
     s.nu = nu
     return s
@@ -153,9 +155,12 @@ def run_rings(args):
     k = L.KERNEL_GAUSSIANERF
     res = {"workload": "leapfrogging rings, 2 x 200 x 19 = 7,600 particles", "n": n,
            "dt": 0.005, "steps": nsteps, "runs": {}}
-    for pname, p in (("fp64", L.PREC_FP64), ("fp32c", L.PREC_FP32C)):
+    finals = {}
+    for pname, p, an in (("fp64", L.PREC_FP64, False), ("fp32c", L.PREC_FP32C, False),
+                         ("fp64_analytic", L.PREC_FP64, True),
+                         ("fp32c_analytic", L.PREC_FP32C, True)):
         f = Field(X, G, S)
-        sc = scheme_for(k, p)
+        sc = scheme_for(k, p, analytic=an)
         hist = [{"step": 0, **ring_observables(f, k, L.PREC_FP64, nh)}]
         t_run = 0.0
         for s0 in range(0, nsteps, every):
@@ -166,14 +171,17 @@ def run_rings(args):
         res["runs"][pname] = {"history": hist, "seconds_stepping": t_run,
                               "steps_per_s": nsteps / t_run}
         res["runs"][pname]["final_state"] = [a.tolist() for a in f.state()] if args.keep else None
-        if pname == "fp64":
-            X64, G64, S64 = f.state()
-        else:
-            X32, G32, S32 = f.state()
+        finals[pname] = f.state()
         f.close()
-    res["fp32c_vs_fp64_final"] = {"max_abs_dx": float(np.abs(X32 - X64).max()),
-                                  "rel_l2_gamma": rel_l2(G32, G64),
-                                  "max_abs_dsigma": float(np.abs(S32 - S64).max())}
+
+    def cmp(a, b):
+        (Xa, Ga, Sa), (Xb, Gb, Sb) = finals[a], finals[b]
+        return {"max_abs_dx": float(np.abs(Xa - Xb).max()), "rel_l2_gamma": rel_l2(Ga, Gb),
+                "max_abs_dsigma": float(np.abs(Sa - Sb).max())}
+
+    res["fp32c_vs_fp64_final"] = cmp("fp32c", "fp64")
+    res["fp32c_analytic_vs_fp64_analytic_final"] = cmp("fp32c_analytic", "fp64_analytic")
+    res["fp64_analytic_vs_fp64_final"] = cmp("fp64_analytic", "fp64")
     return res
 
 
@@ -254,6 +262,7 @@ def run_large(args):
     against the FP64 direct sum of the same state."""
     n = args.n or 1048576
     nsteps = args.steps or 20
+    dt = args.dt or 0.002
     X, G, S = helical_wake(n, turns=12)
     f = Field(X, G, S)
     k = L.KERNEL_GAUSSIANERF
@@ -264,7 +273,7 @@ def run_large(args):
     import torch
     dev = torch.device("cuda:0")
     for s in range(nsteps):
-        _, t = timed(lambda: f.step(sc, 0.002, 1))
+        _, t = timed(lambda: f.step(sc, dt, 1))
         t_steps += t
         Xs, Gs, Ss = f.state()
         idx = np.sort(rng.choice(n, 4096, replace=False))
@@ -288,7 +297,7 @@ def run_large(args):
                        "rel_l2_stretching": rel_l2(stretching(J32, Gs[idx]), stretching(J64, Gs[idx]))})
     d = f.diag(k, L.PREC_FP32C)
     f.close()
-    return {"workload": f"helical wake N={n}, 12 turns", "steps": nsteps, "dt": 0.002,
+    return {"workload": f"helical wake N={n}, 12 turns", "steps": nsteps, "dt": dt,
             "seconds_stepping": t_steps, "seconds_per_step": t_steps / nsteps,
             "uj_pairs_per_step": 4 * n * n, "checks": checks,
             "max_rel_l2_U": max(c["rel_l2_U"] for c in checks),
@@ -301,6 +310,7 @@ def main(argv=None):
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--steps", type=int, default=None)
     p.add_argument("--fields", type=int, default=None)
+    p.add_argument("--dt", type=float, default=None)
     p.add_argument("--keep", action="store_true", help="include the final state (rings)")
     p.add_argument("--no-reference", action="store_true", help="batch: skip the FP64 fields")
     p.add_argument("--out", default=None)

@@ -90,6 +90,11 @@ enum {
 /* sfs_flags bits */
 #define VPM_SFS_CLIP_BACKSCATTER 1u   /* vpm.clipping_backscatter: C_d = 0 where C_d Γ·E_str < 0 */
 #define VPM_SFS_FORCE_POSITIVE 2u     /* the "_positive" procedure: C_d = |C_d|                    */
+/* Dynamic procedure with the σ-derivatives taken analytically (d/dα at α = 1,
+ * computed inside the pair passes) instead of the finite difference between the
+ * σ and ασ filter levels.  The two agree to O(1-α); the analytic form avoids the
+ * 1/(1-α) amplification of rounding noise, which matters for FP32/FP32C passes. */
+#define VPM_SFS_ANALYTIC_DSIGMA 4u
 
 /* Relaxation of Γ towards the local vorticity (FLOWVPM's vpm.pedrizzetti). */
 enum { VPM_RELAX_NONE = 0, VPM_RELAX_PEDRIZZETTI = 1 };
@@ -105,7 +110,7 @@ typedef struct vpm_scheme {
   double uinf[3];        /* freestream velocity added to dx/dt                      */
   double nu;             /* core-spreading viscosity, d(σ²)/dt = 2ν; 0 = inviscid   */
   int32_t sfs;           /* VPM_SFS_*                                               */
-  uint32_t sfs_flags;    /* VPM_SFS_CLIP_BACKSCATTER | VPM_SFS_FORCE_POSITIVE       */
+  uint32_t sfs_flags;    /* VPM_SFS_CLIP_BACKSCATTER | _FORCE_POSITIVE | _ANALYTIC_DSIGMA */
   double sfs_alpha;      /* test-filter ratio of the dynamic procedure (0.999)      */
   double sfs_rlxf;       /* Lagrangian-average relaxation factor (1 = no averaging) */
   double sfs_minC;       /* |C_d| floor (0 = none)                                  */

@@ -67,6 +67,10 @@ def lib():
         _lib.orc_diagnostics.argtypes = [ctypes.c_int, _i64, _i64, _dp, _dp, _dp, _dp, _dp,
                                          ctypes.c_int]
         _lib.orc_relax_pedrizzetti.argtypes = [_i64, ctypes.c_double, _dp, _dp]
+        _lib.orc_uj_direct_dsigma.argtypes = [ctypes.c_int, _i64, _dp, _i64, _dp, _dp, _dp, _dp,
+                                              ctypes.c_int]
+        _lib.orc_estr_direct_dsigma.argtypes = [ctypes.c_int, ctypes.c_int, _i64, _dp, _dp, _dp,
+                                                _dp, _dp, _dp, ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
     return _lib
 
@@ -116,6 +120,26 @@ def estr_direct(kernel, X, G, S, J, transposed=True, sigma_scale=1.0, nthreads=0
     lib().orc_estr_direct(kernel, sigma_scale, int(transposed), n, _p(X), _p(J), _p(S), n, _p(X),
                           _p(G), _p(S), _p(J), _p(E) if J is not None else None, _p(om), nthreads)
     return (E if J is not None else None), om
+
+
+def uj_dsigma(kernel, X, G, S, Xt=None, nthreads=0):
+    """dJ/dα (nt,3,3) for core sizes ασ at α = 1."""
+    X, G, S = _c(X, (3,)), _c(G, (3,)), _c(S, ())
+    Xt = X if Xt is None else _c(Xt, (3,))
+    DJ = np.empty((Xt.shape[0], 3, 3))
+    lib().orc_uj_direct_dsigma(kernel, Xt.shape[0], _p(Xt), X.shape[0], _p(X), _p(G), _p(S),
+                               _p(DJ), nthreads)
+    return DJ
+
+
+def estr_dsigma(kernel, X, G, S, J, DJ, transposed=True, nthreads=0):
+    """dE_str/dα (n,3) at α = 1 (targets = sources)."""
+    X, G, S = _c(X, (3,)), _c(G, (3,)), _c(S, ())
+    J, DJ = _c(J, (3, 3)), _c(DJ, (3, 3))
+    DE = np.empty((X.shape[0], 3))
+    lib().orc_estr_direct_dsigma(kernel, int(transposed), X.shape[0], _p(X), _p(G), _p(S), _p(J),
+                                 _p(DJ), _p(DE), nthreads)
+    return DE
 
 
 def step(scheme_struct, X, G, S, C, dt, n_static=0, nsteps=1, nthreads=0):

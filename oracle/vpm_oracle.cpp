@@ -124,6 +124,31 @@ inline void kernel_q(int kernel, double r2, double sig, double* q, double* qr) {
   *qr = (rhodg - 3.0 * g) * ir3 * ir2;
 }
 
+// Analytic derivatives with respect to a common scale α of all core sizes,
+// D = d/dα at α = 1 = Σ σ ∂/∂σ (used by the analytic dynamic procedure):
+//   D q      = -ρ g'(ρ)/r³,  D (q'/r) = (2ρ g' - ρ² g'')/r⁵,
+//   Winckelmans: D q = -15/2 σ⁴/s^{7/2},  D(q'/r) = 105/2 σ⁴/s^{9/2}  (s = r²+σ²)
+//   Gaussian-erf: D q = -√(2/π) e/σ³,   D(q'/r) = √(2/π) e/σ⁵        (e = e^{-ρ²/2})
+//   D ζ_σ = -3ζ_σ - ρ ζ'(ρ)/σ³:  Winckelmans ζ_σ (4 - 7/(ρ²+1)),  Gaussian ζ_σ (ρ² - 3).
+inline void kernel_dq(int kernel, double r2, double sig, double* dq, double* dqr) {
+  if (kernel == VPM_KERNEL_WINCKELMANS) {
+    double s2 = sig * sig, s = r2 + s2;
+    double rs = 1.0 / std::sqrt(s), rs2 = rs * rs;
+    double rs7 = rs2 * rs2 * rs2 * rs;
+    *dq = -7.5 * s2 * s2 * rs7;
+    *dqr = 52.5 * s2 * s2 * rs7 * rs2;
+    return;
+  }
+  double e = std::exp(-0.5 * r2 / (sig * sig));
+  double k3 = kSqrt2overPi / (sig * sig * sig);
+  *dq = -k3 * e;
+  *dqr = k3 * e / (sig * sig);
+}
+
+inline double dzeta_factor(int kernel, double rho2) {
+  return kernel == VPM_KERNEL_WINCKELMANS ? 4.0 - 7.0 / (rho2 + 1.0) : rho2 - 3.0;
+}
+
 // S(J, v): classic (J v) or transposed (Jᵀ v).
 inline void stretch(const double* J, const double* v, int transposed, double* S) {
   if (transposed) {
@@ -244,6 +269,70 @@ int orc_estr_direct(int kernel, double sigma_scale, int transposed, int64_t nt, 
   return 0;
 }
 
+// D J (the α-derivative of J) at nt targets, same conventions as orc_uj_direct.
+int orc_uj_direct_dsigma(int kernel, int64_t nt, const double* Xt, int64_t ns, const double* Xs,
+                         const double* Gs, const double* Ss, double* DJ, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < nt; ++i) {
+    double jac[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t j = 0; j < ns; ++j) {
+      const double dx = Xt[3 * i] - Xs[3 * j], dy = Xt[3 * i + 1] - Xs[3 * j + 1],
+                   dz = Xt[3 * i + 2] - Xs[3 * j + 2];
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 == 0.0) continue;
+      double dq, dqr;
+      kernel_dq(kernel, r2, Ss[j], &dq, &dqr);
+      const double g0 = Gs[3 * j], g1 = Gs[3 * j + 1], g2 = Gs[3 * j + 2];
+      const double c[3] = {dy * g2 - dz * g1, dz * g0 - dx * g2, dx * g1 - dy * g0};
+      const double d[3] = {dx, dy, dz};
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) jac[3 * a + b] += dqr * c[a] * d[b];
+      jac[1] += dq * g2; jac[2] -= dq * g1;
+      jac[3] -= dq * g2; jac[5] += dq * g0;
+      jac[6] += dq * g1; jac[7] -= dq * g0;
+    }
+    for (int k = 0; k < 9; ++k) DJ[9 * i + k] = -kInv4Pi * jac[k];
+  }
+  return 0;
+}
+
+// D E_str with targets = sources: D E_p = S(DJ_p, Ω_p) + S(J_p, DΩ_p) - DV_p,
+// DΩ_p = Σ Dζ Γ_q, DV_p = Σ [Dζ S(J_q,Γ_q) + ζ S(DJ_q,Γ_q)] (coincident pairs skipped).
+int orc_estr_direct_dsigma(int kernel, int transposed, int64_t n, const double* X, const double* G,
+                           const double* S, const double* J, const double* DJ, double* DE,
+                           int nthreads) {
+  set_threads(nthreads);
+  std::vector<double> v(3 * (size_t)n), w(3 * (size_t)n);
+  for (int64_t q = 0; q < n; ++q) {
+    stretch(J + 9 * q, G + 3 * q, transposed, &v[3 * q]);
+    stretch(DJ + 9 * q, G + 3 * q, transposed, &w[3 * q]);
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t p = 0; p < n; ++p) {
+    double om[3] = {0, 0, 0}, dom[3] = {0, 0, 0}, dv[3] = {0, 0, 0};
+    for (int64_t q = 0; q < n; ++q) {
+      const double dx = X[3 * p] - X[3 * q], dy = X[3 * p + 1] - X[3 * q + 1],
+                   dz = X[3 * p + 2] - X[3 * q + 2];
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 == 0.0) continue;
+      const double sg = S[q], rho2 = r2 / (sg * sg);
+      const double z = zeta_of(kernel, rho2) / (sg * sg * sg);
+      const double dz_ = z * dzeta_factor(kernel, rho2);
+      for (int a = 0; a < 3; ++a) {
+        om[a] += z * G[3 * q + a];
+        dom[a] += dz_ * G[3 * q + a];
+        dv[a] += dz_ * v[3 * q + a] + z * w[3 * q + a];
+      }
+    }
+    double s1[3], s2[3];
+    stretch(DJ + 9 * p, om, transposed, s1);
+    stretch(J + 9 * p, dom, transposed, s2);
+    for (int a = 0; a < 3; ++a) DE[3 * p + a] = s1[a] + s2[a] - dv[a];
+  }
+  return 0;
+}
+
 // One time step of the full method on n particles, the last n_static of which
 // act as sources only.  X, G, S are advanced in place; C (n,3) holds the SFS
 // memory (C_d, <Γ·L>, <Γ·m>) across steps.  E_out (n,3) receives the last
@@ -274,11 +363,22 @@ int orc_step(const vpm_scheme* sc, int64_t n, int64_t n_static, double dt, doubl
       if (sc->sfs == VPM_SFS_CONSTANT) {
         for (int64_t p = 0; p < nf; ++p) C[3 * p] = sc->sfs_Cd;
       } else if (st == 0) {
-        // Dynamic procedure with the test filter ασ.
         const double al = sc->sfs_alpha;
+        if (sc->sfs_flags & VPM_SFS_ANALYTIC_DSIGMA) {
+          // Jt, Et := first-order test-filter values J + (α-1) DJ, E + (α-1) DE,
+          // so the differences below are (α-1) DJ and (α-1) DE.
+          std::vector<double> DJ(9 * n), DE(3 * n);
+          orc_uj_direct_dsigma(kernel, n, X, n, X, G, S, DJ.data(), nthreads);
+          orc_estr_direct_dsigma(kernel, sc->transposed, n, X, G, S, J.data(), DJ.data(),
+                                 DE.data(), nthreads);
+          for (int64_t k = 0; k < 9 * n; ++k) Jt[k] = J[k] + (al - 1.0) * DJ[k];
+          for (int64_t k = 0; k < 3 * n; ++k) Et[k] = E[k] + (al - 1.0) * DE[k];
+        } else {
+        // Dynamic procedure with the test filter ασ.
         orc_uj_direct(kernel, al, n, X, n, X, G, S, Ut.data(), Jt.data(), nthreads);
         orc_estr_direct(kernel, al, sc->transposed, n, X, Jt.data(), S, n, X, G, S, Jt.data(),
                         Et.data(), nullptr, nthreads);
+        }
         for (int64_t p = 0; p < nf; ++p) {
           double s1[3], s0[3];
           stretch(&Jt[9 * p], G + 3 * p, sc->transposed, s1);

@@ -35,12 +35,31 @@ def test_leapfrog_rings_full_scheme_matches_oracle(oracle):
     assert rel_l2(Gg, Go) <= 1e-10 and np.abs(Sg - So).max() <= 1e-13
     assert rel_l2(Cg[:, 0], Co[:, 0]) <= 1e-6
     assert abs(d[0] - d0[0]) <= 1e-10 * abs(d0[0]) and abs(d[3] - d0[3]) <= 1e-12 * abs(d0[3])
-    # FP32C trajectory stays within FP32-level distance of the FP64 one.
+    # FP32C pair passes with the finite-difference C_d: the (α-1)^{-1} = 1000
+    # amplification of FP32 noise in C_d shows in the trajectory.
     with Ctx(X.shape[0]) as c:
         c.set(X, G, S)
         c.step(ring_scheme(L.PREC_FP32C), 0.005, nsteps=10)
         X32, G32, S32 = c.state()
-    assert np.abs(X32 - Xo).max() <= 1e-7 and rel_l2(G32, Go) <= 1e-5
+    assert np.abs(X32 - Xo).max() <= 1e-4 and rel_l2(G32, Go) <= 1e-3
+
+
+def test_leapfrog_rings_analytic_sfs_fp32c_tracks_fp64(oracle):
+    # With the analytic α-derivatives the FP32C trajectory stays at FP32 distance.
+    X, G, S = leapfrog_rings()
+    flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
+    s64 = scheme(kernel=1, prec=L.PREC_FP64, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
+    Xo, Go, So, Co, _ = oracle.step(s64, X, G, S, None, 0.005, nsteps=10)
+    with Ctx(X.shape[0]) as c:
+        c.set(X, G, S)
+        c.step(s64, 0.005, nsteps=10)
+        X64, G64, _ = c.state()
+        assert np.abs(X64 - Xo).max() <= 1e-12 and rel_l2(G64, Go) <= 1e-10
+        s32 = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
+        c.set(X, G, S)
+        c.step(s32, 0.005, nsteps=10)
+        X32, G32, _ = c.state()
+    assert np.abs(X32 - Xo).max() <= 1e-7 and rel_l2(G32, Go) <= 1e-6
 
 
 def test_pedrizzetti_relaxation_matches_oracle(oracle):

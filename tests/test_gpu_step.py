@@ -134,3 +134,27 @@ def test_ring_diagnostics_match_oracle(oracle):
     ref = np.array([(w[:n, None] * Xo[:n]).sum(0) / w[:n].sum(),
                     (w[n:, None] * Xo[n:]).sum(0) / w[n:].sum()])
     assert np.allclose(cen, ref, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("k", [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF])
+def test_step_analytic_dynamic_sfs_matches_oracle(oracle, k):
+    X, G, S = small_field(300, 87)
+    flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
+    sc = scheme(kernel=k, prec=L.PREC_FP64, sfs=L.SFS_DYNAMIC, flags=flags, rlxf=0.5,
+                nu=1e-4 if k == L.KERNEL_GAUSSIANERF else 0.0)
+    Xo, Go, So, Co, Eo = oracle.step(sc, X, G, S, None, 0.01, nsteps=2)
+    with Ctx(300) as c:
+        c.set(X, G, S)
+        c.step(sc, 0.01, nsteps=2)
+        Xg, Gg, Sg = c.state()
+        Cg, Eg = c.sfs()
+        assert rel_max(Xg, Xo) <= 1e-12 and rel_max(Gg, Go) <= 1e-10 and rel_max(Sg, So) <= 1e-12
+        assert rel_max(Cg, Co) <= 1e-9 and rel_max(Eg, Eo) <= 1e-10
+        # FP32C pair passes: the analytic α-derivatives keep C_d close to FP64.
+        sc.precision = L.PREC_FP32C
+        c.set(X, G, S)
+        c.step(sc, 0.01, nsteps=2)
+        C32, _ = c.sfs()
+        m = (Co[:, 0] != 0) & (C32[:, 0] != 0)
+        assert m.sum() > 50
+        assert np.median(np.abs(C32[m, 0] - Co[m, 0]) / np.abs(Co[m, 0])) < 1e-4

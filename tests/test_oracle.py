@@ -151,3 +151,34 @@ def test_thin_ring_self_induced_speed(oracle):
     delta = np.sqrt(2.0) * np.hypot(0.06, 0.05)
     saffman = 1.0 / (4 * np.pi) * (np.log(8 / delta) - 0.558)
     assert 0.85 * saffman < uz < 1.15 * saffman
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_analytic_sigma_derivatives_match_finite_differences(oracle, k):
+    # d/dα at α = 1 of J(ασ) and E_str(ασ) against central differences in α.
+    X, G, S = field(150, 41 + k, 0.08, 0.3)
+    DJ = oracle.uj_dsigma(k, X, G, S)
+    h = 1e-5
+    _, Jp = oracle.uj_direct(k, X, G, S, sigma_scale=1 + h)
+    _, Jm = oracle.uj_direct(k, X, G, S, sigma_scale=1 - h)
+    assert rel_max(DJ, (Jp - Jm) / (2 * h)) < 1e-7
+    _, J = oracle.uj_direct(k, X, G, S)
+    for tr in (0, 1):
+        DE = oracle.estr_dsigma(k, X, G, S, J, DJ, transposed=tr)
+        Ep, _ = oracle.estr_direct(k, X, G, S, Jp, transposed=tr, sigma_scale=1 + h)
+        Em, _ = oracle.estr_direct(k, X, G, S, Jm, transposed=tr, sigma_scale=1 - h)
+        assert rel_max(DE, (Ep - Em) / (2 * h)) < 1e-6
+
+
+def test_analytic_and_finite_difference_dynamic_cd_agree(oracle):
+    # Both dynamic procedures estimate the same C_d up to O(1 - α).
+    X, G, S = field(200, 45, 0.1, 0.3)
+    X *= 0.5
+    G *= 300
+    fd = scheme(kernel=1, sfs=1, flags=1 | 2)
+    an = scheme(kernel=1, sfs=1, flags=1 | 2 | 4)
+    _, _, _, Cf, _ = oracle.step(fd, X, G, S, None, 0.005)
+    _, _, _, Ca, _ = oracle.step(an, X, G, S, None, 0.005)
+    m = (Cf[:, 0] != 0) & (Ca[:, 0] != 0)
+    assert m.sum() > 20
+    assert np.median(np.abs(Ca[m, 0] - Cf[m, 0]) / np.abs(Cf[m, 0])) < 1e-2
