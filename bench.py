@@ -251,6 +251,13 @@ def run_ours(args, world, rank, local, dist):
     prec = {"fp32c": L.PREC_FP32C, "fp32": L.PREC_FP32, "fp64": L.PREC_FP64}[args.precision]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
+    tuned = None
+    if not args.tile and not args.timed_only:
+        # Tile shape for this size bucket from the autotuner (one timed
+        # evaluation per compiled shape); later evaluations use it.
+        tile, tms = L.Tile(), ctypes.c_double()
+        L.check(lib.vpm_autotune(ctx, kernel, prec, ctypes.byref(tile), ctypes.byref(tms)), ctx)
+        tuned = f"{tile.block}x{tile.tpt}"
     for _ in range(args.warmup):
         L.check(lib.vpm_eval_UJ(ctx, kernel, prec), ctx)
     torch.cuda.synchronize(dev)
@@ -283,6 +290,28 @@ def run_ours(args, world, rank, local, dist):
     value = world * args.steps * pairs / total_s
     ms_per_step = 1e3 * total_s / args.steps
     launches = int(l1.value - l0.value)
+    # The other kernel, timed the same way (reported beside the headline).
+    other = None
+    if not args.timed_only:
+        k2 = L.KERNEL_WINCKELMANS if kernel == L.KERNEL_GAUSSIANERF else L.KERNEL_GAUSSIANERF
+        tile2, tms2 = L.Tile(), ctypes.c_double()
+        L.check(lib.vpm_autotune(ctx, k2, prec, ctypes.byref(tile2), ctypes.byref(tms2)), ctx)
+        for _ in range(2):
+            L.check(lib.vpm_eval_UJ(ctx, k2, prec), ctx)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            L.check(lib.vpm_eval_UJ(ctx, k2, prec), ctx)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        ms2 = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+        other = {"kernel": "winckelmans" if k2 == L.KERNEL_WINCKELMANS else "gaussianerf",
+                 "ms_per_step": ms2, "pairs_per_s": float(n) * n / (ms2 / 1e3),
+                 "tile": f"{tile2.block}x{tile2.tpt}",
+                 "frac_of_fp32_fma_peak": (PAIR_FLOP * float(n) * n / (ms2 / 1e3) / 1e12 / f32.value
+                                           if f32.value > 0 else None)}
     if args.timed_only:
         if rank == 0:
             print(json.dumps({"timed_only": True, "ms_per_step": ms_per_step,
@@ -381,6 +410,8 @@ def run_ours(args, world, rank, local, dist):
             "fp32c_over_fp64": value / world / fp64_rate,
             "clocks": clk.summary(),
             "step_ms": step_ms,
+            "tile": args.tile or tuned,
+            "other_kernel": other,
         }
         print(json.dumps(line))
     lib.vpm_ctx_destroy(ctx)

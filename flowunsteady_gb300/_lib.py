@@ -52,7 +52,7 @@ EXPORTS = [
     "vpm_ctx_set_stream", "vpm_get_time", "vpm_set_time", "vpm_set_particles", "vpm_append",
     "vpm_truncate", "vpm_get_np", "vpm_get_state", "vpm_get_sfs", "vpm_eval_UJ",
     "vpm_eval_UJ_targets", "vpm_get_UJ", "vpm_eval_sfs", "vpm_step", "vpm_diagnostics",
-    "vpm_centroids", "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
+    "vpm_centroids", "vpm_ffv_direct", "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
     "vpm_batch_last_error", "vpm_batch_set_stream", "vpm_batch_set_field",
     "vpm_batch_get_field", "vpm_batch_eval_UJ", "vpm_batch_get_UJ", "vpm_batch_step",
     "vpm_autotune", "vpm_set_tile", "vpm_measure_fma_peaks", "vpm_debug_fail_after",
@@ -124,6 +124,8 @@ def _declare(lib):
         "vpm_step": (ctypes.c_int, [_vp, ctypes.c_double, P(Scheme), _i64, ctypes.c_int]),
         "vpm_diagnostics": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
         "vpm_centroids": (ctypes.c_int, [_vp, ctypes.c_int, P(_i64), P(_i64), _dp]),
+        "vpm_ffv_direct": (ctypes.c_int, [_vp, ctypes.c_int, _i64, _dp, _i64, _dp, _i64, _dp, _i64,
+                                          _dp, _i64]),
         "vpm_uj_device_async": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,
                                                _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp]),
         "vpm_uj_device_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,

@@ -575,6 +575,7 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->base);
   cudaFree(c->Ut);
   cudaFree(c->part);
+  cudaFree(c->ffv);
   cudaFree(c->status);
   cudaFree(c->red);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -859,6 +860,58 @@ int vpm_diagnostics(vpm_ctx* c, int kernel, int precision, double* out) {
   out[VPM_DIAG_CD_ZERO_RATIO] = nf > 0 ? v[DS_CZERO] / double(nf) : 0.0;
   out[VPM_DIAG_SIGMA_MEAN] = v[DS_SIG] / double(n);
   out[VPM_DIAG_NONFINITE] = v[DS_NONFIN];
+  return VPM_OK;
+}
+
+int vpm_ffv_direct(vpm_ctx* c, int kernel, int64_t nb, const double* Xb, int64_t sxb,
+                   const double* Gb, int64_t sgb, const double* Sb, int64_t ssb, double* M,
+                   int64_t stride_m) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (!valid_kernel(kernel)) return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel");
+  if (nb < 0) return ctx_fail(c, VPM_ERR_INVALID, "negative bound-particle count");
+  if (nb == 0) return VPM_OK;
+  if (!M || stride_m < 6) return ctx_fail(c, VPM_ERR_INVALID, "bad force output");
+  int rc = validate_host(c, nb, Xb, sxb, Gb, sgb, Sb, ssb);
+  if (rc) return rc;
+  if ((rc = check_inject(c))) return rc;
+  DeviceGuard dg(c->device);
+  const int64_t ldb = round_up(nb, 32);
+  if (ldb > c->ffv_cap) {
+    cudaFree(c->ffv);
+    c->ffv = nullptr;
+    c->ffv_cap = 0;
+    if (cudaMalloc(&c->ffv, 13 * size_t(ldb) * sizeof(double)) != cudaSuccess)
+      return ctx_fail(c, VPM_ERR_NOMEM, "cannot allocate bound-particle buffers");
+    c->ffv_cap = ldb;
+  }
+  const int64_t cap = c->ffv_cap;
+  double* xb = c->ffv;
+  double* gb = xb + 3 * cap;
+  double* sb = gb + 3 * cap;
+  double* md = sb + cap;
+  int64_t chunk = 0;
+  int n_chunk = 1;
+  if ((rc = ensure_part(c, ffv_plan(nb, c->n, c->num_sms, &chunk, &n_chunk)))) return rc;
+  if ((rc = ensure_stage(c, size_t(7) * nb))) return rc;
+  double* h = c->h_stage;
+  for (int64_t i = 0; i < nb; ++i) {
+    for (int k = 0; k < 3; ++k) {
+      h[k * nb + i] = Xb[i * sxb + k];
+      h[(3 + k) * nb + i] = Gb[i * sgb + k];
+    }
+    h[6 * nb + i] = Sb[i * ssb];
+  }
+  const size_t w = size_t(nb) * sizeof(double), dp = size_t(cap) * sizeof(double);
+  CTX_CK(c, cudaMemcpy2DAsync(xb, dp, h, w, w, 7, cudaMemcpyHostToDevice, c->st));
+  CTX_CK(c, launch_ffv(kernel, nb, xb, gb, sb, cap, c->n, c->X, c->G, c->ld, c->part, md, cap,
+                       c->num_sms, c->st));
+  c->launches += n_chunk > 1 ? 2 : 1;
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  if ((rc = ensure_stage(c, size_t(6) * nb))) return rc;
+  CTX_CK(c, cudaMemcpy2DAsync(c->h_stage, w, md, dp, w, 6, cudaMemcpyDeviceToHost, c->st));
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  for (int64_t i = 0; i < nb; ++i)
+    for (int k = 0; k < 6; ++k) M[i * stride_m + k] = c->h_stage[k * nb + i];
   return VPM_OK;
 }
 

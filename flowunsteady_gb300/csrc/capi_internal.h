@@ -50,6 +50,13 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
                      double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
                      cudaStream_t st, PairPlan* plan_out);
 
+// Free-vortex force of bound particles (ffv.cu).
+size_t ffv_plan(int64_t nb, int64_t nf, int num_sms, int64_t* chunk, int* n_chunk);
+cudaError_t launch_ffv(int kernel, int64_t nb, const double* xb, const double* gb,
+                       const double* sb, int64_t ldb, int64_t nf, const double* xf,
+                       const double* gf, int64_t ldf, double* part, double* M, int64_t ldm,
+                       int num_sms, cudaStream_t st);
+
 struct GraphKey {
   int64_t n, n_static;
   double dt;
@@ -106,6 +113,8 @@ struct vpm_ctx {
   int64_t fail_after = 0;
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
+  double* ffv = nullptr;          // bound particles (X3 Γ3 σ1) and M (6) rows, ffv_cap apart
+  int64_t ffv_cap = 0;
   int64_t launches = 0;           // kernels enqueued (graph replays add their kernel count)
   int64_t step_launches = 0;      // kernels of one captured step (counted while enqueuing)
 };

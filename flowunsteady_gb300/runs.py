@@ -177,7 +177,8 @@ def run_rings(args):
     def cmp(a, b):
         (Xa, Ga, Sa), (Xb, Gb, Sb) = finals[a], finals[b]
         return {"max_abs_dx": float(np.abs(Xa - Xb).max()), "rel_l2_gamma": rel_l2(Ga, Gb),
-                "max_abs_dsigma": float(np.abs(Sa - Sb).max())}
+                "max_abs_dsigma": float(np.abs(Sa - Sb).max()), "rel_l2_sigma": rel_l2(Sa, Sb),
+                "median_abs_dsigma": float(np.median(np.abs(Sa - Sb)))}
 
     res["fp32c_vs_fp64_final"] = cmp("fp32c", "fp64")
     res["fp32c_analytic_vs_fp64_analytic_final"] = cmp("fp32c_analytic", "fp64_analytic")

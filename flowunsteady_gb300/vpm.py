@@ -338,6 +338,20 @@ class ParticleField:
         return out
 
 
+def Ffv_direct(pfield: ParticleField, Xb, Gb, Sb) -> np.ndarray:
+    """Free-vortex force terms of bound particles (x_b, Γ_b, σ_b) from every particle
+    of the field: columns 0..2 = Σ U_b(x_f) × Γ_f, 3..5 = Σ g_σb K(x_b - x_f) × (Γ_b × Γ_f)
+    (_Ffv_direct, src/FLOWUnsteady_processing_force.jl:879-929)."""
+    pfield._flush()
+    Xb = np.ascontiguousarray(Xb, dtype=np.float64).reshape(-1, 3)
+    Gb = np.ascontiguousarray(Gb, dtype=np.float64).reshape(-1, 3)
+    Sb = np.ascontiguousarray(Sb, dtype=np.float64).reshape(-1)
+    M = np.empty((Xb.shape[0], 6))
+    L.check(L.lib().vpm_ffv_direct(pfield._ctx, pfield.kernel.id, Xb.shape[0], L.dptr(Xb), 3,
+                                   L.dptr(Gb), 3, L.dptr(Sb), 1, L.dptr(M), 6), pfield._ctx)
+    return M
+
+
 def add_particle(pfield: ParticleField, X, Gamma, sigma, *, static: bool = False):
     """Append one particle or an (n,3)/(n,3)/(n,) batch (vpm.add_particle)."""
     X = np.asarray(X, dtype=np.float64).reshape(-1, 3)

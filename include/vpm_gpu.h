@@ -233,6 +233,18 @@ int vpm_step(vpm_ctx* ctx, double dt, const vpm_scheme* s, int64_t nsteps, int u
  * given kernel and precision. */
 int vpm_diagnostics(vpm_ctx* ctx, int kernel, int precision, double* out);
 
+/* Free-vortex force terms of nb bound particles (host arrays) from all particles
+ * of the context (FLOWUnsteady's _Ffv_direct, src/FLOWUnsteady_processing_force.jl:879-929,
+ * used by generate_calc_aerodynamicforce_freevortices, :746-857).  For each
+ * bound particle b, over every particle f of the field with r = |x_f - x_b| > 0
+ * and the bound core size σ_b:
+ *   M[b*stride_m + 0..2] = Σ_f U_b(x_f) × Γ_f,  U_b(x) = -g_σb/(4π r³) (x - x_b) × Γ_b
+ *   M[b*stride_m + 3..5] = Σ_f g_σb/(4π r³) (x_f - x_b) × (Γ_b × Γ_f)
+ * (the reference's P.M[1:3] and P.M[4:6]).  FP64. */
+int vpm_ffv_direct(vpm_ctx* ctx, int kernel, int64_t nb, const double* Xb, int64_t stride_x,
+                   const double* Gb, int64_t stride_g, const double* Sb, int64_t stride_s,
+                   double* M, int64_t stride_m);
+
 /* Σ|Γ|-weighted centroids of index ranges: for r in [0, nranges) particles
  * [starts[r], ends[r]) -> centroid out[3r..3r+2]. */
 int vpm_centroids(vpm_ctx* ctx, int nranges, const int64_t* starts, const int64_t* ends,

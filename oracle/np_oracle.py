@@ -113,3 +113,19 @@ def step_rk3(kernel, X, G, S, dt, f=0.0, g=0.2, transposed=True, uinf=(0, 0, 0),
             qs2 = a * qs2 + dt * 2 * nu
             S = np.sqrt(S**2 + b * qs2)
     return X, G, S
+
+
+def ffv(kernel, Xb, Gb, Sb, Xf, Gf):
+    """Free-vortex force terms (nb, 6), written from the two cross products of
+    _Ffv_direct (src/FLOWUnsteady_processing_force.jl:900-921)."""
+    d = Xf[None, :, :] - Xb[:, None, :]                        # (nb, nf, 3) = x_f - x_b
+    r = np.sqrt(np.einsum("bfk,bfk->bf", d, d))
+    mask = r > 0
+    rs = np.where(mask, r, 1.0)
+    g, _ = g_dg(kernel, rs / Sb[:, None])
+    k = np.where(mask, g / (4 * np.pi * rs**3), 0.0)
+    U = -k[:, :, None] * np.cross(d, np.broadcast_to(Gb[:, None, :], d.shape))
+    M1 = np.einsum("bfk->bk", np.cross(U, np.broadcast_to(Gf[None, :, :], d.shape)))
+    gxg = np.cross(np.broadcast_to(Gb[:, None, :], d.shape), np.broadcast_to(Gf[None, :, :], d.shape))
+    M2 = np.einsum("bf,bfk->bk", k, np.cross(d, gxg))
+    return np.concatenate([M1, M2], axis=1)

@@ -69,6 +69,8 @@ def lib():
         _lib.orc_relax_pedrizzetti.argtypes = [_i64, ctypes.c_double, _dp, _dp]
         _lib.orc_uj_direct_dsigma.argtypes = [ctypes.c_int, _i64, _dp, _i64, _dp, _dp, _dp, _dp,
                                               ctypes.c_int]
+        _lib.orc_ffv_direct.argtypes = [ctypes.c_int, _i64, _dp, _dp, _dp, _i64, _dp, _dp, _dp,
+                                         ctypes.c_int]
         _lib.orc_estr_direct_dsigma.argtypes = [ctypes.c_int, ctypes.c_int, _i64, _dp, _dp, _dp,
                                                 _dp, _dp, _dp, ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
@@ -140,6 +142,16 @@ def estr_dsigma(kernel, X, G, S, J, DJ, transposed=True, nthreads=0):
     lib().orc_estr_direct_dsigma(kernel, int(transposed), X.shape[0], _p(X), _p(G), _p(S), _p(J),
                                  _p(DJ), _p(DE), nthreads)
     return DE
+
+
+def ffv_direct(kernel, Xb, Gb, Sb, Xf, Gf, nthreads=0):
+    """Free-vortex force terms M (nb, 6) of bound particles from free particles."""
+    Xb, Gb, Sb = _c(Xb, (3,)), _c(Gb, (3,)), _c(Sb, ())
+    Xf, Gf = _c(Xf, (3,)), _c(Gf, (3,))
+    M = np.empty((Xb.shape[0], 6))
+    lib().orc_ffv_direct(kernel, Xb.shape[0], _p(Xb), _p(Gb), _p(Sb), Xf.shape[0], _p(Xf), _p(Gf),
+                         _p(M), nthreads)
+    return M
 
 
 def step(scheme_struct, X, G, S, C, dt, n_static=0, nsteps=1, nthreads=0):

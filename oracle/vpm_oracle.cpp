@@ -333,6 +333,48 @@ int orc_estr_direct_dsigma(int kernel, int transposed, int64_t n, const double* 
   return 0;
 }
 
+// Free-vortex force, restated from _Ffv_direct
+// (src/FLOWUnsteady_processing_force.jl:879-929): for every bound particle b,
+// over every free particle f with r = |x_f - x_b| != 0 and the bound core σ_b,
+//   U_b(x_f) = -g_σb(r)/(4π r³) (Δx × Γ_b),           Δx = x_f - x_b
+//   M[0:3]  += U_b(x_f) × Γ_f
+//   M[3:6]  += g_σb(r)/(4π r³) Δx × (Γ_b × Γ_f)
+// (the reference writes 1/(4π) as 0.07957747154594767).  M is (nb, 6).
+int orc_ffv_direct(int kernel, int64_t nb, const double* Xb, const double* Gb, const double* Sb,
+                   int64_t nf, const double* Xf, const double* Gf, double* M, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t b = 0; b < nb; ++b) {
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    const double* xb = Xb + 3 * b;
+    const double* gb = Gb + 3 * b;
+    for (int64_t f = 0; f < nf; ++f) {
+      const double dX1 = Xf[3 * f] - xb[0], dX2 = Xf[3 * f + 1] - xb[1], dX3 = Xf[3 * f + 2] - xb[2];
+      const double r = std::sqrt(dX1 * dX1 + dX2 * dX2 + dX3 * dX3);
+      if (r == 0.0) continue;
+      double g, dg, z;
+      const double rho = r / Sb[b];
+      orc_kernel_eval(kernel, 1, &rho, &g, &dg, &z);
+      const double k = g * kInv4Pi / (r * r * r);
+      const double U1 = -k * (dX2 * gb[2] - dX3 * gb[1]);
+      const double U2 = -k * (dX3 * gb[0] - dX1 * gb[2]);
+      const double U3 = -k * (dX1 * gb[1] - dX2 * gb[0]);
+      const double* gf = Gf + 3 * f;
+      m[0] += U2 * gf[2] - U3 * gf[1];
+      m[1] += U3 * gf[0] - U1 * gf[2];
+      m[2] += U1 * gf[1] - U2 * gf[0];
+      const double c1 = gb[1] * gf[2] - gb[2] * gf[1];
+      const double c2 = gb[2] * gf[0] - gb[0] * gf[2];
+      const double c3 = gb[0] * gf[1] - gb[1] * gf[0];
+      m[3] += k * (dX2 * c3 - dX3 * c2);
+      m[4] += k * (dX3 * c1 - dX1 * c3);
+      m[5] += k * (dX1 * c2 - dX2 * c1);
+    }
+    for (int c = 0; c < 6; ++c) M[6 * b + c] = m[c];
+  }
+  return 0;
+}
+
 // One time step of the full method on n particles, the last n_static of which
 // act as sources only.  X, G, S are advanced in place; C (n,3) holds the SFS
 // memory (C_d, <Γ·L>, <Γ·m>) across steps.  E_out (n,3) receives the last

@@ -138,3 +138,22 @@ def test_python_api_mirrors_flowvpm():
     with pytest.raises(ValueError):
         vpm.remove_particle(pf, 3)
     pf.close()
+
+
+@pytest.mark.parametrize("k", [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF])
+@pytest.mark.parametrize("nb", [1, 57, 3000])
+def test_free_vortex_force_matches_oracle(oracle, k, nb):
+    X, G, S = uniform_box(5000, seed_index=130)
+    rng = np.random.default_rng(nb)
+    Xb = rng.uniform(-1, 1, (nb, 3))
+    Gb = rng.normal(0, 1, (nb, 3))
+    Sb = rng.uniform(0.05, 0.2, nb)
+    Xb[0] = X[10]                      # a bound particle on top of a free one
+    M0 = oracle.ffv_direct(k, Xb, Gb, Sb, X, G)
+    with Ctx(5000) as c:
+        c.set(X, G, S)
+        M = np.empty((nb, 6))
+        c.rc(c.lib.vpm_ffv_direct(c.p, k, nb, L.dptr(np.ascontiguousarray(Xb)), 3,
+                                  L.dptr(np.ascontiguousarray(Gb)), 3,
+                                  L.dptr(np.ascontiguousarray(Sb)), 1, L.dptr(M), 6))
+    assert rel_l2(M, M0) <= 1e-12 and rel_max(M, M0) <= 1e-11

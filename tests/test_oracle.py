@@ -182,3 +182,14 @@ def test_analytic_and_finite_difference_dynamic_cd_agree(oracle):
     m = (Cf[:, 0] != 0) & (Ca[:, 0] != 0)
     assert m.sum() > 20
     assert np.median(np.abs(Ca[m, 0] - Cf[m, 0]) / np.abs(Cf[m, 0])) < 1e-2
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_free_vortex_force_matches_numpy(oracle, k):
+    rng = np.random.default_rng(60 + k)
+    Xb, Gb, Sb = rng.uniform(-1, 1, (40, 3)), rng.normal(0, 1, (40, 3)), rng.uniform(0.1, 0.3, 40)
+    Xf, Gf = rng.uniform(-1, 1, (300, 3)), rng.normal(0, 1e-2, (300, 3))
+    Xf[7] = Xb[3]   # coincident pair: skipped
+    M = oracle.ffv_direct(k, Xb, Gb, Sb, Xf, Gf)
+    M2 = P.ffv(k, Xb, Gb, Sb, Xf, Gf)
+    assert rel_max(M, M2) < 1e-12
