@@ -123,6 +123,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_config(args):
+    """The workload description shared by both arms (precision is per arm)."""
+    return {"workload": f"helical wake N={args.n}, one U+∇U evaluation at every particle, "
+                        f"{args.kernel} kernel",
+            "n_particles": args.n, "pairs_per_step": args.n * args.n}
+
+
+def aggregate(total_s, steps, pairs_per_step, world, dist, device=None):
+    """Whole-job pairs/s: every rank runs its own replica; the job takes the
+    slowest rank's time (max over ranks)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(total_s)], dtype=torch.float64,
+                         device=device if device is not None else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    return world * steps * pairs_per_step / total_s, total_s
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -204,9 +223,8 @@ def run_reference(args, world, rank):
         "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded helical wake, 262,144 particles)",
-        "config": {"workload": f"helical wake N={args.n}, one U+∇U evaluation, {args.kernel}",
-                   "n_particles": args.n, "pairs_per_step": args.n * args.n},
+        "data": f"synthetic (seeded helical wake, {args.n} particles)",
+        "config": {**workload_config(args), "precision": "fp64 (CPU)"},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
@@ -281,13 +299,8 @@ def run_ours(args, world, rank, local, dist):
         dist.barrier()
     lib.vpm_get_launch_count(ctx, ctypes.byref(l1))
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = sum(step_ms) / 1e3
-    if dist:
-        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
     pairs = float(n) * float(n)
-    value = world * args.steps * pairs / total_s
+    value, total_s = aggregate(sum(step_ms) / 1e3, args.steps, pairs, world, dist, dev)
     ms_per_step = 1e3 * total_s / args.steps
     launches = int(l1.value - l0.value)
     # The other kernel, timed the same way (reported beside the headline).
@@ -395,9 +408,7 @@ def run_ours(args, world, rank, local, dist):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated; FP64 state)",
             "data": "synthetic (seeded helical wake)",
-            "config": {"workload": f"helical wake N={n}, one FP32-compensated U+∇U evaluation, "
-                                   f"{args.kernel} kernel", "n_particles": n,
-                       "pairs_per_step": n * n, "precision": "fp32c",
+            "config": {**workload_config(args), "precision": args.precision,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": BYTES_H2D * n,
