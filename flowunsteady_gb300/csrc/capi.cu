@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -137,6 +138,20 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.items = nullptr; a.n_items = 0; a.counter = nullptr;
   a.u = pc.u; a.j = pc.j; a.ldo = pc.ldo;
   a.part = part; a.ldp = ldp;
+  a.status = pc.status;
+  {
+    // Bulk copies need 16-byte aligned row starts: even ld and tile starts (the
+    // chunk length is a multiple of the block) and 16-byte aligned bases.
+    static const bool disabled = [] {
+      const char* v = std::getenv("VPM_NO_TMA");
+      return v && v[0] && v[0] != '0';
+    }();
+    const bool aligned = (pc.lds % 2 == 0) && (chunk % sh.block == 0) &&
+                         (reinterpret_cast<uintptr_t>(pc.xs) % 16 == 0) &&
+                         (reinterpret_cast<uintptr_t>(pc.gs) % 16 == 0) &&
+                         (reinterpret_cast<uintptr_t>(pc.ss) % 16 == 0);
+    a.tma = (pc.tma_ok && aligned && !disabled) ? 1 : 0;
+  }
   cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
   if (n_chunk > 1) {
@@ -350,6 +365,8 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   pc.sigma_scale = scale;
   pc.u = u; pc.j = j; pc.ldo = c->ld;
   pc.ws = ws; pc.dj = dj;
+  pc.tma_ok = true;        // context rows: ld % 32 == 0, one allocation
+  pc.status = c->status;
   const Shape* pinned = &c->pinned[pass & 1][kernel][prec];  // D passes share their plain pass's pin
   PairPlan plan;
   plan.n_chunk = 1;
@@ -465,6 +482,8 @@ static int check_status(vpm_ctx* c) {
     CTX_CK(c, cudaStreamSynchronize(c->st));
     if (st & STATUS_NONFINITE)
       return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite particle state after the update");
+    if (st & STATUS_TIMEOUT)
+      return ctx_fail(c, VPM_ERR_CUDA, "a source-tile copy did not complete in time");
     return ctx_fail(c, VPM_ERR_CUDA, "device status word set");
   }
   return VPM_OK;
@@ -699,10 +718,9 @@ int vpm_eval_UJ_targets(vpm_ctx* c, int kernel, int precision, int64_t t0, int64
   rc = ensure_part(c, c->part_need);
   if (rc) return rc;
   CTX_CK(c, ctx_pair(c, PASS_UJ, kernel, precision, t0, t1, 1.0, nullptr, c->U, c->J));
-  CTX_CK(c, cudaStreamSynchronize(c->st));
   c->uj_lo = t0;
   c->uj_hi = t1;
-  return VPM_OK;
+  return check_status(c);
 }
 
 int vpm_eval_UJ(vpm_ctx* c, int kernel, int precision) {

@@ -31,6 +31,11 @@ struct PairCall {
   double* dj = nullptr;         // PASS_UJD: DJ rows
   int64_t ldo;
   int max_chunks = 0;   // upper bound on source chunks (0 = planner's choice)
+  // The source rows may be staged with bulk copies: the caller guarantees that
+  // reading one element past an odd-length tile stays inside each row's
+  // allocation (context arrays: ld is a multiple of 32 and rows are contiguous).
+  bool tma_ok = false;
+  int* status = nullptr;
 };
 
 struct PairPlan {

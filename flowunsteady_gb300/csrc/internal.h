@@ -62,6 +62,11 @@ struct PairArgs {
   int64_t ldo;
   double* part;
   int64_t ldp;
+  // Stage source tiles with bulk asynchronous copies (set by the host only when
+  // every row start is 16-byte aligned and the even-padded tiles stay inside
+  // the rows' allocation).
+  int32_t tma;
+  int* status;   // STATUS_TIMEOUT is OR-ed here if a copy wait gives up (may be null)
 };
 
 // Tile shape of a launch.

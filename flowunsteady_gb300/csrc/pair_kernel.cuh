@@ -32,6 +32,7 @@
 #include <type_traits>
 
 #include "internal.h"
+#include "update.h"
 #include "vpm_device.cuh"
 
 namespace vpm {
@@ -50,6 +51,9 @@ struct PairTraits {
   static constexpr bool kD = PASS == PASS_UJD || PASS == PASS_ZETAD;
   // shared quads per source: (x, a), (Γ, b), and for ζ passes v_q (and w_q)
   static constexpr int kQuads = kUJ ? 2 : (PASS == PASS_ZETA ? 3 : 4);
+  // The FP32 U/J pass can stage its FP64 source rows with bulk copies.
+  static constexpr bool kTma = PASS == PASS_UJ && PREC != VPM_PREC_FP64;
+  static constexpr int kTmaRows = 7;   // x, y, z, Γx, Γy, Γz, σ
 };
 
 template <int PASS, int PREC>
@@ -57,7 +61,8 @@ __host__ __device__ constexpr size_t smem_bytes(int block, int tpt) {
   using Tr = PairTraits<PASS, PREC>;
   size_t src = size_t(block) * Tr::kQuads * sizeof(Quad<typename Tr::R>);
   size_t fold = Tr::kComp ? size_t(block) * tpt * Tr::kNval * 2 * sizeof(float) : 0;
-  return src + fold;
+  size_t stage = Tr::kTma ? size_t(block) * Tr::kTmaRows * sizeof(double) + 16 : 0;
+  return src + fold + stage;
 }
 
 // Minimum resident CTAs requested from the compiler: caps the FP32 U/J kernels
@@ -124,11 +129,38 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   Quad<R>* tileD = tileC + BLOCK;  // PASS_ZETAD: w_q
   float* fold_hi = reinterpret_cast<float*>(smem_raw + size_t(BLOCK) * Tr::kQuads * sizeof(Quad<R>));
   float* fold_lo = fold_hi + size_t(BLOCK) * T * NV;
+  // TMA staging: kTmaRows FP64 rows of BLOCK sources, then the mbarrier.
+  double* stage = reinterpret_cast<double*>(
+      smem_raw + size_t(BLOCK) * Tr::kQuads * sizeof(Quad<R>) +
+      (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage + size_t(BLOCK) * Tr::kTmaRows);
   __shared__ int s_item;
 
   const int tid = threadIdx.x;
   const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
   const bool same_arrays = a.xt == a.xs && a.ldt == a.lds;
+  const bool use_tma = Tr::kTma && a.tma != 0;
+  uint32_t phase = 0;
+  if (use_tma) {
+    if (tid == 0) mbar_init(bar, 1);
+    __syncthreads();
+  }
+  // Copies of the source tile [tile, tile + cnt) into the staging rows: each
+  // row is padded to an even count (16-byte multiple); the host guarantees the
+  // padded element lies inside the row's allocation.
+  auto issue = [&](int64_t tile, int64_t send) {
+    const int cnt = int(min(int64_t(BLOCK), send - tile));
+    const uint32_t bytes = uint32_t((cnt + 1) & ~1) * uint32_t(sizeof(double));
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, bytes * Tr::kTmaRows);
+    bulk_g2s(stage + 0 * BLOCK, a.xs + tile, bytes, bar);
+    bulk_g2s(stage + 1 * BLOCK, a.xs + a.lds + tile, bytes, bar);
+    bulk_g2s(stage + 2 * BLOCK, a.xs + 2 * a.lds + tile, bytes, bar);
+    bulk_g2s(stage + 3 * BLOCK, a.gs + tile, bytes, bar);
+    bulk_g2s(stage + 4 * BLOCK, a.gs + a.lds + tile, bytes, bar);
+    bulk_g2s(stage + 5 * BLOCK, a.gs + 2 * a.lds + tile, bytes, bar);
+    bulk_g2s(stage + 6 * BLOCK, a.ss + tile, bytes, bar);
+  };
 
   int item;
   if (a.counter) {
@@ -190,10 +222,44 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     }
 
     int tiles = 0;
+    if (use_tma && tid == 0 && s0 < s1) issue(s0, s1);
     for (int64_t tile0 = s0; tile0 < s1; tile0 += BLOCK) {
       // ---- stage one tile of sources -------------------------------------
       __syncthreads();  // previous tile fully consumed
-      {
+      if constexpr (Tr::kTma) {
+        if (use_tma) {
+          const bool ok = mbar_wait(bar, phase);
+          phase ^= 1u;
+          if (__syncthreads_or(!ok)) {
+            // A copy did not complete in time: record it, give the copies in
+            // flight a second bounded wait, and leave together.
+            if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+            mbar_wait(bar, phase ^ 1u);
+            return;
+          }
+          const int64_t jj = tile0 + tid;
+          Quad<R> qa, qb;
+          if (jj < s1) {
+            const double sig = stage[6 * BLOCK + tid] * a.sigma_scale;
+            qa.x = R(stage[0 * BLOCK + tid] - cx);
+            qa.y = R(stage[1 * BLOCK + tid] - cy);
+            qa.z = R(stage[2 * BLOCK + tid] - cz);
+            qb.x = R(stage[3 * BLOCK + tid]);
+            qb.y = R(stage[4 * BLOCK + tid]);
+            qb.z = R(stage[5 * BLOCK + tid]);
+            source_consts<KERNEL, R>(sig, qa.w, qb.w);
+          } else {
+            qa.x = qa.y = qa.z = R(0);
+            qb.x = qb.y = qb.z = R(0);
+            source_consts<KERNEL, R>(1.0, qa.w, qb.w);
+          }
+          tileA[tid] = qa;
+          tileB[tid] = qb;
+          __syncthreads();  // quads ready, staging rows consumed
+          if (tid == 0 && tile0 + BLOCK < s1) issue(tile0 + BLOCK, s1);
+        }
+      }
+      if (!use_tma) {
         const int64_t jj = tile0 + tid;
         Quad<R> qa, qb, qc, qd;
         qc.x = qc.y = qc.z = qc.w = R(0);
@@ -225,8 +291,8 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         tileB[tid] = qb;
         if (!Tr::kUJ) tileC[tid] = qc;
         if (PASS == PASS_ZETAD) tileD[tid] = qd;
+        __syncthreads();
       }
-      __syncthreads();
 
       // ---- all pairs of the tile ------------------------------------------
       const int cnt = int(min(int64_t(BLOCK), s1 - tile0));

@@ -159,3 +159,45 @@ def test_estr_and_enstrophy_match_oracle(oracle, k):
         assert rel_l2(E, E0) <= 1e-5
         d = c.diag(k, L.PREC_FP32C)
         assert abs(d[0] - d0[0]) <= 1e-6 * abs(d0[0])
+
+
+_PLAIN_STAGING_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from tests.helpers import Ctx
+from flowunsteady_gb300.workloads import helical_wake
+X, G, S = helical_wake(int(sys.argv[2]))
+out = {}
+with Ctx(X.shape[0]) as c:
+    c.set(X, G, S)
+    for k in (0, 1):
+        for p in (1, 2):
+            out[f"U{k}{p}"], out[f"J{k}{p}"] = c.uj(k, p)
+    out["Us"], out["Js"] = c.uj(1, 2, 1000, 1777)
+np.savez(sys.argv[3], **out)
+"""
+
+
+@pytest.mark.parametrize("n", [20001, 4096])
+def test_bulk_copy_staging_matches_plain_loads_bitwise(tmp_path, n):
+    # The U/J FP32 passes stage source tiles with cp.async.bulk; VPM_NO_TMA=1
+    # forces plain loads.  Same conversion and summation order: identical bits.
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = tmp_path / "plain.npz"
+    script = tmp_path / "plain.py"
+    script.write_text(_PLAIN_STAGING_SCRIPT)
+    env = dict(os.environ, VPM_NO_TMA="1")
+    subprocess.run([sys.executable, str(script), root, str(n), str(out)], check=True, env=env,
+                   timeout=300)
+    ref = np.load(out)
+    X, G, S = helical_wake(n)
+    with Ctx(n) as c:
+        c.set(X, G, S)
+        for k in (0, 1):
+            for p in (1, 2):
+                U, J = c.uj(k, p)
+                assert np.array_equal(U, ref[f"U{k}{p}"]) and np.array_equal(J, ref[f"J{k}{p}"])
+        Us, Js = c.uj(1, 2, 1000, 1777)
+        assert np.array_equal(Us, ref["Us"]) and np.array_equal(Js, ref["Js"])
