@@ -166,10 +166,15 @@ import sys, numpy as np
 sys.path.insert(0, sys.argv[1])
 from tests.helpers import Ctx
 from flowunsteady_gb300.workloads import helical_wake
+import ctypes
+from flowunsteady_gb300 import _lib as L
 X, G, S = helical_wake(int(sys.argv[2]))
 out = {}
 with Ctx(X.shape[0]) as c:
     c.set(X, G, S)
+    for k in (0, 1):
+        for p in (1, 2):
+            c.rc(c.lib.vpm_set_tile(c.p, k, p, ctypes.byref(L.Tile(128, 2, 0, 0))))
     for k in (0, 1):
         for p in (1, 2):
             out[f"U{k}{p}"], out[f"J{k}{p}"] = c.uj(k, p)
@@ -195,6 +200,9 @@ def test_bulk_copy_staging_matches_plain_loads_bitwise(tmp_path, n):
     X, G, S = helical_wake(n)
     with Ctx(n) as c:
         c.set(X, G, S)
+        for k in (0, 1):       # same tile shape in both processes
+            for p in (1, 2):
+                c.rc(c.lib.vpm_set_tile(c.p, k, p, ctypes.byref(L.Tile(128, 2, 0, 0))))
         for k in (0, 1):
             for p in (1, 2):
                 U, J = c.uj(k, p)
