@@ -152,12 +152,9 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
                          (reinterpret_cast<uintptr_t>(pc.ss) % 16 == 0);
     a.tma = (pc.tma_ok && aligned && !disabled) ? 1 : 0;
   }
-  const bool fused = n_chunk > 1 && pc.tile_done && n_tb <= pc.tile_done_cap;
-  a.tile_done = fused ? pc.tile_done : nullptr;
-  if (plan_out) plan_out->fused = fused;
   cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
-  if (n_chunk > 1 && !fused) {
+  if (n_chunk > 1) {
     e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
@@ -370,15 +367,12 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   pc.ws = ws; pc.dj = dj;
   pc.tma_ok = true;        // context rows: ld % 32 == 0, one allocation
   pc.status = c->status;
-  pc.tile_done = c->tile_done;
-  pc.tile_done_cap = c->tile_done_cap;
   const Shape* pinned = &c->pinned[pass & 1][kernel][prec];  // D passes share their plain pass's pin
   PairPlan plan;
   plan.n_chunk = 1;
-  plan.fused = false;
   cudaError_t e = run_pair(pc, c->device, c->num_sms, pinned, c->part, c->ld, c->part_elems,
                            &c->part_need, c->dry, c->st, &plan);
-  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += (plan.n_chunk > 1 && !plan.fused) ? 2 : 1;
+  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += plan.n_chunk > 1 ? 2 : 1;
   return e;
 }
 
@@ -488,12 +482,8 @@ static int check_status(vpm_ctx* c) {
     CTX_CK(c, cudaStreamSynchronize(c->st));
     if (st & STATUS_NONFINITE)
       return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite particle state after the update");
-    if (st & STATUS_TIMEOUT) {
-      // A CTA that left early may not have counted its tile: clear the counters.
-      CTX_CK(c, cudaMemsetAsync(c->tile_done, 0, size_t(c->tile_done_cap) * sizeof(unsigned), c->st));
-      CTX_CK(c, cudaStreamSynchronize(c->st));
+    if (st & STATUS_TIMEOUT)
       return ctx_fail(c, VPM_ERR_CUDA, "a source-tile copy did not complete in time");
-    }
     return ctx_fail(c, VPM_ERR_CUDA, "device status word set");
   }
   return VPM_OK;
@@ -585,11 +575,6 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   if (e == cudaSuccess) e = cudaMalloc(&c->status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(c->status, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->red, (size_t(kRedBlocks) + 1) * kDiagSlots * sizeof(double));
-  if (e == cudaSuccess) {
-    c->tile_done_cap = c->ld / 128 + 1;
-    e = cudaMalloc(&c->tile_done, size_t(c->tile_done_cap) * sizeof(unsigned int));
-  }
-  if (e == cudaSuccess) e = cudaMemset(c->tile_done, 0, size_t(c->tile_done_cap) * sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     vpm_ctx_destroy(c);
@@ -610,7 +595,6 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->Ut);
   cudaFree(c->part);
   cudaFree(c->ffv);
-  cudaFree(c->tile_done);
   cudaFree(c->status);
   cudaFree(c->red);
   if (c->h_stage) cudaFreeHost(c->h_stage);

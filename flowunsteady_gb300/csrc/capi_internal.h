@@ -36,10 +36,6 @@ struct PairCall {
   // allocation (context arrays: ld is a multiple of 32 and rows are contiguous).
   bool tma_ok = false;
   int* status = nullptr;
-  // Per-target-tile counters for the in-kernel fixed-order reduction (null:
-  // a separate reduction launch); tile_done_cap counters are available.
-  unsigned int* tile_done = nullptr;
-  int64_t tile_done_cap = 0;
 };
 
 struct PairPlan {
@@ -47,7 +43,6 @@ struct PairPlan {
   int64_t n_tb;
   int n_chunk;
   int64_t chunk;
-  bool fused;   // partial slots summed inside the pair kernel
 };
 
 Shape default_shape(int pass, int precision);
@@ -123,8 +118,6 @@ struct vpm_ctx {
   int64_t fail_after = 0;
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
-  unsigned int* tile_done = nullptr;   // one counter per 128-target tile, zero between launches
-  int64_t tile_done_cap = 0;
   double* ffv = nullptr;          // bound particles (X3 Γ3 σ1) and M (6) rows, ffv_cap apart
   int64_t ffv_cap = 0;
   int64_t launches = 0;           // kernels enqueued (graph replays add their kernel count)

@@ -67,11 +67,6 @@ struct PairArgs {
   // the rows' allocation).
   int32_t tma;
   int* status;   // STATUS_TIMEOUT is OR-ed here if a copy wait gives up (may be null)
-  // Single-field form with n_chunk > 1: per-target-tile completion counters
-  // (n_tb of them, zero between launches).  The CTA that completes a tile last
-  // sums its partial slots in slot order and writes the final values; null
-  // leaves the partials to launch_reduce.
-  unsigned int* tile_done;
 };
 
 // Tile shape of a launch.

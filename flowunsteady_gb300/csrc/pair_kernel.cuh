@@ -135,7 +135,6 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
   uint64_t* bar = reinterpret_cast<uint64_t*>(stage + size_t(BLOCK) * Tr::kTmaRows);
   __shared__ int s_item;
-  __shared__ int s_last;
 
   const int tid = threadIdx.x;
   const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
@@ -174,13 +173,12 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 
   while (item < n_items) {
     int64_t t0, t1, s0, s1;
-    int slot, tb = 0;
+    int slot;
     if (a.items) {
       const PairItem it = a.items[item];
       t0 = it.t0; t1 = it.t1; s0 = it.s0; s1 = it.s1; slot = it.slot;
     } else {
-      tb = item % a.n_tb;
-      const int c = item / a.n_tb;
+      const int tb = item % a.n_tb, c = item / a.n_tb;
       t0 = a.t_off + int64_t(tb) * TB;
       t1 = min(t0 + TB, a.t_off + a.nt);
       s0 = int64_t(c) * a.chunk;
@@ -427,30 +425,6 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         for (int w = 0; w < NV; ++w) a.part[(int64_t(slot) * NV + w) * a.ldp + i] = v[w];
       } else {
         write_final<PASS, KERNEL>(v, a, i);
-      }
-    }
-
-    // ---- last CTA of a target tile sums its partial slots --------------------
-    if (slot >= 0 && a.tile_done && !a.items) {
-      __threadfence();   // this CTA's partials are visible device-wide
-      __syncthreads();
-      if (tid == 0) s_last = atomicAdd(a.tile_done + tb, 1u) == unsigned(a.n_chunk - 1);
-      __syncthreads();
-      if (s_last) {
-        __threadfence();
-#pragma unroll
-        for (int k = 0; k < T; ++k) {
-          const int64_t i = t0 + k * BLOCK + tid;
-          if (i >= t1) continue;
-          double v[NV];
-#pragma unroll
-          for (int w = 0; w < NV; ++w) v[w] = 0.0;
-          for (int cc = 0; cc < a.n_chunk; ++cc)
-#pragma unroll
-            for (int w = 0; w < NV; ++w) v[w] += __ldcg(a.part + (int64_t(cc) * NV + w) * a.ldp + i);
-          write_final<PASS, KERNEL>(v, a, i);
-        }
-        if (tid == 0) a.tile_done[tb] = 0u;   // ready for the next launch
       }
     }
 
