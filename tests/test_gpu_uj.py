@@ -209,3 +209,27 @@ def test_bulk_copy_staging_matches_plain_loads_bitwise(tmp_path, n):
                 assert np.array_equal(U, ref[f"U{k}{p}"]) and np.array_equal(J, ref[f"J{k}{p}"])
         Us, Js = c.uj(1, 2, 1000, 1777)
         assert np.array_equal(Us, ref["Us"]) and np.array_equal(Js, ref["Js"])
+
+
+@pytest.mark.parametrize("n", [3001, 40000])
+def test_context_and_device_pointer_paths_agree_bitwise(n):
+    # The context path (TMA staging) and the device-pointer entry point (plain
+    # loads) plan the same launch and sum the source-chunk partials in the same
+    # slot order: identical bits.
+    torch = pytest.importorskip("torch")
+    X, G, S = uniform_box(n, seed_index=70 + n % 7)
+    with Ctx(n) as c:
+        c.set(X, G, S)
+        U0, J0 = c.uj(1, L.PREC_FP32C)
+        U1, J1 = c.uj(0, L.PREC_FP64)
+    dev = torch.device("cuda:0")
+    Xd, Gd, Sd = (torch.tensor(a, device=dev) for a in (X.T.copy(), G.T.copy(), S))
+    for k, p, U_ref, J_ref in ((1, L.PREC_FP32C, U0, J0), (0, L.PREC_FP64, U1, J1)):
+        Ud = torch.zeros((3, n), dtype=torch.float64, device=dev)
+        Jd = torch.zeros((9, n), dtype=torch.float64, device=dev)
+        rc = L.lib().vpm_uj_device_async(k, p, n, Xd.data_ptr(), Gd.data_ptr(), Sd.data_ptr(), n,
+                                         n, None, n, Ud.data_ptr(), Jd.data_ptr(), n, None)
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(Ud.cpu().numpy().T, U_ref)
+        assert np.array_equal(Jd.cpu().numpy().T.reshape(n, 3, 3), J_ref)
