@@ -4,6 +4,7 @@
     python -m flowunsteady_gb300.runs rings     # two leapfrogging rings, full rVPM, 400 RK3 steps
     python -m flowunsteady_gb300.runs batch     # 48 fields, log-uniform N in [2,048, 131,072], 50 steps
     python -m flowunsteady_gb300.runs large     # N = 1,048,576 helical wake (12 turns), 20 RK3 steps
+    python -m flowunsteady_gb300.runs step      # k full steps of an N-particle wake (profiling)
 
 They use the public API only (the C ABI through `_lib`, and `FieldBatch`).  Their
 FP64 reference is the GPU FP64 direct sum, which the tests tie to the CPU oracle.
@@ -305,9 +306,27 @@ def run_large(args):
             "max_rel_l2_J": max(c["rel_l2_J"] for c in checks), "final_diagnostics": d}
 
 
+# ------------------------------------------------------------------------ step --
+def run_step(args):
+    """k full RK3 steps (Gaussian-erf, dynamic SFS with analytic ∂/∂σ, ν = 1e-4,
+    FP32C pair passes) of an N-particle helical wake; a plain driver for
+    profiling the O(N) kernels at sizes above L2."""
+    n = args.n or 1048576
+    nsteps = args.steps or 1
+    X, G, S = helical_wake(n, turns=12 if n > 500000 else 4)
+    f = Field(X, G, S)
+    sc = scheme_for(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    _, t = timed(lambda: f.step(sc, args.dt or 1e-4, nsteps))
+    d = f.diag(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    f.close()
+    return {"workload": f"helical wake N={n}", "steps": nsteps, "seconds": t,
+            "seconds_per_step": t / nsteps, "sigma_mean": d["sigma_mean"],
+            "nonfinite": d["nonfinite"]}
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("run", choices=["sweep", "rings", "batch", "large"])
+    p.add_argument("run", choices=["sweep", "rings", "batch", "large", "step"])
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--steps", type=int, default=None)
     p.add_argument("--fields", type=int, default=None)
@@ -316,7 +335,8 @@ def main(argv=None):
     p.add_argument("--no-reference", action="store_true", help="batch: skip the FP64 fields")
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
-    fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large}[args.run]
+    fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,
+          "step": run_step}[args.run]
     res = fn(args)
     txt = json.dumps(res)
     if args.out:
