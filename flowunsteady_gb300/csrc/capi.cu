@@ -426,7 +426,7 @@ static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
     }
     SfsParams sp;
     sp.alpha = al; sp.rlxf = s->sfs_rlxf; sp.minC = s->sfs_minC; sp.maxC = s->sfs_maxC;
-    sp.zeta0 = zeta0_of(K); sp.transposed = s->transposed;
+    sp.zeta0 = zeta0_of(K); sp.inv_zeta0 = 1.0 / sp.zeta0; sp.transposed = s->transposed;
     sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
     sp.analytic = analytic ? 1 : 0;
     ENQ(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
@@ -448,6 +448,7 @@ static cudaError_t enqueue_stage(vpm_ctx* c, const vpm_scheme* s, double dt, dou
   up.zs = (s->f + s->g) / (1.0 + 3.0 * s->f);
   up.ze = s->f / (1.0 + 3.0 * s->f);
   up.zeta0 = zeta0_of(K);
+  up.inv_zeta0 = 1.0 / up.zeta0;
   up.nu = s->nu;
   up.transposed = s->transposed;
   up.sfs = sfs ? 1 : 0;

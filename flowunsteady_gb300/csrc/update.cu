@@ -118,7 +118,7 @@ __global__ void sfs_dynamic_kernel(int64_t nf, int64_t ld, const double* __restr
   }
   const double sg = S[i];
   nume *= 3.0 * p.alpha - 2.0;
-  deno *= sg * sg * sg / p.zeta0;
+  deno *= sg * sg * sg * p.inv_zeta0;
   nume = p.rlxf * nume + (1.0 - p.rlxf) * C[ld + i];
   deno = p.rlxf * deno + (1.0 - p.rlxf) * C[2 * ld + i];
   double cd = deno != 0.0 ? nume / deno : 0.0;
@@ -159,7 +159,7 @@ __global__ void rk_update_kernel(int64_t nf, int64_t ld, double* X, double* G, d
       cd = 0.0;
       C[i] = 0.0;
     }
-    cz = cd * sg * sg * sg / p.zeta0;   // C_d/ζ_σ(0)
+    cz = cd * sg * sg * sg * p.inv_zeta0;   // C_d/ζ_σ(0)
     Z -= p.ze * cz * ge;
   }
   Z = gg > 0.0 ? Z / gg : 0.0;

@@ -11,6 +11,7 @@ enum : int { STATUS_NONFINITE = 1, STATUS_TIMEOUT = 2 };
 
 struct SfsParams {
   double alpha, rlxf, minC, maxC, zeta0;
+  double inv_zeta0;   // 1/ζ(0) (FP64 divides are scarce on the FP64 pipe)
   int transposed;
   int force_positive;
   int analytic;   // Jt, Et hold DJ, DE (analytic α-derivatives)
@@ -22,6 +23,7 @@ struct UpdateParams {
   double zs;                // (f+g)/(1+3f)
   double ze;                // f/(1+3f)
   double zeta0;             // ζ(0) of the kernel
+  double inv_zeta0;         // 1/ζ(0)
   double nu;                // core spreading viscosity (0 = off)
   int transposed;
   int sfs;                  // E_str / C_d terms on
