@@ -272,7 +272,8 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           if (Tr::kUJ) {
             source_consts<KERNEL, R>(sig, qa.w, qb.w);
           } else {
-            zeta_consts<KERNEL, R>(sig, qa.w, qb.w);
+            if constexpr (F32) zeta_consts_f32<KERNEL>(sig, qa.w, qb.w, qc.w);
+            else zeta_consts<KERNEL, R>(sig, qa.w, qb.w);
             if (a.vs) {
               qc.x = R(a.vs[jj]); qc.y = R(a.vs[a.lds + jj]); qc.z = R(a.vs[2 * a.lds + jj]);
             }
@@ -285,6 +286,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           qa.x = qa.y = qa.z = R(0);
           qb.x = qb.y = qb.z = R(0);
           if (Tr::kUJ) source_consts<KERNEL, R>(1.0, qa.w, qb.w);
+          else if constexpr (F32) zeta_consts_f32<KERNEL>(1.0, qa.w, qb.w, qc.w);
           else zeta_consts<KERNEL, R>(1.0, qa.w, qb.w);
         }
         tileA[tid] = qa;
@@ -354,8 +356,24 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
             }
           }
         }
+      } else if constexpr (F32) {
+        // ζ passes, FP32.
+        const float4* ta = reinterpret_cast<const float4*>(tileA);
+        const float4* tb = reinterpret_cast<const float4*>(tileB);
+        const float4* tc = reinterpret_cast<const float4*>(tileC);
+        const float4* td = reinterpret_cast<const float4*>(PASS == PASS_ZETAD ? tileD : tileC);
+        constexpr bool DD = PASS == PASS_ZETAD;
+        if (!own) {
+#pragma unroll 2
+          for (int js = 0; js < cnt; ++js)
+            zeta_source<KERNEL, T, false, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+        } else {
+#pragma unroll 2
+          for (int js = 0; js < cnt; ++js)
+            zeta_source<KERNEL, T, true, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+        }
       } else {
-        // ζ passes.
+        // ζ passes, FP64.
 #pragma unroll 2
         for (int js = 0; js < cnt; ++js) {
           const Quad<R> sa = tileA[js];

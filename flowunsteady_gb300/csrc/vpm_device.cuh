@@ -585,3 +585,73 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 }  // namespace vpm
+
+// ------------------------------------------------------------------------------
+// FP32 ζ pass: one staged source against the T targets of a thread.
+//   Source quads: (x, y, z, a), (Γ, b), (v, c) [and (w, -) for the D form], with
+//   Gaussian-erf: a = -log2(e)/(2σ²), b = (2π)^{-3/2}/σ³                 → ζ_σ = b·2^{r² a}
+//   Winckelmans:  c' = (15/(8π)/σ³)^{-2/7}, a = c'/σ², b = c', c = -7c'  → with
+//                 s' = r² a + b = c'(ρ²+1),  ζ_σ = s'^{-7/2}  (the prefactor is in c'),
+//                 and 1/(ρ²+1) = c'/s' for the D form.
+//   Dζ_σ = ζ_σ (ρ² - 3) (Gaussian) or ζ_σ (4 - 7/(ρ²+1)) (Winckelmans).
+// Accumulators: Ω 0..2, V 3..5 (and DΩ 6..8, DV 9..11).  MASK drops coincident
+// pairs (only tiles that can hold a target's own particle need it).
+namespace vpm {
+
+template <int KERNEL>
+__device__ inline void zeta_consts_f32(double sig, float& a, float& b, float& c) {
+  const double s3 = sig * sig * sig;
+  if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+    const double cp = pow(kZeta0Winck / s3, -2.0 / 7.0);
+    a = float(cp / (sig * sig));
+    b = float(cp);
+    c = float(-7.0 * cp);
+  } else {
+    a = float(-0.5 * kLog2e / (sig * sig));
+    b = float(kZeta0Gauss / s3);
+    c = 0.f;
+  }
+}
+
+template <int KERNEL, int T, bool MASK, bool D>
+__device__ __forceinline__ void zeta_source(const float4 sa, const float4 sb, const float4 sc,
+                                            const float4 sd, const float (&tx)[T],
+                                            const float (&ty)[T], const float (&tz)[T],
+                                            float (&acc)[T][D ? 12 : 6]) {
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float z, dzz = 0.f;
+    if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+      const float rs = rsqrt_ftz(fmaf(r2, sa.w, sb.w));
+      const float rs2 = rs * rs;
+      z = (rs2 * rs2) * (rs2 * rs);
+      if (D) dzz = z * fmaf(sc.w, rs2, 4.f);
+    } else {
+      const float x = r2 * sa.w;
+      z = sb.w * ex2_ftz(x);
+      if (D) dzz = z * fmaf(x, kArgToRho2, -3.f);
+    }
+    if (MASK) {
+      z = r2 > 0.f ? z : 0.f;
+      if (D) dzz = r2 > 0.f ? dzz : 0.f;
+    }
+    acc[k][0] = fmaf(z, sb.x, acc[k][0]);
+    acc[k][1] = fmaf(z, sb.y, acc[k][1]);
+    acc[k][2] = fmaf(z, sb.z, acc[k][2]);
+    acc[k][3] = fmaf(z, sc.x, acc[k][3]);
+    acc[k][4] = fmaf(z, sc.y, acc[k][4]);
+    acc[k][5] = fmaf(z, sc.z, acc[k][5]);
+    if (D) {
+      acc[k][6] = fmaf(dzz, sb.x, acc[k][6]);
+      acc[k][7] = fmaf(dzz, sb.y, acc[k][7]);
+      acc[k][8] = fmaf(dzz, sb.z, acc[k][8]);
+      acc[k][9] = fmaf(dzz, sc.x, fmaf(z, sd.x, acc[k][9]));
+      acc[k][10] = fmaf(dzz, sc.y, fmaf(z, sd.y, acc[k][10]));
+      acc[k][11] = fmaf(dzz, sc.z, fmaf(z, sd.z, acc[k][11]));
+    }
+  }
+}
+
+}  // namespace vpm
