@@ -43,17 +43,19 @@ int size_bucket(int64_t n) {
 }
 }  // namespace
 
+// Untuned shapes.  The ζ passes do ~15 instructions of pair work per source
+// against a fixed per-source cost, so they take more targets per thread.
 Shape default_shape(int pass, int precision) {
   if (precision == VPM_PREC_FP64) return Shape{128, 1};
-  (void)pass;
-  return Shape{128, 2};
+  return (pass & 1) ? Shape{128, 4} : Shape{128, 2};
 }
 
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n,
                    const Shape* pinned) {
   if (pinned && pinned->block > 0) return *pinned;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  auto it = g_tune.find(std::make_tuple(device, pass, kernel, precision, size_bucket(n)));
+  // The α-derivative passes use the shape tuned for their plain pass.
+  auto it = g_tune.find(std::make_tuple(device, pass & 1, kernel, precision, size_bucket(n)));
   if (it != g_tune.end()) return it->second;
   return default_shape(pass, precision);
 }
@@ -971,6 +973,45 @@ int vpm_set_tile(vpm_ctx* c, int kernel, int precision, const vpm_tile* t) {
   return VPM_OK;
 }
 
+// Time one pass of the context's particles with a given tile shape (best of 3).
+static int time_pass(vpm_ctx* c, int pass, int kernel, int precision, Shape s, cudaEvent_t e0,
+                     cudaEvent_t e1, float* out_ms) {
+  const Shape saved = c->pinned[pass][kernel][precision];
+  c->pinned[pass][kernel][precision] = s;
+  auto enqueue = [&]() {
+    return pass == PASS_UJ ? ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J)
+                           : ctx_pair(c, PASS_ZETA, kernel, precision, 0, c->n, 1.0, c->V, c->raw,
+                                      nullptr);
+  };
+  c->dry = true;
+  c->part_need = 0;
+  enqueue();
+  c->dry = false;
+  int rc = ensure_part(c, c->part_need);
+  if (rc) {
+    c->pinned[pass][kernel][precision] = saved;
+    return rc;
+  }
+  float best = 1e30f;
+  cudaError_t e = enqueue();
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, c->st);
+    e = enqueue();
+    cudaEventRecord(e1, c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    best = std::min(best, t);
+  }
+  c->pinned[pass][kernel][precision] = saved;
+  if (e != cudaSuccess) return cuda_fail(c, e, "autotune launch");
+  *out_ms = best;
+  return VPM_OK;
+}
+
+// Pick the fastest compiled tile shape of the U/J pass and, separately, of the
+// ζ pass for this size bucket; the choice is stored for every context on the
+// device (the α-derivative passes follow their plain pass).
 int vpm_autotune(vpm_ctx* c, int kernel, int precision, vpm_tile* chosen, double* ms) {
   if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
   if (!valid_kernel(kernel) || !valid_prec(precision))
@@ -978,54 +1019,40 @@ int vpm_autotune(vpm_ctx* c, int kernel, int precision, vpm_tile* chosen, double
   if (c->n == 0) return ctx_fail(c, VPM_ERR_STATE, "autotune needs particles");
   DeviceGuard dg(c->device);
   static const Shape cands[] = {{128, 2}, {128, 4}, {256, 2}, {128, 1}};
-  Shape best{0, 0};
-  double best_ms = 1e30;
   cudaEvent_t e0, e1;
   CTX_CK(c, cudaEventCreate(&e0));
   CTX_CK(c, cudaEventCreate(&e1));
-  const Shape saved = c->pinned[PASS_UJ][kernel][precision];
-  for (const Shape& s : cands) {
-    if (!pair_shape_supported(precision, s)) continue;
-    c->pinned[PASS_UJ][kernel][precision] = s;
-    c->dry = true;
-    c->part_need = 0;
-    ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J);
-    c->dry = false;
-    int rc = ensure_part(c, c->part_need);
-    if (rc) return rc;
-    CTX_CK(c, ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J));
-    float best_rep = 1e30f;
-    for (int rep = 0; rep < 3; ++rep) {
-      CTX_CK(c, cudaEventRecord(e0, c->st));
-      CTX_CK(c, ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J));
-      CTX_CK(c, cudaEventRecord(e1, c->st));
-      CTX_CK(c, cudaEventSynchronize(e1));
+  Shape best[2] = {{0, 0}, {0, 0}};
+  double best_ms[2] = {1e30, 1e30};
+  int rc = VPM_OK;
+  for (int pass = PASS_UJ; pass <= PASS_ZETA && rc == VPM_OK; ++pass) {
+    for (const Shape& s : cands) {
+      if (!pair_shape_supported(precision, s)) continue;
       float t = 0.f;
-      cudaEventElapsedTime(&t, e0, e1);
-      best_rep = std::min(best_rep, t);
-    }
-    if (best_rep < best_ms) {
-      best_ms = best_rep;
-      best = s;
+      rc = time_pass(c, pass, kernel, precision, s, e0, e1, &t);
+      if (rc) break;
+      if (t < best_ms[pass]) {
+        best_ms[pass] = t;
+        best[pass] = s;
+      }
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->pinned[PASS_UJ][kernel][precision] = saved;
-  if (best.block == 0) return ctx_fail(c, VPM_ERR_UNSUPPORTED, "no tile shape compiled");
-  store_shape(c->device, PASS_UJ, kernel, precision, c->n, best);
-  store_shape(c->device, PASS_ZETA, kernel, precision, c->n, best);
+  if (rc) return rc;
+  if (best[0].block == 0) return ctx_fail(c, VPM_ERR_UNSUPPORTED, "no tile shape compiled");
+  store_shape(c->device, PASS_UJ, kernel, precision, c->n, best[0]);
+  store_shape(c->device, PASS_ZETA, kernel, precision, c->n, best[1]);
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   c->graphs.clear();
-  c->uj_lo = 0;
-  c->uj_hi = c->n;
+  c->uj_lo = c->uj_hi = 0;   // U/J now hold timing runs of the last candidate
   if (chosen) {
-    chosen->block = best.block;
-    chosen->tpt = best.tpt;
+    chosen->block = best[0].block;
+    chosen->tpt = best[0].tpt;
     chosen->chunk = 0;
-    chosen->reserved = 0;
+    chosen->reserved = best[1].block * 16 + best[1].tpt;   // ζ-pass shape, packed
   }
-  if (ms) *ms = best_ms;
+  if (ms) *ms = best_ms[0];
   return VPM_OK;
 }
 

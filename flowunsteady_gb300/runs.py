@@ -316,11 +316,17 @@ def run_step(args):
     X, G, S = helical_wake(n, turns=12 if n > 500000 else 4)
     f = Field(X, G, S)
     sc = scheme_for(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    tuned = None
+    if args.autotune:
+        tile, ms = L.Tile(), ctypes.c_double()
+        L.check(f.lib.vpm_autotune(f.p, L.KERNEL_GAUSSIANERF, L.PREC_FP32C, ctypes.byref(tile),
+                                   ctypes.byref(ms)), f.p)
+        tuned = {"uj": f"{tile.block}x{tile.tpt}", "zeta": "{}x{}".format(*divmod(tile.reserved, 16))}
     _, t = timed(lambda: f.step(sc, args.dt or 1e-4, nsteps))
     d = f.diag(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
     f.close()
     return {"workload": f"helical wake N={n}", "steps": nsteps, "seconds": t,
-            "seconds_per_step": t / nsteps, "sigma_mean": d["sigma_mean"],
+            "seconds_per_step": t / nsteps, "tile": tuned, "sigma_mean": d["sigma_mean"],
             "nonfinite": d["nonfinite"]}
 
 
@@ -333,6 +339,7 @@ def main(argv=None):
     p.add_argument("--dt", type=float, default=None)
     p.add_argument("--keep", action="store_true", help="include the final state (rings)")
     p.add_argument("--no-reference", action="store_true", help="batch: skip the FP64 fields")
+    p.add_argument("--autotune", action="store_true", help="step: tune the tile shapes first")
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,

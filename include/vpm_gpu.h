@@ -304,14 +304,16 @@ int vpm_batch_get_UJ(vpm_batch* b, int field, double* U, int64_t stride_u, doubl
 int vpm_batch_step(vpm_batch* b, double dt, const vpm_scheme* s, int64_t nsteps, int use_graph);
 
 /* ----------------------------------------------------------- utilities -- */
-/* Tile shape of the FP32 pair kernels: block size, targets per thread and
- * source chunk length.  The autotuner picks one per size bucket on first use
- * (per device, mutex-guarded); these calls expose and pin that choice. */
+/* Tile shape of the pair kernels: block size, targets per thread and source
+ * chunk length.  vpm_autotune times every compiled shape of the U/J pass and,
+ * separately, of the ζ pass on the context's particles and stores the fastest
+ * for that size bucket (log2 N) in a per-device table (mutex-guarded) that
+ * every context then uses; vpm_set_tile pins a shape on one context. */
 typedef struct vpm_tile {
   int32_t block;        /* threads per CTA                         */
   int32_t tpt;          /* targets per thread (register blocking)  */
   int32_t chunk;        /* sources per work item (0 = all)         */
-  int32_t reserved;
+  int32_t reserved;     /* vpm_autotune: ζ-pass shape as block*16 + tpt */
 } vpm_tile;
 int vpm_autotune(vpm_ctx* ctx, int kernel, int precision, vpm_tile* chosen, double* ms);
 int vpm_set_tile(vpm_ctx* ctx, int kernel, int precision, const vpm_tile* t);
