@@ -54,8 +54,9 @@ Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n,
                    const Shape* pinned) {
   if (pinned && pinned->block > 0) return *pinned;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  // The α-derivative passes use the shape tuned for their plain pass.
-  auto it = g_tune.find(std::make_tuple(device, pass & 1, kernel, precision, size_bucket(n)));
+  // Only the plain passes are tuned: the α-derivative passes carry about twice
+  // the registers and keep their default shapes.
+  auto it = g_tune.find(std::make_tuple(device, pass, kernel, precision, size_bucket(n)));
   if (it != g_tune.end()) return it->second;
   return default_shape(pass, precision);
 }
@@ -141,19 +142,9 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.u = pc.u; a.j = pc.j; a.ldo = pc.ldo;
   a.part = part; a.ldp = ldp;
   a.status = pc.status;
-  {
-    // Bulk copies need 16-byte aligned row starts: even ld and tile starts (the
-    // chunk length is a multiple of the block) and 16-byte aligned bases.
-    static const bool disabled = [] {
-      const char* v = std::getenv("VPM_NO_TMA");
-      return v && v[0] && v[0] != '0';
-    }();
-    const bool aligned = (pc.lds % 2 == 0) && (chunk % sh.block == 0) &&
-                         (reinterpret_cast<uintptr_t>(pc.xs) % 16 == 0) &&
-                         (reinterpret_cast<uintptr_t>(pc.gs) % 16 == 0) &&
-                         (reinterpret_cast<uintptr_t>(pc.ss) % 16 == 0);
-    a.tma = (pc.tma_ok && aligned && !disabled) ? 1 : 0;
-  }
+  a.rec = pc.rec;
+  a.tma = (pc.rec && !tma_disabled()) ? 1 : 0;
+  a.far = farfield_enabled() ? 1 : 0;
   cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
   if (n_chunk > 1) {
@@ -161,6 +152,22 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
   return e;
+}
+
+bool tma_disabled() {
+  static const bool off = [] {
+    const char* v = std::getenv("VPM_NO_TMA");
+    return v && v[0] && v[0] != '0';
+  }();
+  return off;
+}
+
+bool farfield_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("VPM_NO_FARFIELD");
+    return !(v && v[0] && v[0] != '0');
+  }();
+  return on;
 }
 
 }  // namespace vpm
@@ -349,6 +356,14 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     a.items = bp->d_items; a.n_items = bp->n_items; a.counter = bp->d_counter;
     a.u = u; a.j = j; a.ldo = c->ld;
     a.part = c->part; a.ldp = c->ld;
+    a.far = farfield_enabled() ? 1 : 0;
+    if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
+      e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec, c->st);
+      if (e != cudaSuccess) return e;
+      c->launches += 1;
+      a.rec = c->rec;
+      a.tma = tma_disabled() ? 0 : 1;
+    }
     e = launch_pair(pass, kernel, prec, bp->shape, a, std::min(bp->resident, bp->n_items), c->st);
     if (e != cudaSuccess) return e;
     c->launches += 1;
@@ -367,8 +382,16 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   pc.sigma_scale = scale;
   pc.u = u; pc.j = j; pc.ldo = c->ld;
   pc.ws = ws; pc.dj = dj;
-  pc.tma_ok = true;        // context rows: ld % 32 == 0, one allocation
   pc.status = c->status;
+  if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
+    if (!c->dry) {
+      cudaError_t e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec,
+                                          c->st);
+      if (e != cudaSuccess) return e;
+      c->launches += 1;
+    }
+    pc.rec = c->rec;
+  }
   const Shape* pinned = &c->pinned[pass & 1][kernel][prec];  // D passes share their plain pass's pin
   PairPlan plan;
   plan.n_chunk = 1;
@@ -575,6 +598,7 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   c->V = p; p += 6 * ld;      // v rows 0..2, w rows 3..5
   c->raw = p; p += 12 * ld;   // raw ζ sums (12 rows for the α-derivative pass)
   cudaError_t e = cudaMemset(c->base, 0, rows * ld * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c->rec, 3 * ld * sizeof(float4));
   if (e == cudaSuccess) e = cudaMalloc(&c->status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(c->status, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->red, (size_t(kRedBlocks) + 1) * kDiagSlots * sizeof(double));
@@ -598,6 +622,7 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->Ut);
   cudaFree(c->part);
   cudaFree(c->ffv);
+  cudaFree(c->rec);
   cudaFree(c->status);
   cudaFree(c->red);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -1011,7 +1036,7 @@ static int time_pass(vpm_ctx* c, int pass, int kernel, int precision, Shape s, c
 
 // Pick the fastest compiled tile shape of the U/J pass and, separately, of the
 // ζ pass for this size bucket; the choice is stored for every context on the
-// device (the α-derivative passes follow their plain pass).
+// device.
 int vpm_autotune(vpm_ctx* c, int kernel, int precision, vpm_tile* chosen, double* ms) {
   if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
   if (!valid_kernel(kernel) || !valid_prec(precision))

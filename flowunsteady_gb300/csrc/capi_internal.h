@@ -31,10 +31,9 @@ struct PairCall {
   double* dj = nullptr;         // PASS_UJD: DJ rows
   int64_t ldo;
   int max_chunks = 0;   // upper bound on source chunks (0 = planner's choice)
-  // The source rows may be staged with bulk copies: the caller guarantees that
-  // reading one element past an odd-length tile stays inside each row's
-  // allocation (context arrays: ld is a multiple of 32 and rows are contiguous).
-  bool tma_ok = false;
+  // FP32 U/J passes: packed records of the ns sources (launch_pack_sources),
+  // or null to read the FP64 rows in the kernel.  Bulk copies stage records.
+  const float4* rec = nullptr;
   int* status = nullptr;
 };
 
@@ -118,6 +117,7 @@ struct vpm_ctx {
   int64_t fail_after = 0;
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
+  float4* rec = nullptr;          // packed source records, 3 per particle (FP32 U/J passes)
   double* ffv = nullptr;          // bound particles (X3 Γ3 σ1) and M (6) rows, ffv_cap apart
   int64_t ffv_cap = 0;
   int64_t launches = 0;           // kernels enqueued (graph replays add their kernel count)

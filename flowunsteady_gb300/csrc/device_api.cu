@@ -48,7 +48,21 @@ extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const 
     cudaError_t e = cudaMallocAsync(&part, need * sizeof(double), st);
     if (e != cudaSuccess) return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate scratch");
   }
-  cudaError_t e = run_pair(pc, dev, sms, nullptr, part, nt, need, nullptr, false, st, nullptr);
+  // FP32 passes read packed source records, as the context path does.
+  float4* rec = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (precision != VPM_PREC_FP64 && ns > 0) {
+    e = cudaMallocAsync(&rec, size_t(ns) * 3 * sizeof(float4), st);
+    if (e != cudaSuccess) {
+      if (part) cudaFreeAsync(part, st);
+      return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate scratch");
+    }
+    e = launch_pack_sources(kernel, ns, Xs, Gs, Ss, ld_s, 1.0, rec, st);
+    pc.rec = rec;
+  }
+  if (e == cudaSuccess)
+    e = run_pair(pc, dev, sms, nullptr, part, nt, need, nullptr, false, st, nullptr);
+  if (rec) cudaFreeAsync(rec, st);
   if (part) cudaFreeAsync(part, st);
   if (e != cudaSuccess)
     return set_error(nullptr, VPM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));

@@ -62,14 +62,25 @@ struct PairArgs {
   int64_t ldo;
   double* part;
   int64_t ldp;
-  // Stage source tiles with bulk asynchronous copies (set by the host only when
-  // every row start is 16-byte aligned and the even-padded tiles stay inside
-  // the rows' allocation).
+  // FP32 U/J passes: packed source records, 3 float4 per source (null: read
+  // and convert the FP64 rows in the kernel).  Records are 16-byte aligned.
+  const float4* rec;
+  // Stage the records with bulk asynchronous copies (PASS_UJ; needs rec).
   int32_t tma;
+  // Gaussian-erf FP32 passes: classify (warp, 32-source) blocks by their
+  // bounding boxes and take the far-field forms (0 = always the general form).
+  int32_t far;
   int* status;   // STATUS_TIMEOUT is OR-ed here if a copy wait gives up (may be null)
 };
 
 // Tile shape of a launch.
+// Far-field classification of the Gaussian-erf FP32 passes is on unless the
+// environment sets VPM_NO_FARFIELD (to non-zero).
+bool farfield_enabled();
+// Bulk-copy staging of the packed records is on unless VPM_NO_TMA is set (to
+// non-zero); the kernels then read the records with plain loads.
+bool tma_disabled();
+
 struct Shape {
   int block;   // threads per CTA
   int tpt;     // targets per thread
@@ -90,6 +101,11 @@ bool pair_shape_supported(int precision, Shape shape);
 // Targets are [t_begin, t_end); the slot count of target i is scalar_chunks
 // when foff is null, else found from the device field table (foff[f] <= i,
 // fchunks[f]); targets whose count is 1 are skipped (already final).
+// Packed source records (3 float4 per source) of n particles for the FP32
+// U/J passes with kernel constants of σ·scale.
+cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
+                                const double* S, int64_t ld, double scale, float4* rec,
+                                cudaStream_t st);
 cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,

@@ -29,6 +29,38 @@ cudaError_t launch_pair(int pass, int kernel, int precision, Shape s, const Pair
   return launch_pair_d(pass, kernel, precision, s, a, grid, st);
 }
 
+// Packed source records of the FP32 U/J passes, per source
+//   (xh, yh, zh, a), (xl, yl, zl, b), (Γx, Γy, Γz, 0)
+// with x ≈ xh + xl (split_f32) and (a, b) the kernel constants of σ·scale.
+template <int KERNEL>
+__global__ void __launch_bounds__(256) pack_sources_kernel(int64_t n, const double* __restrict__ X,
+                                                           const double* __restrict__ G,
+                                                           const double* __restrict__ S, int64_t ld,
+                                                           double scale, float4* __restrict__ rec) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float xh, xl, yh, yl, zh, zl, ka, kb;
+  split_f32(X[i], xh, xl);
+  split_f32(X[ld + i], yh, yl);
+  split_f32(X[2 * ld + i], zh, zl);
+  source_consts<KERNEL, float>(S[i] * scale, ka, kb);
+  rec[3 * i] = make_float4(xh, yh, zh, ka);
+  rec[3 * i + 1] = make_float4(xl, yl, zl, kb);
+  rec[3 * i + 2] = make_float4(float(G[i]), float(G[ld + i]), float(G[2 * ld + i]), 0.f);
+}
+
+cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
+                                const double* S, int64_t ld, double scale, float4* rec,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = int((n + 255) / 256);
+  if (kernel == VPM_KERNEL_WINCKELMANS)
+    pack_sources_kernel<VPM_KERNEL_WINCKELMANS><<<grid, 256, 0, st>>>(n, X, G, S, ld, scale, rec);
+  else
+    pack_sources_kernel<VPM_KERNEL_GAUSSIANERF><<<grid, 256, 0, st>>>(n, X, G, S, ld, scale, rec);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,

@@ -51,18 +51,28 @@ struct PairTraits {
   static constexpr bool kD = PASS == PASS_UJD || PASS == PASS_ZETAD;
   // shared quads per source: (x, a), (Γ, b), and for ζ passes v_q (and w_q)
   static constexpr int kQuads = kUJ ? 2 : (PASS == PASS_ZETA ? 3 : 4);
-  // The FP32 U/J pass can stage its FP64 source rows with bulk copies.
+  // The FP32 U/J passes read packed source records (3 float4 per source, see
+  // pack_sources_kernel); the plain U/J pass stages them with bulk copies.
+  static constexpr bool kRec = kUJ && PREC != VPM_PREC_FP64;
   static constexpr bool kTma = PASS == PASS_UJ && PREC != VPM_PREC_FP64;
-  static constexpr int kTmaRows = 7;   // x, y, z, Γx, Γy, Γz, σ
+  static constexpr int kRecBytes = 48;
 };
+
+// Shared memory: source quads, then (FP32) the far-field boxes (per warp two
+// float4 for its staged sources and two for its targets), then (FP32C) the
+// fold pairs, then (bulk copies) the staging rows and the mbarrier.
+template <int PASS, int PREC>
+__host__ __device__ constexpr size_t box_bytes(int block) {
+  return PREC == VPM_PREC_FP64 ? 0 : size_t(block / 32) * 4 * 16;
+}
 
 template <int PASS, int PREC>
 __host__ __device__ constexpr size_t smem_bytes(int block, int tpt) {
   using Tr = PairTraits<PASS, PREC>;
   size_t src = size_t(block) * Tr::kQuads * sizeof(Quad<typename Tr::R>);
   size_t fold = Tr::kComp ? size_t(block) * tpt * Tr::kNval * 2 * sizeof(float) : 0;
-  size_t stage = Tr::kTma ? size_t(block) * Tr::kTmaRows * sizeof(double) + 16 : 0;
-  return src + fold + stage;
+  size_t stage = Tr::kTma ? size_t(block) * Tr::kRecBytes + 16 : 0;
+  return src + box_bytes<PASS, PREC>(block) + fold + stage;
 }
 
 // Minimum resident CTAs requested from the compiler: caps the FP32 U/J kernels
@@ -127,39 +137,43 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   Quad<R>* tileB = tileA + BLOCK;
   Quad<R>* tileC = tileB + BLOCK;  // ζ passes: v_q
   Quad<R>* tileD = tileC + BLOCK;  // PASS_ZETAD: w_q
-  float* fold_hi = reinterpret_cast<float*>(smem_raw + size_t(BLOCK) * Tr::kQuads * sizeof(Quad<R>));
+  constexpr size_t kQuadBytes = size_t(BLOCK) * Tr::kQuads * sizeof(Quad<R>);
+  constexpr size_t kBoxBytes = box_bytes<PASS, PREC>(BLOCK);
+  // Far-field boxes of warp w: sources at sbox[2w..2w+1], targets at tbox[2w..2w+1].
+  float4* sbox = reinterpret_cast<float4*>(smem_raw + kQuadBytes);
+  float4* tbox = sbox + 2 * (BLOCK / 32);
+  float* fold_hi = reinterpret_cast<float*>(smem_raw + kQuadBytes + kBoxBytes);
   float* fold_lo = fold_hi + size_t(BLOCK) * T * NV;
-  // TMA staging: kTmaRows FP64 rows of BLOCK sources, then the mbarrier.
-  double* stage = reinterpret_cast<double*>(
-      smem_raw + size_t(BLOCK) * Tr::kQuads * sizeof(Quad<R>) +
-      (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
-  uint64_t* bar = reinterpret_cast<uint64_t*>(stage + size_t(BLOCK) * Tr::kTmaRows);
+  // Bulk-copy staging: the records of BLOCK sources, then the mbarrier.
+  float4* stage = reinterpret_cast<float4*>(
+      smem_raw + kQuadBytes + kBoxBytes + (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage + size_t(BLOCK) * 3);
   __shared__ int s_item;
 
   const int tid = threadIdx.x;
   const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
   const bool same_arrays = a.xt == a.xs && a.ldt == a.lds;
-  const bool use_tma = Tr::kTma && a.tma != 0;
+  // Packed records replace the FP64 source reads (and their conversion) when
+  // the host provides them; bulk copies need them.
+  const bool use_rec = Tr::kRec && a.rec != nullptr;
+  const bool use_tma = Tr::kTma && use_rec && a.tma != 0;
+  // Gaussian-erf FP32 passes classify (warp, 32 sources) blocks by distance.
+  constexpr bool kFarKernel = F32 && KERNEL == VPM_KERNEL_GAUSSIANERF;
+  const bool use_far = kFarKernel && a.far != 0;
+  const int warp = tid >> 5;
   uint32_t phase = 0;
   if (use_tma) {
     if (tid == 0) mbar_init(bar, 1);
     __syncthreads();
   }
-  // Copies of the source tile [tile, tile + cnt) into the staging rows: each
-  // row is padded to an even count (16-byte multiple); the host guarantees the
-  // padded element lies inside the row's allocation.
+  // One bulk copy of the records of the source tile [tile, tile + cnt): 48·cnt
+  // bytes from a 16-byte aligned address (48-byte records, aligned base).
   auto issue = [&](int64_t tile, int64_t send) {
     const int cnt = int(min(int64_t(BLOCK), send - tile));
-    const uint32_t bytes = uint32_t((cnt + 1) & ~1) * uint32_t(sizeof(double));
+    const uint32_t bytes = uint32_t(cnt) * uint32_t(Tr::kRecBytes);
     fence_proxy_async_smem();
-    mbar_arrive_expect_tx(bar, bytes * Tr::kTmaRows);
-    bulk_g2s(stage + 0 * BLOCK, a.xs + tile, bytes, bar);
-    bulk_g2s(stage + 1 * BLOCK, a.xs + a.lds + tile, bytes, bar);
-    bulk_g2s(stage + 2 * BLOCK, a.xs + 2 * a.lds + tile, bytes, bar);
-    bulk_g2s(stage + 3 * BLOCK, a.gs + tile, bytes, bar);
-    bulk_g2s(stage + 4 * BLOCK, a.gs + a.lds + tile, bytes, bar);
-    bulk_g2s(stage + 5 * BLOCK, a.gs + 2 * a.lds + tile, bytes, bar);
-    bulk_g2s(stage + 6 * BLOCK, a.ss + tile, bytes, bar);
+    mbar_arrive_expect_tx(bar, bytes);
+    bulk_g2s(stage, a.rec + 3 * tile, bytes, bar);
   };
 
   int item;
@@ -193,6 +207,15 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       cy = a.xt[a.ldt + t0];
       cz = a.xt[2 * a.ldt + t0];
     }
+    // With records, relative positions come from the (hi, lo) float split of
+    // both ends, (h - ch) + (l - cl), for targets and sources alike, so that
+    // coincident particles stay exactly coincident.
+    float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
+    if (use_rec && COMP) {
+      split_f32(cx, chx, clx);
+      split_f32(cy, chy, cly);
+      split_f32(cz, chz, clz);
+    }
 
     R tx[T], ty[T], tz[T];
 #pragma unroll
@@ -200,10 +223,24 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       const int64_t i = t0 + k * BLOCK + tid;
       if (i < t1) {
         const double px = a.xt[i], py = a.xt[a.ldt + i], pz = a.xt[2 * a.ldt + i];
-        tx[k] = R(px - cx); ty[k] = R(py - cy); tz[k] = R(pz - cz);
+        if (use_rec) {
+          float h, l;
+          split_f32(px, h, l);
+          tx[k] = R(rel_f32(h, l, chx, clx));
+          split_f32(py, h, l);
+          ty[k] = R(rel_f32(h, l, chy, cly));
+          split_f32(pz, h, l);
+          tz[k] = R(rel_f32(h, l, chz, clz));
+        } else {
+          tx[k] = R(px - cx); ty[k] = R(py - cy); tz[k] = R(pz - cz);
+        }
       } else {
         tx[k] = R(0); ty[k] = R(0); tz[k] = R(0);
       }
+    }
+
+    if constexpr (kFarKernel) {
+      if (use_far) warp_target_box<T>(tx, ty, tz, tbox + 2 * warp);
     }
 
     R acc[T][NV];
@@ -240,14 +277,13 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           const int64_t jj = tile0 + tid;
           Quad<R> qa, qb;
           if (jj < s1) {
-            const double sig = stage[6 * BLOCK + tid] * a.sigma_scale;
-            qa.x = R(stage[0 * BLOCK + tid] - cx);
-            qa.y = R(stage[1 * BLOCK + tid] - cy);
-            qa.z = R(stage[2 * BLOCK + tid] - cz);
-            qb.x = R(stage[3 * BLOCK + tid]);
-            qb.y = R(stage[4 * BLOCK + tid]);
-            qb.z = R(stage[5 * BLOCK + tid]);
-            source_consts<KERNEL, R>(sig, qa.w, qb.w);
+            const float4 r0 = stage[3 * tid], r1 = stage[3 * tid + 1], r2 = stage[3 * tid + 2];
+            qa.x = R(rel_f32(r0.x, r1.x, chx, clx));
+            qa.y = R(rel_f32(r0.y, r1.y, chy, cly));
+            qa.z = R(rel_f32(r0.z, r1.z, chz, clz));
+            qa.w = R(r0.w);
+            qb.x = R(r2.x); qb.y = R(r2.y); qb.z = R(r2.z);
+            qb.w = R(r1.w);
           } else {
             qa.x = qa.y = qa.z = R(0);
             qb.x = qb.y = qb.z = R(0);
@@ -255,6 +291,9 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           }
           tileA[tid] = qa;
           tileB[tid] = qb;
+          if constexpr (kFarKernel) {
+            if (use_far) warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
+          }
           __syncthreads();  // quads ready, staging rows consumed
           if (tid == 0 && tile0 + BLOCK < s1) issue(tile0 + BLOCK, s1);
         }
@@ -264,7 +303,15 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         Quad<R> qa, qb, qc, qd;
         qc.x = qc.y = qc.z = qc.w = R(0);
         qd.x = qd.y = qd.z = qd.w = R(0);
-        if (jj < s1) {
+        if (use_rec && jj < s1) {
+          const float4 r0 = a.rec[3 * jj], r1 = a.rec[3 * jj + 1], r2 = a.rec[3 * jj + 2];
+          qa.x = R(rel_f32(r0.x, r1.x, chx, clx));
+          qa.y = R(rel_f32(r0.y, r1.y, chy, cly));
+          qa.z = R(rel_f32(r0.z, r1.z, chz, clz));
+          qa.w = R(r0.w);
+          qb.x = R(r2.x); qb.y = R(r2.y); qb.z = R(r2.z);
+          qb.w = R(r1.w);
+        } else if (jj < s1) {
           const double px = a.xs[jj], py = a.xs[a.lds + jj], pz = a.xs[2 * a.lds + jj];
           const double sig = a.ss[jj] * a.sigma_scale;
           qa.x = R(px - cx); qa.y = R(py - cy); qa.z = R(pz - cz);
@@ -293,6 +340,9 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         tileB[tid] = qb;
         if (!Tr::kUJ) tileC[tid] = qc;
         if (PASS == PASS_ZETAD) tileD[tid] = qd;
+        if constexpr (kFarKernel) {
+          if (use_far) warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
+        }
         __syncthreads();
       }
 
@@ -312,8 +362,17 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 #pragma unroll 2
             for (int js = 0; js < cnt; ++js) uj_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
           } else {
+            // Gaussian-erf in blocks of 32 sources: far blocks skip erfcx/exp.
+            for (int u = 0; u < cnt; u += 32) {
+              const int ue = min(u + 32, cnt);
+              if (use_far && box_arg_bound(tbox + 2 * warp, sbox + (u >> 4)) <= kArgFar) {
 #pragma unroll 2
-            for (int js = 0; js < cnt; ++js) uj_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc);
+                for (int js = u; js < ue; ++js) uj_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+              } else {
+#pragma unroll 2
+                for (int js = u; js < ue; ++js) uj_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc, use_far);
+              }
+            }
           }
         } else {
           if (KERNEL == VPM_KERNEL_WINCKELMANS && !own) {
@@ -321,7 +380,19 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           } else if (KERNEL == VPM_KERNEL_WINCKELMANS) {
             for (int js = 0; js < cnt; ++js) ujd_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
           } else {
-            for (int js = 0; js < cnt; ++js) ujd_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc);
+            // Gaussian-erf: where Dq and Dp vanish only the plain sums take the
+            // pair; far blocks skip erfcx.
+            for (int u = 0; u < cnt; u += 32) {
+              const int ue = min(u + 32, cnt);
+              const float bound = use_far ? box_arg_bound(tbox + 2 * warp, sbox + (u >> 4)) : 0.f;
+              if (bound <= kArgZero) {
+                for (int js = u; js < ue; ++js) uj_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+              } else if (bound <= kArgFar) {
+                for (int js = u; js < ue; ++js) ujd_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+              } else {
+                for (int js = u; js < ue; ++js) ujd_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc, use_far);
+              }
+            }
           }
         }
       } else if constexpr (Tr::kUJ) {
@@ -363,14 +434,30 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         const float4* tc = reinterpret_cast<const float4*>(tileC);
         const float4* td = reinterpret_cast<const float4*>(PASS == PASS_ZETAD ? tileD : tileC);
         constexpr bool DD = PASS == PASS_ZETAD;
-        if (!own) {
+        if (kFarKernel && use_far) {
+          // Gaussian-erf: blocks of 32 sources whose ζ is exactly zero at every
+          // target of the warp are skipped.
+          for (int u = 0; u < cnt; u += 32) {
+            if (box_arg_bound(tbox + 2 * warp, sbox + (u >> 4)) <= kArgZero) continue;
+            const int ue = min(u + 32, cnt);
+            if (!own) {
+#pragma unroll 2
+              for (int js = u; js < ue; ++js)
+                zeta_source<KERNEL, T, false, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
+            } else {
+#pragma unroll 2
+              for (int js = u; js < ue; ++js)
+                zeta_source<KERNEL, T, true, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
+            }
+          }
+        } else if (!own) {
 #pragma unroll 2
           for (int js = 0; js < cnt; ++js)
-            zeta_source<KERNEL, T, false, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+            zeta_source<KERNEL, T, false, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
         } else {
 #pragma unroll 2
           for (int js = 0; js < cnt; ++js)
-            zeta_source<KERNEL, T, true, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+            zeta_source<KERNEL, T, true, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
         }
       } else {
         // ζ passes, FP64.

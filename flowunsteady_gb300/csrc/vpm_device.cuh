@@ -193,6 +193,18 @@ __device__ inline double pair_zeta(double r2, double a, double b) {
   return r2 > 0.0 ? z : 0.0;
 }
 
+// x ≈ h + l with h the float nearest x and l the float nearest x - h.
+__host__ __device__ inline void split_f32(double x, float& h, float& l) {
+  h = float(x);
+  l = float(x - double(h));
+}
+
+// Position relative to a reference point, both in (h, l) form: (h - ch) + (l - cl)
+// in FP32, within one rounding of the exact difference when h and ch are close.
+__device__ __forceinline__ float rel_f32(float h, float l, float ch, float cl) {
+  return __fadd_rn(__fadd_rn(h, -ch), __fadd_rn(l, -cl));
+}
+
 // Knuth's TwoSum: s + e == a + b exactly (round-to-nearest, no reassociation).
 __device__ inline void two_sum(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);
@@ -293,29 +305,49 @@ __device__ __forceinline__ void uj_source_winck(const float4 sa, const float4 sb
   }
 }
 
+constexpr float kArgFar = float(-0.5 * kLog2e * 50.0);
+constexpr float kArgZero = -128.f;
+
 // Gaussian-erf: source quads (x, y, z, -log2(e)/(2σ²)) and (Γx, Γy, Γz, 1/σ).
-// All T targets take the erf-free form; one warp vote per source sends the
-// rare warps holding a pair with ρ² < 3/2 (or the self pair) through the series.
+// A warp vote per source takes the far form (q = 1/r³, p = -3/r⁵; see the
+// far-field notes below) when every pair of the warp has ρ² >= 50; otherwise
+// all T targets take the erf-free form, and a second vote sends the rare warps
+// holding a pair with ρ² < 3/2 (or the self pair) through the series.
 template <int T>
 __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb,
                                                 const float (&tx)[T], const float (&ty)[T],
-                                                const float (&tz)[T], float (&acc)[T][15]) {
+                                                const float (&tz)[T], float (&acc)[T][15],
+                                                bool far) {
   const float ea = sa.w, is1 = sb.w;
-  const float kt = kErfcxP * is1;                      // t = 1/(1 + kt r)
-  const float kc = float(kSqrt2overPi) * is1;          // √(2/π) ρ = kc r
-  const float k3 = float(kSqrt2overPi) * is1 * is1 * is1;
-  float dx[T], dy[T], dz[T], arg[T], q[T], p[T];
+  float dx[T], dy[T], dz[T], r2[T], arg[T], q[T], p[T];
   float amax = -INFINITY;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
     dx[k] = tx[k] - sa.x;
     dy[k] = ty[k] - sa.y;
     dz[k] = tz[k] - sa.z;
-    const float r2 = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
-    arg[k] = r2 * ea;
+    r2[k] = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
+    arg[k] = r2[k] * ea;
     amax = fmaxf(amax, arg[k]);
-    const float ri = rsqrt_ftz(r2);
-    const float r = r2 * ri;
+  }
+  if (far && __all_sync(0xffffffffu, amax <= kArgFar)) {
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      const float ri = rsqrt_ftz(r2[k]);
+      const float ri2 = ri * ri;
+      q[k] = ri2 * ri;
+      p[k] = (-3.f * q[k]) * ri2;
+      accum_pair(dx[k], dy[k], dz[k], q[k], p[k], sb.x, sb.y, sb.z, acc[k]);
+    }
+    return;
+  }
+  const float kt = kErfcxP * is1;                      // t = 1/(1 + kt r)
+  const float kc = float(kSqrt2overPi) * is1;          // √(2/π) ρ = kc r
+  const float k3 = float(kSqrt2overPi) * is1 * is1 * is1;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float ri = rsqrt_ftz(r2[k]);
+    const float r = r2[k] * ri;
     const float e = ex2_ftz(arg[k]);
     const float t = rcp_ftz(fmaf(kt, r, 1.f));
     const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
@@ -339,6 +371,97 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
   }
 #pragma unroll
   for (int k = 0; k < T; ++k) accum_pair(dx[k], dy[k], dz[k], q[k], p[k], sb.x, sb.y, sb.z, acc[k]);
+}
+
+// ---- Gaussian-erf far field ---------------------------------------------------
+// With the exponent argument arg = r²·(-log2(e)/(2σ²)) = -log2(e)·ρ²/2:
+//  - arg <= kArgFar (ρ² >= 50): e^{-ρ²/2}(erfcx(ρ/√2) + √(2/π)ρ) < 1e-10, far
+//    below half an FP32 ulp of 1, so g rounds to 1; the √(2/π)ρ³e term of
+//    q'/r is below 2e-9 of 3g.  The general path then yields q = 1/r³ and
+//    p = -3/r⁵ (up to a tie-break in the last bit of p), which is what the
+//    far routines compute, without erfcx, exp or the series test.
+//  - arg <= kArgZero: 2^arg is subnormal and ex2.approx.ftz returns +0, so
+//    ζ_σ, Dζ, Dq and Dp are exactly zero in FP32.
+// The classification is made per warp and per 32 staged sources from bounding
+// boxes (warp_target_box, warp_source_box): the box gap g² satisfies
+// g² <= r² for every pair of the two boxes in the same FP32 arithmetic
+// (rounding is monotone), so g²·max(a) >= arg for every pair.  Blocks that do
+// not pass as a whole are classified again per source by warp votes
+// (uj_source_gauss, ujd_source_gauss, zeta_source).  kArgFar and kArgZero are
+// defined above uj_source_gauss.
+// q = 1/r³, p = -3/r⁵ for one source against T targets; acc holds the plain
+// sums first (U 0..2, A 3..10, W 12..14), so the α-derivative layout works too.
+template <int T, int NV>
+__device__ __forceinline__ void uj_source_gauss_far(const float4 sa, const float4 sb,
+                                                    const float (&tx)[T], const float (&ty)[T],
+                                                    const float (&tz)[T], float (&acc)[T][NV]) {
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float ri = rsqrt_ftz(r2);
+    const float ri2 = ri * ri;
+    const float q = ri2 * ri;
+    const float p = (-3.f * q) * ri2;
+    accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
+  }
+}
+
+// 6 xor-shuffle reductions: every lane ends with the warp's box.
+__device__ __forceinline__ void warp_box_reduce(float& lx, float& ly, float& lz, float& hx,
+                                                float& hy, float& hz) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+    ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+    lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+    hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+    hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+    hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+  }
+}
+
+// Box of the T·32 targets of a warp, stored as (lo, 0), (hi, 0) at box[0..1].
+template <int T>
+__device__ __forceinline__ void warp_target_box(const float (&tx)[T], const float (&ty)[T],
+                                                const float (&tz)[T], float4* box) {
+  float lx = tx[0], ly = ty[0], lz = tz[0], hx = tx[0], hy = ty[0], hz = tz[0];
+#pragma unroll
+  for (int k = 1; k < T; ++k) {
+    lx = fminf(lx, tx[k]); ly = fminf(ly, ty[k]); lz = fminf(lz, tz[k]);
+    hx = fmaxf(hx, tx[k]); hy = fmaxf(hy, ty[k]); hz = fmaxf(hz, tz[k]);
+  }
+  warp_box_reduce(lx, ly, lz, hx, hy, hz);
+  if ((threadIdx.x & 31) == 0) {
+    box[0] = make_float4(lx, ly, lz, 0.f);
+    box[1] = make_float4(hx, hy, hz, 0.f);
+  }
+}
+
+// Box of the 32 sources a warp staged, with the largest exponent constant a
+// (the widest core) in lo.w; padding sources are left out.
+__device__ __forceinline__ void warp_source_box(float x, float y, float z, float a, bool valid,
+                                                float4* box) {
+  float lx = valid ? x : INFINITY, ly = valid ? y : INFINITY, lz = valid ? z : INFINITY;
+  float hx = valid ? x : -INFINITY, hy = valid ? y : -INFINITY, hz = valid ? z : -INFINITY;
+  float w = valid ? a : -INFINITY;
+  warp_box_reduce(lx, ly, lz, hx, hy, hz);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+  if ((threadIdx.x & 31) == 0) {
+    box[0] = make_float4(lx, ly, lz, w);
+    box[1] = make_float4(hx, hy, hz, 0.f);
+  }
+}
+
+// Upper bound of the exponent argument over all pairs of a target box and a
+// source box (both read from shared memory; the result is warp-uniform).
+__device__ __forceinline__ float box_arg_bound(const float4* tbox, const float4* sbox) {
+  const float4 tl = tbox[0], th = tbox[1], sl = sbox[0], sh = sbox[1];
+  const float gx = fmaxf(0.f, fmaxf(sl.x - th.x, tl.x - sh.x));
+  const float gy = fmaxf(0.f, fmaxf(sl.y - th.y, tl.y - sh.y));
+  const float gz = fmaxf(0.f, fmaxf(sl.z - th.z, tl.z - sh.z));
+  return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) * sl.w;
 }
 
 }  // namespace vpm
@@ -417,24 +540,46 @@ __device__ __forceinline__ void ujd_source_winck(const float4 sa, const float4 s
 template <int T>
 __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 sb,
                                                  const float (&tx)[T], const float (&ty)[T],
-                                                 const float (&tz)[T], float (&acc)[T][27]) {
+                                                 const float (&tz)[T], float (&acc)[T][27],
+                                                 bool far) {
   const float ea = sa.w, is1 = sb.w;
-  const float kt = kErfcxP * is1;
-  const float kc = float(kSqrt2overPi) * is1;
   const float is2 = is1 * is1;
   const float k3 = float(kSqrt2overPi) * is2 * is1;
-  float dx[T], dy[T], dz[T], arg[T], q[T], p[T], dq[T], dp[T];
+  float dx[T], dy[T], dz[T], r2[T], arg[T], q[T], p[T], dq[T], dp[T];
   float amax = -INFINITY;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
     dx[k] = tx[k] - sa.x;
     dy[k] = ty[k] - sa.y;
     dz[k] = tz[k] - sa.z;
-    const float r2 = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
-    arg[k] = r2 * ea;
+    r2[k] = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
+    arg[k] = r2[k] * ea;
     amax = fmaxf(amax, arg[k]);
-    const float ri = rsqrt_ftz(r2);
-    const float r = r2 * ri;
+  }
+  // Per-source far forms, as in uj_source_gauss (Dq = Dp = 0 below kArgZero).
+  if (far && __all_sync(0xffffffffu, amax <= kArgFar)) {
+    const bool zero = __all_sync(0xffffffffu, amax <= kArgZero);
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      const float ri = rsqrt_ftz(r2[k]);
+      const float ri2 = ri * ri;
+      const float qq = ri2 * ri;
+      const float pp = (-3.f * qq) * ri2;
+      if (zero) {
+        accum_pair(dx[k], dy[k], dz[k], qq, pp, sb.x, sb.y, sb.z, acc[k]);
+      } else {
+        const float k3e = k3 * ex2_ftz(arg[k]);
+        accum_pair_d(dx[k], dy[k], dz[k], qq, pp, -k3e, k3e * is2, sb.x, sb.y, sb.z, acc[k]);
+      }
+    }
+    return;
+  }
+  const float kt = kErfcxP * is1;
+  const float kc = float(kSqrt2overPi) * is1;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float ri = rsqrt_ftz(r2[k]);
+    const float r = r2[k] * ri;
     const float e = ex2_ftz(arg[k]);
     const float t = rcp_ftz(fmaf(kt, r, 1.f));
     const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
@@ -464,6 +609,29 @@ __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 s
 #pragma unroll
   for (int k = 0; k < T; ++k)
     accum_pair_d(dx[k], dy[k], dz[k], q[k], p[k], dq[k], dp[k], sb.x, sb.y, sb.z, acc[k]);
+}
+
+// ujd_source_gauss for a source with arg <= kArgFar at every target: q and p
+// as in uj_source_gauss_far, Dq = -√(2/π)e/σ³ and Dp = √(2/π)e/σ⁵ as in the
+// general path.
+template <int T>
+__device__ __forceinline__ void ujd_source_gauss_far(const float4 sa, const float4 sb,
+                                                     const float (&tx)[T], const float (&ty)[T],
+                                                     const float (&tz)[T], float (&acc)[T][27]) {
+  const float ea = sa.w, is1 = sb.w;
+  const float is2 = is1 * is1;
+  const float k3 = float(kSqrt2overPi) * is2 * is1;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
+    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float ri = rsqrt_ftz(r2);
+    const float ri2 = ri * ri;
+    const float q = ri2 * ri;
+    const float p = (-3.f * q) * ri2;
+    const float k3e = k3 * ex2_ftz(r2 * ea);
+    accum_pair_d(dx, dy, dz, q, p, -k3e, k3e * is2, sb.x, sb.y, sb.z, acc[k]);
+  }
 }
 
 // FP64 α-derivatives of one pair (zero when r² == 0).
@@ -617,25 +785,34 @@ template <int KERNEL, int T, bool MASK, bool D>
 __device__ __forceinline__ void zeta_source(const float4 sa, const float4 sb, const float4 sc,
                                             const float4 sd, const float (&tx)[T],
                                             const float (&ty)[T], const float (&tz)[T],
-                                            float (&acc)[T][D ? 12 : 6]) {
+                                            float (&acc)[T][D ? 12 : 6], bool far) {
+  float r2[T];
+  float amax = -INFINITY;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
     const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    r2[k] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (KERNEL != VPM_KERNEL_WINCKELMANS) amax = fmaxf(amax, r2[k] * sa.w);
+  }
+  // Gaussian-erf: a source whose ζ underflows to +0 at every target of the
+  // warp (exponent argument <= kArgZero) adds nothing.
+  if (KERNEL != VPM_KERNEL_WINCKELMANS && far && __all_sync(0xffffffffu, amax <= kArgZero)) return;
+#pragma unroll
+  for (int k = 0; k < T; ++k) {
     float z, dzz = 0.f;
     if (KERNEL == VPM_KERNEL_WINCKELMANS) {
-      const float rs = rsqrt_ftz(fmaf(r2, sa.w, sb.w));
+      const float rs = rsqrt_ftz(fmaf(r2[k], sa.w, sb.w));
       const float rs2 = rs * rs;
       z = (rs2 * rs2) * (rs2 * rs);
       if (D) dzz = z * fmaf(sc.w, rs2, 4.f);
     } else {
-      const float x = r2 * sa.w;
+      const float x = r2[k] * sa.w;
       z = sb.w * ex2_ftz(x);
       if (D) dzz = z * fmaf(x, kArgToRho2, -3.f);
     }
     if (MASK) {
-      z = r2 > 0.f ? z : 0.f;
-      if (D) dzz = r2 > 0.f ? dzz : 0.f;
+      z = r2[k] > 0.f ? z : 0.f;
+      if (D) dzz = r2[k] > 0.f ? dzz : 0.f;
     }
     acc[k][0] = fmaf(z, sb.x, acc[k][0]);
     acc[k][1] = fmaf(z, sb.y, acc[k][1]);

@@ -233,3 +233,67 @@ def test_context_and_device_pointer_paths_agree_bitwise(n):
         torch.cuda.synchronize()
         assert np.array_equal(Ud.cpu().numpy().T, U_ref)
         assert np.array_equal(Jd.cpu().numpy().T.reshape(n, 3, 3), J_ref)
+
+
+_GENERAL_FORMS_SCRIPT = r"""
+import sys, ctypes, numpy as np
+sys.path.insert(0, sys.argv[1])
+from tests.helpers import Ctx, scheme
+from flowunsteady_gb300.workloads import helical_wake
+from flowunsteady_gb300 import _lib as L
+X, G, S = helical_wake(int(sys.argv[2]))
+flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
+out = {}
+with Ctx(X.shape[0]) as c:
+    c.set(X, G, S)
+    for p in (1, 2):
+        c.rc(c.lib.vpm_set_tile(c.p, 1, p, ctypes.byref(L.Tile(128, 2, 0, 0))))
+    for p in (1, 2):
+        out[f"U{p}"], out[f"J{p}"] = c.uj(1, p)
+    sc = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
+    c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
+    out["C"], out["E"] = c.sfs()
+    c.step(sc, 1e-4, nsteps=2)
+    out["X"], out["G"], out["S"] = c.state()
+np.savez(sys.argv[3], **out)
+"""
+
+
+def test_gaussian_far_field_forms_match_general_forms(tmp_path, oracle):
+    # Warp/32-source blocks with ρ² >= 50 at every pair take q = 1/r³,
+    # p = -3/r⁵, and blocks where ζ underflows to zero are skipped in the ζ
+    # passes; VPM_NO_FARFIELD=1 forces the general forms everywhere.  The
+    # helical wake (coherent particle order) takes the far forms for most blocks.
+    import subprocess
+    import sys
+    n = 30000
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = tmp_path / "general.npz"
+    script = tmp_path / "general.py"
+    script.write_text(_GENERAL_FORMS_SCRIPT)
+    env = dict(os.environ, VPM_NO_FARFIELD="1")
+    subprocess.run([sys.executable, str(script), root, str(n), str(out)], check=True, env=env,
+                   timeout=300)
+    ref = np.load(out)
+    X, G, S = helical_wake(n)
+    flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
+    with Ctx(n) as c:
+        c.set(X, G, S)
+        for p in (1, 2):
+            c.rc(c.lib.vpm_set_tile(c.p, 1, p, ctypes.byref(L.Tile(128, 2, 0, 0))))
+        for p in (1, 2):
+            U, J = c.uj(1, p)
+            # Same pair values up to a last-bit tie in p.
+            assert rel_l2(U, ref[f"U{p}"]) <= 1e-7 and rel_l2(J, ref[f"J{p}"]) <= 1e-7
+        sc = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
+        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
+        C, E = c.sfs()
+        assert rel_l2(E, ref["E"]) <= 1e-6 and rel_l2(C, ref["C"]) <= 1e-4
+        c.step(sc, 1e-4, nsteps=2)
+        Xs, Gs, Ss = c.state()
+    assert np.abs(Xs - ref["X"]).max() <= 1e-9 and rel_l2(Gs, ref["G"]) <= 1e-6
+    assert rel_max(Ss, ref["S"]) <= 1e-7
+    # And both against the FP64 oracle on a target sample.
+    idx = np.sort(np.random.default_rng(9).choice(n, 400, replace=False))
+    U0, J0 = oracle.uj_direct(1, X, G, S, Xt=X[idx])
+    assert rel_l2(ref["U2"][idx], U0) <= 1e-5 and rel_l2(ref["J2"][idx], J0) <= 1e-5
