@@ -145,6 +145,8 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.rec = pc.rec;
   a.tma = (pc.rec && !tma_disabled()) ? 1 : 0;
   a.far = farfield_enabled() ? 1 : 0;
+  a.coh = pc.coh;
+  a.coh_blocks = ceil_div(pc.ns, 32);
   cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
   if (n_chunk > 1) {
@@ -357,8 +359,10 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     a.u = u; a.j = j; a.ldo = c->ld;
     a.part = c->part; a.ldp = c->ld;
     a.far = farfield_enabled() ? 1 : 0;
+    a.coh = c->coh;
+    a.coh_blocks = ceil_div(c->n, 32);
     if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
-      e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec, c->st);
+      e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec, c->coh, c->st);
       if (e != cudaSuccess) return e;
       c->launches += 1;
       a.rec = c->rec;
@@ -383,10 +387,11 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   pc.u = u; pc.j = j; pc.ldo = c->ld;
   pc.ws = ws; pc.dj = dj;
   pc.status = c->status;
+  pc.coh = c->coh;
   if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
     if (!c->dry) {
       cudaError_t e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec,
-                                          c->st);
+                                          c->coh, c->st);
       if (e != cudaSuccess) return e;
       c->launches += 1;
     }
@@ -599,6 +604,9 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   c->raw = p; p += 12 * ld;   // raw ζ sums (12 rows for the α-derivative pass)
   cudaError_t e = cudaMemset(c->base, 0, rows * ld * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c->rec, 3 * ld * sizeof(float4));
+  // Until the first packing the particle order counts as coherent.
+  if (e == cudaSuccess) e = cudaMalloc(&c->coh, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(c->coh, 0xff, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c->status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(c->status, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->red, (size_t(kRedBlocks) + 1) * kDiagSlots * sizeof(double));
@@ -623,6 +631,7 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->part);
   cudaFree(c->ffv);
   cudaFree(c->rec);
+  cudaFree(c->coh);
   cudaFree(c->status);
   cudaFree(c->red);
   if (c->h_stage) cudaFreeHost(c->h_stage);

@@ -34,6 +34,7 @@ struct PairCall {
   // FP32 U/J passes: packed records of the ns sources (launch_pack_sources),
   // or null to read the FP64 rows in the kernel.  Bulk copies stage records.
   const float4* rec = nullptr;
+  const unsigned int* coh = nullptr;   // compact-block count (see PairArgs::coh)
   int* status = nullptr;
 };
 
@@ -118,6 +119,7 @@ struct vpm_ctx {
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
   float4* rec = nullptr;          // packed source records, 3 per particle (FP32 U/J passes)
+  unsigned int* coh = nullptr;    // compact 32-particle blocks at the last packing
   double* ffv = nullptr;          // bound particles (X3 Γ3 σ1) and M (6) rows, ffv_cap apart
   int64_t ffv_cap = 0;
   int64_t launches = 0;           // kernels enqueued (graph replays add their kernel count)

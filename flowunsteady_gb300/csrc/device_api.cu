@@ -57,7 +57,7 @@ extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const 
       if (part) cudaFreeAsync(part, st);
       return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate scratch");
     }
-    e = launch_pack_sources(kernel, ns, Xs, Gs, Ss, ld_s, 1.0, rec, st);
+    e = launch_pack_sources(kernel, ns, Xs, Gs, Ss, ld_s, 1.0, rec, nullptr, st);
     pc.rec = rec;
   }
   if (e == cudaSuccess)

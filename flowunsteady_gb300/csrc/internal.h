@@ -70,6 +70,11 @@ struct PairArgs {
   // Gaussian-erf FP32 passes: classify (warp, 32-source) blocks by their
   // bounding boxes and take the far-field forms (0 = always the general form).
   int32_t far;
+  // When non-null: the number of compact 32-particle source blocks (counted
+  // by the pack kernel); the classification runs only when at least a quarter
+  // of the coh_blocks blocks are compact (coherent particle order).
+  const unsigned int* coh;
+  int64_t coh_blocks;
   int* status;   // STATUS_TIMEOUT is OR-ed here if a copy wait gives up (may be null)
 };
 
@@ -102,10 +107,11 @@ bool pair_shape_supported(int precision, Shape shape);
 // when foff is null, else found from the device field table (foff[f] <= i,
 // fchunks[f]); targets whose count is 1 are skipped (already final).
 // Packed source records (3 float4 per source) of n particles for the FP32
-// U/J passes with kernel constants of σ·scale.
+// U/J passes with kernel constants of σ·scale.  Gaussian-erf: *compact (may
+// be null) is reset and then counts the compact 32-particle blocks.
 cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
                                 const double* S, int64_t ld, double scale, float4* rec,
-                                cudaStream_t st);
+                                unsigned int* compact, cudaStream_t st);
 cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,

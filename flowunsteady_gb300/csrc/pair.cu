@@ -32,32 +32,55 @@ cudaError_t launch_pair(int pass, int kernel, int precision, Shape s, const Pair
 // Packed source records of the FP32 U/J passes, per source
 //   (xh, yh, zh, a), (xl, yl, zl, b), (Γx, Γy, Γz, 0)
 // with x ≈ xh + xl (split_f32) and (a, b) the kernel constants of σ·scale.
+// Gaussian-erf: each warp (32 consecutive particles) also adds one to
+// *compact when its bounding box is compact against the far radius (diagonal
+// exponent argument >= kVoteSpan·kArgFar), the measure by which the pair
+// kernels decide whether the far-field classification can pay.
 template <int KERNEL>
 __global__ void __launch_bounds__(256) pack_sources_kernel(int64_t n, const double* __restrict__ X,
                                                            const double* __restrict__ G,
                                                            const double* __restrict__ S, int64_t ld,
-                                                           double scale, float4* __restrict__ rec) {
+                                                           double scale, float4* __restrict__ rec,
+                                                           unsigned int* compact) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float xh, xl, yh, yl, zh, zl, ka, kb;
-  split_f32(X[i], xh, xl);
-  split_f32(X[ld + i], yh, yl);
-  split_f32(X[2 * ld + i], zh, zl);
-  source_consts<KERNEL, float>(S[i] * scale, ka, kb);
-  rec[3 * i] = make_float4(xh, yh, zh, ka);
-  rec[3 * i + 1] = make_float4(xl, yl, zl, kb);
-  rec[3 * i + 2] = make_float4(float(G[i]), float(G[ld + i]), float(G[2 * ld + i]), 0.f);
+  const bool valid = i < n;
+  float xh = 0.f, xl, yh = 0.f, yl, zh = 0.f, zl, ka = -INFINITY, kb;
+  if (valid) {
+    split_f32(X[i], xh, xl);
+    split_f32(X[ld + i], yh, yl);
+    split_f32(X[2 * ld + i], zh, zl);
+    source_consts<KERNEL, float>(S[i] * scale, ka, kb);
+    rec[3 * i] = make_float4(xh, yh, zh, ka);
+    rec[3 * i + 1] = make_float4(xl, yl, zl, kb);
+    rec[3 * i + 2] = make_float4(float(G[i]), float(G[ld + i]), float(G[2 * ld + i]), 0.f);
+  }
+  if (KERNEL == VPM_KERNEL_GAUSSIANERF && compact) {
+    if (__all_sync(0xffffffffu, !valid)) return;
+    float4 box[2];
+    warp_source_box(xh, yh, zh, ka, valid, box);
+    if ((threadIdx.x & 31) == 0) {
+      const float ex = box[1].x - box[0].x, ey = box[1].y - box[0].y, ez = box[1].z - box[0].z;
+      const float span = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) * box[0].w;
+      if (span >= kVoteSpan * kArgFar) atomicAdd(compact, 1u);
+    }
+  }
 }
 
 cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
                                 const double* S, int64_t ld, double scale, float4* rec,
-                                cudaStream_t st) {
+                                unsigned int* compact, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int grid = int((n + 255) / 256);
+  if (compact) {
+    cudaError_t e = cudaMemsetAsync(compact, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+  }
   if (kernel == VPM_KERNEL_WINCKELMANS)
-    pack_sources_kernel<VPM_KERNEL_WINCKELMANS><<<grid, 256, 0, st>>>(n, X, G, S, ld, scale, rec);
+    pack_sources_kernel<VPM_KERNEL_WINCKELMANS><<<grid, 256, 0, st>>>(n, X, G, S, ld, scale, rec,
+                                                                      compact);
   else
-    pack_sources_kernel<VPM_KERNEL_GAUSSIANERF><<<grid, 256, 0, st>>>(n, X, G, S, ld, scale, rec);
+    pack_sources_kernel<VPM_KERNEL_GAUSSIANERF><<<grid, 256, 0, st>>>(n, X, G, S, ld, scale, rec,
+                                                                      compact);
   return cudaGetLastError();
 }
 

@@ -60,7 +60,7 @@ struct PairTraits {
 
 // Shared memory: source quads, then (FP32) the far-field boxes (per warp two
 // float4 for its staged sources and two for its targets), then (FP32C) the
-// fold pairs, then (bulk copies) the staging rows and the mbarrier.
+// fold pairs, then (bulk copies) the staging records and the mbarrier.
 template <int PASS, int PREC>
 __host__ __device__ constexpr size_t box_bytes(int block) {
   return PREC == VPM_PREC_FP64 ? 0 : size_t(block / 32) * 4 * 16;
@@ -133,20 +133,23 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   constexpr bool F32 = sizeof(R) == sizeof(float);
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // Source quads: A (x, a) and B (Γ, b) for BLOCK sources, then for ζ passes
+  // C (v_q) and for PASS_ZETAD D (w_q).
   Quad<R>* tileA = reinterpret_cast<Quad<R>*>(smem_raw);
   Quad<R>* tileB = tileA + BLOCK;
-  Quad<R>* tileC = tileB + BLOCK;  // ζ passes: v_q
-  Quad<R>* tileD = tileC + BLOCK;  // PASS_ZETAD: w_q
+  Quad<R>* tileC = tileB + BLOCK;
+  Quad<R>* tileD = tileC + BLOCK;
   constexpr size_t kQuadBytes = size_t(BLOCK) * Tr::kQuads * sizeof(Quad<R>);
   constexpr size_t kBoxBytes = box_bytes<PASS, PREC>(BLOCK);
-  // Far-field boxes of warp w: sources at sbox[2w..2w+1], targets at tbox[2w..2w+1].
+  // Far-field boxes of warp w: its staged sources at sbox[2w + 0..1], its
+  // targets at tbox[2w + 0..1].
   float4* sbox = reinterpret_cast<float4*>(smem_raw + kQuadBytes);
   float4* tbox = sbox + 2 * (BLOCK / 32);
   float* fold_hi = reinterpret_cast<float*>(smem_raw + kQuadBytes + kBoxBytes);
   float* fold_lo = fold_hi + size_t(BLOCK) * T * NV;
   // Bulk-copy staging: the records of BLOCK sources, then the mbarrier.
-  float4* stage = reinterpret_cast<float4*>(
-      smem_raw + kQuadBytes + kBoxBytes + (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
+  float4* stage = reinterpret_cast<float4*>(smem_raw + kQuadBytes + kBoxBytes +
+                                            (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
   uint64_t* bar = reinterpret_cast<uint64_t*>(stage + size_t(BLOCK) * 3);
   __shared__ int s_item;
 
@@ -159,7 +162,8 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   const bool use_tma = Tr::kTma && use_rec && a.tma != 0;
   // Gaussian-erf FP32 passes classify (warp, 32 sources) blocks by distance.
   constexpr bool kFarKernel = F32 && KERNEL == VPM_KERNEL_GAUSSIANERF;
-  const bool use_far = kFarKernel && a.far != 0;
+  const bool use_far =
+      kFarKernel && a.far != 0 && (!a.coh || 4 * uint64_t(*a.coh) >= uint64_t(a.coh_blocks));
   const int warp = tid >> 5;
   uint32_t phase = 0;
   if (use_tma) {
@@ -294,7 +298,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           if constexpr (kFarKernel) {
             if (use_far) warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
           }
-          __syncthreads();  // quads ready, staging rows consumed
+          __syncthreads();  // quads ready, staging records consumed
           if (tid == 0 && tile0 + BLOCK < s1) issue(tile0 + BLOCK, s1);
         }
       }
@@ -362,15 +366,23 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 #pragma unroll 2
             for (int js = 0; js < cnt; ++js) uj_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
           } else {
-            // Gaussian-erf in blocks of 32 sources: far blocks skip erfcx/exp.
-            for (int u = 0; u < cnt; u += 32) {
-              const int ue = min(u + 32, cnt);
-              if (use_far && box_arg_bound(tbox + 2 * warp, sbox + (u >> 4)) <= kArgFar) {
+            // Gaussian-erf by runs of 32-source blocks of one class: far blocks
+            // skip erfcx/exp, vote blocks decide per source.
+            const uint32_t cls = classify_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt,
+                                                             kVoteSpan * kArgFar, use_far);
+            auto key = [](uint32_t c) { return c >= 2u ? 2u : c; };
+            for (int js = 0; js < cnt;) {
+              const int je = block_run_end(cls, js, cnt, key);
+              const uint32_t c = key((cls >> (2 * (js >> 5))) & 3u);
+              if (c == 2u) {
 #pragma unroll 2
-                for (int js = u; js < ue; ++js) uj_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+                for (; js < je; ++js) uj_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+              } else if (c == 1u) {
+#pragma unroll 2
+                for (; js < je; ++js) uj_source_gauss<T, true>(ta[js], tb[js], tx, ty, tz, acc);
               } else {
 #pragma unroll 2
-                for (int js = u; js < ue; ++js) uj_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc, use_far);
+                for (; js < je; ++js) uj_source_gauss<T, false>(ta[js], tb[js], tx, ty, tz, acc);
               }
             }
           }
@@ -382,15 +394,20 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           } else {
             // Gaussian-erf: where Dq and Dp vanish only the plain sums take the
             // pair; far blocks skip erfcx.
-            for (int u = 0; u < cnt; u += 32) {
-              const int ue = min(u + 32, cnt);
-              const float bound = use_far ? box_arg_bound(tbox + 2 * warp, sbox + (u >> 4)) : 0.f;
-              if (bound <= kArgZero) {
-                for (int js = u; js < ue; ++js) uj_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
-              } else if (bound <= kArgFar) {
-                for (int js = u; js < ue; ++js) ujd_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+            const uint32_t cls = classify_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt,
+                                                             kVoteSpan * kArgFar, use_far);
+            auto key = [](uint32_t c) { return c; };
+            for (int js = 0; js < cnt;) {
+              const int je = block_run_end(cls, js, cnt, key);
+              const uint32_t c = (cls >> (2 * (js >> 5))) & 3u;
+              if (c == 3u) {
+                for (; js < je; ++js) uj_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+              } else if (c == 2u) {
+                for (; js < je; ++js) ujd_source_gauss_far<T>(ta[js], tb[js], tx, ty, tz, acc);
+              } else if (c == 1u) {
+                for (; js < je; ++js) ujd_source_gauss<T, true>(ta[js], tb[js], tx, ty, tz, acc);
               } else {
-                for (int js = u; js < ue; ++js) ujd_source_gauss<T>(ta[js], tb[js], tx, ty, tz, acc, use_far);
+                for (; js < je; ++js) ujd_source_gauss<T, false>(ta[js], tb[js], tx, ty, tz, acc);
               }
             }
           }
@@ -437,27 +454,38 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         if (kFarKernel && use_far) {
           // Gaussian-erf: blocks of 32 sources whose ζ is exactly zero at every
           // target of the warp are skipped.
-          for (int u = 0; u < cnt; u += 32) {
-            if (box_arg_bound(tbox + 2 * warp, sbox + (u >> 4)) <= kArgZero) continue;
-            const int ue = min(u + 32, cnt);
-            if (!own) {
+          // Runs of 32-source blocks: zero blocks are skipped, far and vote
+          // blocks decide per source (outside the CTA's own tiles).
+          const uint32_t cls = classify_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt,
+                                                           kVoteSpan * kArgZero, true);
+          auto key = [](uint32_t c) { return c == 3u ? 3u : (c >= 1u ? 1u : 0u); };
+          for (int js = 0; js < cnt;) {
+            const int je = block_run_end(cls, js, cnt, key);
+            const uint32_t c = key((cls >> (2 * (js >> 5))) & 3u);
+            if (c == 3u) {
+              js = je;
+            } else if (!own && c == 1u) {
 #pragma unroll 2
-              for (int js = u; js < ue; ++js)
-                zeta_source<KERNEL, T, false, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
+              for (; js < je; ++js)
+                zeta_source<KERNEL, T, false, DD, true>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+            } else if (!own) {
+#pragma unroll 2
+              for (; js < je; ++js)
+                zeta_source<KERNEL, T, false, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
             } else {
 #pragma unroll 2
-              for (int js = u; js < ue; ++js)
-                zeta_source<KERNEL, T, true, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
+              for (; js < je; ++js)
+                zeta_source<KERNEL, T, true, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
             }
           }
         } else if (!own) {
 #pragma unroll 2
           for (int js = 0; js < cnt; ++js)
-            zeta_source<KERNEL, T, false, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
+            zeta_source<KERNEL, T, false, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
         } else {
 #pragma unroll 2
           for (int js = 0; js < cnt; ++js)
-            zeta_source<KERNEL, T, true, DD>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc, use_far);
+            zeta_source<KERNEL, T, true, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
         }
       } else {
         // ζ passes, FP64.

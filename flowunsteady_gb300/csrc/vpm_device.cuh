@@ -199,10 +199,16 @@ __host__ __device__ inline void split_f32(double x, float& h, float& l) {
   l = float(x - double(h));
 }
 
-// Position relative to a reference point, both in (h, l) form: (h - ch) + (l - cl)
-// in FP32, within one rounding of the exact difference when h and ch are close.
+// Position relative to a reference point, both in (h, l) form.  h - ch is
+// taken exactly as s + e (Knuth's TwoSum), then s + (e + (l - cl)) is rounded
+// once more: the result is the float nearest (h + l) - (ch + cl) except in
+// rare double-rounding ties, as if the FP64 difference were rounded to FP32.
 __device__ __forceinline__ float rel_f32(float h, float l, float ch, float cl) {
-  return __fadd_rn(__fadd_rn(h, -ch), __fadd_rn(l, -cl));
+  const float s = __fadd_rn(h, -ch);
+  const float bp = __fadd_rn(s, -h);
+  const float ap = __fadd_rn(s, -bp);
+  const float e = __fadd_rn(__fadd_rn(h, -ap), __fadd_rn(-ch, -bp));
+  return __fadd_rn(s, __fadd_rn(e, __fadd_rn(l, -cl)));
 }
 
 // Knuth's TwoSum: s + e == a + b exactly (round-to-nearest, no reassociation).
@@ -309,52 +315,73 @@ constexpr float kArgFar = float(-0.5 * kLog2e * 50.0);
 constexpr float kArgZero = -128.f;
 
 // Gaussian-erf: source quads (x, y, z, -log2(e)/(2σ²)) and (Γx, Γy, Γz, 1/σ).
-// A warp vote per source takes the far form (q = 1/r³, p = -3/r⁵; see the
-// far-field notes below) when every pair of the warp has ρ² >= 50; otherwise
-// all T targets take the erf-free form, and a second vote sends the rare warps
-// holding a pair with ρ² < 3/2 (or the self pair) through the series.
-template <int T>
+// All T targets take the erf-free form, and a warp vote sends the rare warps
+// holding a pair with ρ² < 3/2 (or the self pair) through the series.  With
+// VOTE, a first warp vote takes the far form (q = 1/r³, p = -3/r⁵; see the
+// far-field notes below) when every pair of the warp has ρ² >= 50; the caller
+// uses it only for warps whose targets are compact enough for the vote to pay
+// (it splits the straight-line code that overlaps the exp/rcp latencies).
+template <int T, bool VOTE>
 __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb,
                                                 const float (&tx)[T], const float (&ty)[T],
-                                                const float (&tz)[T], float (&acc)[T][15],
-                                                bool far) {
+                                                const float (&tz)[T], float (&acc)[T][15]) {
   const float ea = sa.w, is1 = sb.w;
-  float dx[T], dy[T], dz[T], r2[T], arg[T], q[T], p[T];
-  float amax = -INFINITY;
-#pragma unroll
-  for (int k = 0; k < T; ++k) {
-    dx[k] = tx[k] - sa.x;
-    dy[k] = ty[k] - sa.y;
-    dz[k] = tz[k] - sa.z;
-    r2[k] = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
-    arg[k] = r2[k] * ea;
-    amax = fmaxf(amax, arg[k]);
-  }
-  if (far && __all_sync(0xffffffffu, amax <= kArgFar)) {
-#pragma unroll
-    for (int k = 0; k < T; ++k) {
-      const float ri = rsqrt_ftz(r2[k]);
-      const float ri2 = ri * ri;
-      q[k] = ri2 * ri;
-      p[k] = (-3.f * q[k]) * ri2;
-      accum_pair(dx[k], dy[k], dz[k], q[k], p[k], sb.x, sb.y, sb.z, acc[k]);
-    }
-    return;
-  }
   const float kt = kErfcxP * is1;                      // t = 1/(1 + kt r)
   const float kc = float(kSqrt2overPi) * is1;          // √(2/π) ρ = kc r
   const float k3 = float(kSqrt2overPi) * is1 * is1 * is1;
+  float dx[T], dy[T], dz[T], arg[T], q[T], p[T];
+  float amax = -INFINITY;
+  if constexpr (VOTE) {
+    float r2[T], ri[T];
 #pragma unroll
-  for (int k = 0; k < T; ++k) {
-    const float ri = rsqrt_ftz(r2[k]);
-    const float r = r2[k] * ri;
-    const float e = ex2_ftz(arg[k]);
-    const float t = rcp_ftz(fmaf(kt, r, 1.f));
-    const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
-    const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
-    const float ri2 = ri * ri;
-    q[k] = g * (ri2 * ri);
-    p[k] = fmaf(-3.f, q[k], k3 * e) * ri2;
+    for (int k = 0; k < T; ++k) {
+      dx[k] = tx[k] - sa.x;
+      dy[k] = ty[k] - sa.y;
+      dz[k] = tz[k] - sa.z;
+      r2[k] = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
+      arg[k] = r2[k] * ea;
+      amax = fmaxf(amax, arg[k]);
+      ri[k] = rsqrt_ftz(r2[k]);
+    }
+    if (__all_sync(0xffffffffu, amax <= kArgFar)) {
+#pragma unroll
+      for (int k = 0; k < T; ++k) {
+        const float ri2 = ri[k] * ri[k];
+        const float qq = ri2 * ri[k];
+        accum_pair(dx[k], dy[k], dz[k], qq, (-3.f * qq) * ri2, sb.x, sb.y, sb.z, acc[k]);
+      }
+      return;
+    }
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      const float r = r2[k] * ri[k];
+      const float e = ex2_ftz(arg[k]);
+      const float t = rcp_ftz(fmaf(kt, r, 1.f));
+      const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
+      const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
+      const float ri2 = ri[k] * ri[k];
+      q[k] = g * (ri2 * ri[k]);
+      p[k] = fmaf(-3.f, q[k], k3 * e) * ri2;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      dx[k] = tx[k] - sa.x;
+      dy[k] = ty[k] - sa.y;
+      dz[k] = tz[k] - sa.z;
+      const float r2 = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
+      arg[k] = r2 * ea;
+      amax = fmaxf(amax, arg[k]);
+      const float ri = rsqrt_ftz(r2);
+      const float r = r2 * ri;
+      const float e = ex2_ftz(arg[k]);
+      const float t = rcp_ftz(fmaf(kt, r, 1.f));
+      const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
+      const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
+      const float ri2 = ri * ri;
+      q[k] = g * (ri2 * ri);
+      p[k] = fmaf(-3.f, q[k], k3 * e) * ri2;
+    }
   }
   if (__any_sync(0xffffffffu, amax > kArgSeries)) {
     const float is2 = is1 * is1, is3 = is2 * is1, is5 = is3 * is2;
@@ -421,7 +448,7 @@ __device__ __forceinline__ void warp_box_reduce(float& lx, float& ly, float& lz,
   }
 }
 
-// Box of the T·32 targets of a warp, stored as (lo, 0), (hi, 0) at box[0..1].
+// Box of the T·32 targets of a warp, stored as (lo, extent²), (hi, 0) at box[0..1].
 template <int T>
 __device__ __forceinline__ void warp_target_box(const float (&tx)[T], const float (&ty)[T],
                                                 const float (&tz)[T], float4* box) {
@@ -433,7 +460,8 @@ __device__ __forceinline__ void warp_target_box(const float (&tx)[T], const floa
   }
   warp_box_reduce(lx, ly, lz, hx, hy, hz);
   if ((threadIdx.x & 31) == 0) {
-    box[0] = make_float4(lx, ly, lz, 0.f);
+    const float ex = hx - lx, ey = hy - ly, ez = hz - lz;
+    box[0] = make_float4(lx, ly, lz, fmaf(ex, ex, fmaf(ey, ey, ez * ez)));
     box[1] = make_float4(hx, hy, hz, 0.f);
   }
 }
@@ -455,13 +483,55 @@ __device__ __forceinline__ void warp_source_box(float x, float y, float z, float
 }
 
 // Upper bound of the exponent argument over all pairs of a target box and a
-// source box (both read from shared memory; the result is warp-uniform).
-__device__ __forceinline__ float box_arg_bound(const float4* tbox, const float4* sbox) {
+// source box (both read from shared memory; the result is warp-uniform), and
+// the exponent argument of the target box's own extent (its diagonal at the
+// block's widest core): per-source votes pay only when this is a few times
+// the vote's threshold at most.
+__device__ __forceinline__ float box_arg_bound(const float4* tbox, const float4* sbox,
+                                               float& span) {
   const float4 tl = tbox[0], th = tbox[1], sl = sbox[0], sh = sbox[1];
   const float gx = fmaxf(0.f, fmaxf(sl.x - th.x, tl.x - sh.x));
   const float gy = fmaxf(0.f, fmaxf(sl.y - th.y, tl.y - sh.y));
   const float gz = fmaxf(0.f, fmaxf(sl.z - th.z, tl.z - sh.z));
+  span = tl.w * sl.w;
   return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) * sl.w;
+}
+
+// Per-source votes are used where the target box's extent argument is above
+// kVoteSpan times the vote's threshold (both negative).
+constexpr float kVoteSpan = 4.f;
+
+// Classes of the 32-source blocks of a staged tile for one warp, 2 bits per
+// block (NB <= 16 blocks): 3 where every pair has arg <= kArgZero, 2 where
+// every pair has arg <= kArgFar, 1 where per-source votes pay (the target
+// box's extent argument is >= vote_span), 0 otherwise.  0 for every block
+// when the far field is off.
+template <int NB>
+__device__ __forceinline__ uint32_t classify_blocks(const float4* tbox, const float4* sbox,
+                                                    int cnt, float vote_span, bool on) {
+  uint32_t cls = 0;
+  if (!on) return cls;
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    if (b * 32 < cnt) {
+      float span;
+      const float bound = box_arg_bound(tbox, sbox + 2 * b, span);
+      const uint32_t c = bound <= kArgZero ? 3u : bound <= kArgFar ? 2u : (span >= vote_span ? 1u : 0u);
+      cls |= c << (2 * b);
+    }
+  }
+  return cls;
+}
+
+// End (exclusive, in sources) of the run of blocks that starts at source js and
+// shares the class `key(block class)` of its first block.
+template <typename Key>
+__device__ __forceinline__ int block_run_end(uint32_t cls, int js, int cnt, Key key) {
+  const int b0 = js >> 5;
+  const uint32_t k0 = key((cls >> (2 * b0)) & 3u);
+  int b = b0 + 1;
+  while (b * 32 < cnt && key((cls >> (2 * b)) & 3u) == k0) ++b;
+  return min(b * 32, cnt);
 }
 
 }  // namespace vpm
@@ -537,15 +607,18 @@ __device__ __forceinline__ void ujd_source_winck(const float4 sa, const float4 s
   }
 }
 
-template <int T>
+// ujd_source_gauss: uj_source_gauss plus Dq, Dp.  With VOTE, per-source far
+// forms as in uj_source_gauss (and only the plain sums where Dq = Dp = 0).
+template <int T, bool VOTE>
 __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 sb,
                                                  const float (&tx)[T], const float (&ty)[T],
-                                                 const float (&tz)[T], float (&acc)[T][27],
-                                                 bool far) {
+                                                 const float (&tz)[T], float (&acc)[T][27]) {
   const float ea = sa.w, is1 = sb.w;
   const float is2 = is1 * is1;
   const float k3 = float(kSqrt2overPi) * is2 * is1;
-  float dx[T], dy[T], dz[T], r2[T], arg[T], q[T], p[T], dq[T], dp[T];
+  const float kt = kErfcxP * is1;
+  const float kc = float(kSqrt2overPi) * is1;
+  float dx[T], dy[T], dz[T], r2[T], ri[T], arg[T], q[T], p[T], dq[T], dp[T];
   float amax = -INFINITY;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
@@ -555,15 +628,14 @@ __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 s
     r2[k] = fmaf(dx[k], dx[k], fmaf(dy[k], dy[k], dz[k] * dz[k]));
     arg[k] = r2[k] * ea;
     amax = fmaxf(amax, arg[k]);
+    ri[k] = rsqrt_ftz(r2[k]);
   }
-  // Per-source far forms, as in uj_source_gauss (Dq = Dp = 0 below kArgZero).
-  if (far && __all_sync(0xffffffffu, amax <= kArgFar)) {
+  if (VOTE && __all_sync(0xffffffffu, amax <= kArgFar)) {
     const bool zero = __all_sync(0xffffffffu, amax <= kArgZero);
 #pragma unroll
     for (int k = 0; k < T; ++k) {
-      const float ri = rsqrt_ftz(r2[k]);
-      const float ri2 = ri * ri;
-      const float qq = ri2 * ri;
+      const float ri2 = ri[k] * ri[k];
+      const float qq = ri2 * ri[k];
       const float pp = (-3.f * qq) * ri2;
       if (zero) {
         accum_pair(dx[k], dy[k], dz[k], qq, pp, sb.x, sb.y, sb.z, acc[k]);
@@ -574,19 +646,16 @@ __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 s
     }
     return;
   }
-  const float kt = kErfcxP * is1;
-  const float kc = float(kSqrt2overPi) * is1;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
-    const float ri = rsqrt_ftz(r2[k]);
-    const float r = r2[k] * ri;
+    const float r = r2[k] * ri[k];
     const float e = ex2_ftz(arg[k]);
     const float t = rcp_ftz(fmaf(kt, r, 1.f));
     const float f = t * fmaf(t, fmaf(t, fmaf(t, kErfcxA4, kErfcxA3), kErfcxA2), kErfcxA1);
     const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
-    const float ri2 = ri * ri;
+    const float ri2 = ri[k] * ri[k];
     const float k3e = k3 * e;
-    q[k] = g * (ri2 * ri);
+    q[k] = g * (ri2 * ri[k]);
     p[k] = fmaf(-3.f, q[k], k3e) * ri2;
     dq[k] = -k3e;
     dp[k] = k3e * is2;
@@ -781,22 +850,24 @@ __device__ inline void zeta_consts_f32(double sig, float& a, float& b, float& c)
   }
 }
 
-template <int KERNEL, int T, bool MASK, bool D>
+// ζ sums of one source against T targets.  With VOTE (Gaussian-erf only), a
+// warp vote skips a source whose ζ underflows to +0 at every target.
+template <int KERNEL, int T, bool MASK, bool D, bool VOTE>
 __device__ __forceinline__ void zeta_source(const float4 sa, const float4 sb, const float4 sc,
                                             const float4 sd, const float (&tx)[T],
                                             const float (&ty)[T], const float (&tz)[T],
-                                            float (&acc)[T][D ? 12 : 6], bool far) {
+                                            float (&acc)[T][D ? 12 : 6]) {
   float r2[T];
   float amax = -INFINITY;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
     const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
     r2[k] = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (KERNEL != VPM_KERNEL_WINCKELMANS) amax = fmaxf(amax, r2[k] * sa.w);
+    if (VOTE) amax = fmaxf(amax, r2[k] * sa.w);
   }
   // Gaussian-erf: a source whose ζ underflows to +0 at every target of the
   // warp (exponent argument <= kArgZero) adds nothing.
-  if (KERNEL != VPM_KERNEL_WINCKELMANS && far && __all_sync(0xffffffffu, amax <= kArgZero)) return;
+  if (VOTE && KERNEL != VPM_KERNEL_WINCKELMANS && __all_sync(0xffffffffu, amax <= kArgZero)) return;
 #pragma unroll
   for (int k = 0; k < T; ++k) {
     float z, dzz = 0.f;
