@@ -45,7 +45,10 @@ BYTES_D2H = 96          # U (3) and J (9) per particle (FP64)
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one pair-kernel launch of the default workload,
 # from an ncu capture (profiles/launches_bench_helical_n262144.md).
-PAIR_KERNEL_TRAFFIC = {262144: 25233408 + 194519296}
+# DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch at the tuned
+# 256x2 shape, from an ncu capture of the benchmark workload; the writes are
+# mostly the FP64 partial sums of the source chunks, so other shapes differ.
+PAIR_KERNEL_TRAFFIC = {262144: 29289728 + 162531584}
 
 
 def parse():
