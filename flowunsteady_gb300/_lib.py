@@ -52,7 +52,8 @@ EXPORTS = [
     "vpm_ctx_set_stream", "vpm_get_time", "vpm_set_time", "vpm_set_particles", "vpm_append",
     "vpm_truncate", "vpm_get_np", "vpm_get_state", "vpm_get_sfs", "vpm_eval_UJ",
     "vpm_eval_UJ_targets", "vpm_get_UJ", "vpm_eval_sfs", "vpm_step", "vpm_diagnostics",
-    "vpm_centroids", "vpm_ffv_direct", "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
+    "vpm_centroids", "vpm_ffv_direct", "vpm_fmm_default", "vpm_eval_UJ_fmm", "vpm_fmm_stats",
+    "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
     "vpm_batch_last_error", "vpm_batch_set_stream", "vpm_batch_set_field",
     "vpm_batch_get_field", "vpm_batch_eval_UJ", "vpm_batch_get_UJ", "vpm_batch_step",
     "vpm_autotune", "vpm_set_tile", "vpm_measure_fma_peaks", "vpm_debug_fail_after",
@@ -87,6 +88,18 @@ class Scheme(ctypes.Structure):
 class Tile(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("tpt", ctypes.c_int32), ("chunk", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]
+
+
+class Fmm(ctypes.Structure):
+    """Mirror of struct vpm_fmm (treecode settings)."""
+    _fields_ = [("p", ctypes.c_int32), ("ncrit", ctypes.c_int32), ("theta", ctypes.c_double),
+                ("sigma_factor", ctypes.c_double)]
+
+
+def default_fmm():
+    f = Fmm()
+    lib().vpm_fmm_default(ctypes.byref(f))
+    return f
 
 
 class VPMError(RuntimeError):
@@ -124,6 +137,9 @@ def _declare(lib):
         "vpm_step": (ctypes.c_int, [_vp, ctypes.c_double, P(Scheme), _i64, ctypes.c_int]),
         "vpm_diagnostics": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
         "vpm_centroids": (ctypes.c_int, [_vp, ctypes.c_int, P(_i64), P(_i64), _dp]),
+        "vpm_fmm_default": (None, [P(Fmm)]),
+        "vpm_eval_UJ_fmm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Fmm)]),
+        "vpm_fmm_stats": (ctypes.c_int, [_vp, P(_i64), P(_i64), P(_i64), P(_i64)]),
         "vpm_ffv_direct": (ctypes.c_int, [_vp, ctypes.c_int, _i64, _dp, _i64, _dp, _i64, _dp, _i64,
                                           _dp, _i64]),
         "vpm_uj_device_async": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,

@@ -632,6 +632,7 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->ffv);
   cudaFree(c->rec);
   cudaFree(c->coh);
+  vpm::fmm_free(c->fmm);
   cudaFree(c->status);
   cudaFree(c->red);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -763,6 +764,42 @@ int vpm_eval_UJ_targets(vpm_ctx* c, int kernel, int precision, int64_t t0, int64
 int vpm_eval_UJ(vpm_ctx* c, int kernel, int precision) {
   if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
   return vpm_eval_UJ_targets(c, kernel, precision, 0, c->n);
+}
+
+void vpm_fmm_default(vpm_fmm* f) {
+  if (!f) return;
+  f->p = 4;
+  f->ncrit = 50;
+  f->theta = 0.4;
+  f->sigma_factor = 7.1;
+}
+
+int vpm_eval_UJ_fmm(vpm_ctx* c, int kernel, int precision, const vpm_fmm* f) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (!f) return ctx_fail(c, VPM_ERR_INVALID, "null treecode settings");
+  if (!valid_kernel(kernel) || !valid_prec(precision))
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown kernel or precision");
+  if (!fmm_order_supported(f->p)) return ctx_fail(c, VPM_ERR_UNSUPPORTED, "expansion order not compiled (2, 4, 6)");
+  if (f->ncrit < 1 || !(f->theta > 0.0 && f->theta < 1.0) || !(f->sigma_factor >= 0.0))
+    return ctx_fail(c, VPM_ERR_INVALID, "treecode settings out of range");
+  int rc = check_inject(c);
+  if (rc) return rc;
+  DeviceGuard dg(c->device);
+  const char* why = nullptr;
+  cudaError_t e = fmm_eval(c, kernel, precision, f->p, f->ncrit, f->theta, f->sigma_factor, &why);
+  if (e == cudaErrorInvalidValue && why) return ctx_fail(c, VPM_ERR_CUDA, why);
+  if (e != cudaSuccess)
+    return cuda_fail(c, e, why ? (std::string("treecode evaluation, ") + why).c_str() : "treecode evaluation");
+  c->uj_lo = 0;
+  c->uj_hi = c->n;
+  return VPM_OK;
+}
+
+int vpm_fmm_stats(const vpm_ctx* c, int64_t* cells, int64_t* leaves, int64_t* far_entries,
+                  int64_t* near_entries) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  fmm_stats(c->fmm, cells, leaves, far_entries, near_entries);
+  return VPM_OK;
 }
 
 int vpm_get_UJ(vpm_ctx* c, int64_t i0, int64_t n, double* U, int64_t su, double* J, int64_t sj) {

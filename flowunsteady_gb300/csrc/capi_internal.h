@@ -92,6 +92,16 @@ struct BatchPlan {
 
 }  // namespace vpm
 
+namespace vpm {
+struct FmmWork;
+void fmm_free(FmmWork* w);
+bool fmm_order_supported(int p);
+cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
+                     double sfac, const char** why);
+void fmm_stats(const FmmWork* w, int64_t* cells, int64_t* leaves, int64_t* far_entries,
+               int64_t* near_entries);
+}  // namespace vpm
+
 struct vpm_ctx {
   int device = 0;
   int num_sms = 0;
@@ -118,6 +128,7 @@ struct vpm_ctx {
   int64_t fail_after = 0;
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
+  vpm::FmmWork* fmm = nullptr;    // treecode workspace (allocated on first use)
   float4* rec = nullptr;          // packed source records, 3 per particle (FP32 U/J passes)
   unsigned int* coh = nullptr;    // compact 32-particle blocks at the last packing
   double* ffv = nullptr;          // bound particles (X3 Γ3 σ1) and M (6) rows, ffv_cap apart

@@ -1,0 +1,900 @@
+// tree.cu — GPU treecode for U and ∇U (the role of FLOWVPM's UJ_fmm with
+// vpm.FMM(p, ncrit, theta), src/FLOWUnsteady_simulation.jl:38,43).
+//
+// One evaluation runs entirely on the device, in this order:
+//   1. bounding cube and 63-bit Morton codes of the particles; radix sort of
+//      (code, index) pairs; gather of the state into Morton order and the
+//      packed FP32 source records of that order;
+//   2. octree built generation by generation: a cell with more than ncrit
+//      particles whose codes differ is split at the first 3-bit Morton digit
+//      where they differ (so no single-child chains), children are appended
+//      with an atomic counter; cells are contiguous ranges of sorted particles;
+//   3. upward pass, deepest generation first: leaves take their bounding box,
+//      largest core and moments (order P) from their particles, parents from
+//      their children (box union; moments shifted to the parent centre);
+//   4. one thread per target leaf walks the tree: a cell s is far for leaf t
+//      when (R_t + R_s) < θ·d and d - R_t - R_s >= sigma_factor·σmax_s
+//      (d = distance of the centres), then it is evaluated from its moments;
+//      otherwise its leaves are summed directly (two passes: count, fill);
+//   5. the direct near field: one CTA per target leaf over its near leaves,
+//      with the regularised kernels of the direct sum (FP32 pair routines on
+//      positions relative to the leaf's first particle, or FP64);
+//   6. the far field: one thread per target over the far cells of its leaf
+//      (tree.cuh), added to the near field; results go to the original order.
+// The far field uses the singular kernel, as FLOWVPM's nonzero_sigma=false;
+// sigma_factor keeps regularised pairs out of it (Gaussian-erf: beyond 7.1 σ
+// the kernels agree to FP32 rounding).
+#include <cuda_runtime.h>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "capi_internal.h"
+#include "tree.cuh"
+#include "vpm_device.cuh"
+
+namespace vpm {
+
+constexpr int kMaxGen = 23;        // root + at most 21 Morton digits (+1 spare)
+constexpr int kStack = 256;        // traversal stack (cells)
+constexpr int kTreeBlock = 64;     // threads of the near/far evaluation CTAs
+
+// ------------------------------------------------------------- workspace --
+struct FmmWork {
+  int64_t cap = 0;            // particles
+  int64_t cell_cap = 0;       // cells (2·cap + 8 bounds any octree of cap points)
+  int64_t mom_cells = 0;      // cells the moment buffers hold
+  int mom_p = -1;
+  int64_t list_cap = 0;       // interaction list entries
+  // particles in Morton order
+  uint64_t *codes = nullptr, *codes_alt = nullptr;
+  int *idx = nullptr, *perm = nullptr;
+  double* sorted = nullptr;   // X 3, Γ 3, σ 1 rows of length cap
+  float4* rec = nullptr;      // packed FP32 source records of the sorted particles
+  double* near_raw = nullptr; // 15 raw near-field sums per sorted particle
+  // cells
+  int *lo = nullptr, *hi = nullptr, *child = nullptr, *nchild = nullptr;
+  double* geom = nullptr;     // per cell: box min x y z, box max x y z, σmax, unused
+  double* mom = nullptr;      // per cell: 3·ncoef(P) FP64 moments
+  float* momf = nullptr;      // FP32 copy
+  int* leaves = nullptr;      // leaf cell ids
+  int* counters = nullptr;    // [0] cells, [1] leaves, [2] overflow, [3..3+kMaxGen] generation starts
+  double* box = nullptr;      // bounding cube: min x y z, size
+  double* box_part = nullptr; // per-block min/max partials
+  // interaction lists
+  int *nfar = nullptr, *nnear = nullptr, *ofar = nullptr, *onear = nullptr;
+  int *far_list = nullptr, *near_list = nullptr;
+  void* cub_tmp = nullptr;
+  size_t cub_bytes = 0;
+  int h_counters[3 + kMaxGen + 1];
+  // statistics of the last evaluation
+  int64_t last_cells = 0, last_leaves = 0, last_far = 0, last_near = 0;
+};
+
+void fmm_free(FmmWork* w) {
+  if (!w) return;
+  void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
+                  w->lo, w->hi, w->child, w->nchild, w->geom, w->mom, w->momf, w->leaves,
+                  w->counters, w->box, w->box_part, w->nfar, w->nnear, w->ofar, w->onear,
+                  w->far_list, w->near_list, w->cub_tmp};
+  for (void* p : ptrs) cudaFree(p);
+  delete w;
+}
+
+// ------------------------------------------------------ bounding cube, codes --
+constexpr int kBoxBlocks = 256;
+
+__global__ void box_partial_kernel(int64_t n, const double* __restrict__ X, int64_t ld,
+                                   double* part) {
+  __shared__ double s[6][256];
+  double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double x = X[d * ld + i];
+      v[d] = fmin(v[d], x);
+      v[3 + d] = fmax(v[3 + d], x);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 6; ++d) s[d][threadIdx.x] = v[d];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        s[d][threadIdx.x] = fmin(s[d][threadIdx.x], s[d][threadIdx.x + o]);
+        s[3 + d][threadIdx.x] = fmax(s[3 + d][threadIdx.x], s[3 + d][threadIdx.x + o]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int d = 0; d < 6; ++d) part[blockIdx.x * 6 + d] = s[d][0];
+}
+
+__global__ void box_final_kernel(const double* part, int nblocks, double* box) {
+  double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int b = 0; b < nblocks; ++b)
+    for (int d = 0; d < 3; ++d) {
+      v[d] = fmin(v[d], part[b * 6 + d]);
+      v[3 + d] = fmax(v[3 + d], part[b * 6 + 3 + d]);
+    }
+  const double size = fmax(fmax(v[3] - v[0], v[4] - v[1]), v[5] - v[2]);
+  box[0] = v[0];
+  box[1] = v[1];
+  box[2] = v[2];
+  box[3] = size > 0 ? size * (1.0 + 1e-9) : 1.0;
+}
+
+// Spread the low 21 bits of v to every third bit (Morton interleaving).
+__device__ __forceinline__ uint64_t spread3(uint64_t x) {
+  x &= 0x1fffffull;
+  x = (x | x << 32) & 0x1f00000000ffffull;
+  x = (x | x << 16) & 0x1f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+
+__global__ void morton_kernel(int64_t n, const double* __restrict__ X, int64_t ld,
+                              const double* __restrict__ box, uint64_t* codes, int* idx) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double scale = double(1 << 21) / box[3];
+  uint64_t q[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double t = floor((X[d * ld + i] - box[d]) * scale);
+    q[d] = uint64_t(fmin(fmax(t, 0.0), double((1 << 21) - 1)));
+  }
+  codes[i] = spread3(q[0]) << 2 | spread3(q[1]) << 1 | spread3(q[2]);
+  idx[i] = int(i);
+}
+
+// Sorted FP64 state (X 3, Γ 3, σ 1 rows of length ldw) in Morton order.
+__global__ void gather_kernel(int64_t n, const int* __restrict__ perm, const double* __restrict__ X,
+                              const double* __restrict__ G, const double* __restrict__ S,
+                              int64_t ld, double* sorted, int64_t ldw) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t j = perm[i];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    sorted[d * ldw + i] = X[d * ld + j];
+    sorted[(3 + d) * ldw + i] = G[d * ld + j];
+  }
+  sorted[6 * ldw + i] = S[j];
+}
+
+// ------------------------------------------------------------- tree build --
+__global__ void tree_init_kernel(int64_t n, int* lo, int* hi, int* counters) {
+  lo[0] = 0;
+  hi[0] = int(n);
+  counters[0] = 1;   // cells
+  counters[1] = 0;   // leaves
+  counters[2] = 0;   // overflow
+  counters[3] = 0;   // generation 0 starts at cell 0
+  counters[4] = 1;   // generation 1 starts at cell 1
+}
+
+__device__ __forceinline__ int lower_bound_code(const uint64_t* codes, int lo, int hi,
+                                                uint64_t key) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (codes[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Split or close the cells of generation g: [counters[3+g], counters[4+g]).
+__global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint64_t* __restrict__ codes,
+                                  int* lo, int* hi, int* child, int* nchild, int* leaves,
+                                  int* counters) {
+  const int begin = counters[3 + g], end = counters[4 + g];
+  for (int cell = begin + int(blockIdx.x * blockDim.x + threadIdx.x); cell < end;
+       cell += int(gridDim.x * blockDim.x)) {
+    const int a = lo[cell], b = hi[cell];
+    const uint64_t first = codes[a], last = codes[b - 1];
+    if (b - a <= ncrit || first == last) {
+      child[cell] = -1;
+      nchild[cell] = 0;
+      leaves[atomicAdd(&counters[1], 1)] = cell;
+      continue;
+    }
+    const int bit = 63 - __clzll((long long)(first ^ last));   // highest differing bit
+    const int shift = (bit / 3) * 3;                            // its Morton digit
+    const uint64_t prefix = first & ~((uint64_t(8) << shift) - 1);
+    int bounds[9];
+    bounds[0] = a;
+    bounds[8] = b;
+    for (int v = 1; v < 8; ++v) bounds[v] = lower_bound_code(codes, a, b, prefix | (uint64_t(v) << shift));
+    int nc = 0;
+    for (int v = 0; v < 8; ++v) nc += bounds[v + 1] > bounds[v];
+    const int first_child = atomicAdd(&counters[0], nc);
+    if (first_child + nc > cell_cap) {
+      atomicOr(&counters[2], 1);
+      child[cell] = -1;
+      nchild[cell] = 0;
+      continue;
+    }
+    int k = first_child;
+    for (int v = 0; v < 8; ++v) {
+      if (bounds[v + 1] > bounds[v]) {
+        lo[k] = bounds[v];
+        hi[k] = bounds[v + 1];
+        ++k;
+      }
+    }
+    child[cell] = first_child;
+    nchild[cell] = nc;
+  }
+}
+
+// Generation g+1 ends where the cells appended while splitting generation g end.
+__global__ void tree_advance_kernel(int g, int* counters) { counters[5 + g] = counters[0]; }
+
+// ------------------------------------------------------------ upward pass --
+// Cell geometry record (8 doubles): box min x y z, box max x y z, σmax, unused.
+constexpr int kGeom = 8;
+
+// Binomial coefficient, iteratively: a recursive form becomes a recursive
+// device call wherever the loops around it are not fully unrolled, and
+// recursion has no static stack bound.
+__host__ __device__ constexpr int binom(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  int r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+
+__device__ __forceinline__ void cell_centre(const double* g, double& cx, double& cy, double& cz,
+                                            double& r) {
+  cx = 0.5 * (g[0] + g[3]);
+  cy = 0.5 * (g[1] + g[4]);
+  cz = 0.5 * (g[2] + g[5]);
+  const double ex = 0.5 * (g[3] - g[0]), ey = 0.5 * (g[4] - g[1]), ez = 0.5 * (g[5] - g[2]);
+  r = sqrt(ex * ex + ey * ey + ez * ez);
+}
+
+// Cells of generation g: leaves from their particles, parents from their
+// children (which belong to later generations, already done).
+template <int P>
+__global__ void tree_upward_kernel(int g, const int* __restrict__ counters, const int* __restrict__ lo,
+                                   const int* __restrict__ hi, const int* __restrict__ child,
+                                   const int* __restrict__ nchild, const double* __restrict__ sorted,
+                                   int64_t ldw, double* geom, double* mom) {
+  constexpr int NC = ncoef(P);
+  const int begin = counters[3 + g], end = counters[4 + g];
+  for (int cell = begin + int(blockIdx.x * blockDim.x + threadIdx.x); cell < end;
+       cell += int(gridDim.x * blockDim.x)) {
+    double* gc = geom + int64_t(cell) * kGeom;
+    const int nc = nchild[cell];
+    double bx[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    double smax = 0.0;
+    if (nc == 0) {
+      for (int i = lo[cell]; i < hi[cell]; ++i) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const double x = sorted[d * ldw + i];
+          bx[d] = fmin(bx[d], x);
+          bx[3 + d] = fmax(bx[3 + d], x);
+        }
+        smax = fmax(smax, sorted[6 * ldw + i]);
+      }
+    } else {
+      for (int k = 0; k < nc; ++k) {
+        if (child[cell] + k >= counters[0]) {
+          atomicOr(const_cast<int*>(&counters[2]), 32);
+          break;
+        }
+        const double* gk = geom + int64_t(child[cell] + k) * kGeom;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          bx[d] = fmin(bx[d], gk[d]);
+          bx[3 + d] = fmax(bx[3 + d], gk[3 + d]);
+        }
+        smax = fmax(smax, gk[6]);
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < 6; ++d) gc[d] = bx[d];
+    gc[6] = smax;
+    gc[7] = 0.0;
+    double cx, cy, cz, rad;
+    cell_centre(gc, cx, cy, cz, rad);
+    double* mc = mom + int64_t(cell) * 3 * NC;
+    for (int m = 0; m < 3; ++m) {
+      double acc[NC];
+#pragma unroll
+      for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+      if (nc == 0) {
+        for (int i = lo[cell]; i < hi[cell]; ++i) {
+          double pw[NC];
+          monomials<P, double>(sorted[i] - cx, sorted[ldw + i] - cy, sorted[2 * ldw + i] - cz, pw);
+          const double gm = sorted[(3 + m) * ldw + i];
+#pragma unroll
+          for (int k = 0; k < NC; ++k) acc[k] += gm * pw[k];
+        }
+      } else {
+        for (int q = 0; q < nc; ++q) {
+          const int ch = child[cell] + q;
+          double qx, qy, qz, qr;
+          cell_centre(geom + int64_t(ch) * kGeom, qx, qy, qz, qr);
+          double tp[NC];
+          monomials<P, double>(qx - cx, qy - cy, qz - cz, tp);
+          const double* mq = mom + int64_t(ch) * 3 * NC + m * NC;
+          // (y - c)^k = Σ_{j<=k} C(k, j) (y - c_q)^j (c_q - c)^{k-j}
+#pragma unroll
+          for (int n = 0; n <= P; ++n)
+#pragma unroll
+            for (int a = n; a >= 0; --a)
+#pragma unroll
+              for (int b = n - a; b >= 0; --b) {
+                const int c = n - a - b;
+                double s = 0.0;
+#pragma unroll
+                for (int ja = 0; ja <= a; ++ja)
+#pragma unroll
+                  for (int jb = 0; jb <= b; ++jb)
+#pragma unroll
+                    for (int jc = 0; jc <= c; ++jc)
+                      s += double(binom(a, ja) * binom(b, jb) * binom(c, jc)) *
+                           tp[midx(a - ja, b - jb, c - jc)] * mq[midx(ja, jb, jc)];
+                acc[midx(a, b, c)] += s;
+              }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NC; ++k) mc[m * NC + k] = acc[k];
+    }
+  }
+}
+
+__global__ void moments_to_f32_kernel(int64_t n, const double* __restrict__ a, float* b) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = float(a[i]);
+}
+
+// -------------------------------------------------------------- traversal --
+// One thread per target leaf; FILL = false counts the far cells and near
+// leaves, FILL = true writes them at the scanned offsets (same order).
+template <bool FILL>
+__global__ void traverse_kernel(int nleaves, const int* __restrict__ leaves, const int* __restrict__ child,
+                                const int* __restrict__ nchild, const double* __restrict__ geom,
+                                double theta, double sfac, int* nfar, int* nnear,
+                                const int* __restrict__ ofar, const int* __restrict__ onear,
+                                int* far_list, int* near_list, int* counters, int ncells) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nleaves) return;
+  const int tc = leaves[t];
+  double tx, ty, tz, tr;
+  cell_centre(geom + int64_t(tc) * kGeom, tx, ty, tz, tr);
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  int cf = 0, cn = 0;
+  const int of = FILL ? ofar[t] : 0, on = FILL ? onear[t] : 0;
+  while (sp > 0) {
+    const int s = stack[--sp];
+    if (s < 0 || s >= ncells) {
+      atomicOr(&counters[2], 16);
+      break;
+    }
+    const double* gs = geom + int64_t(s) * kGeom;
+    double sx, sy, sz, sr;
+    cell_centre(gs, sx, sy, sz, sr);
+    const double dx = tx - sx, dy = ty - sy, dz = tz - sz;
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
+    if (tr + sr < theta * d && d - tr - sr >= sfac * gs[6]) {
+      if (FILL) far_list[of + cf] = s;
+      ++cf;
+    } else if (nchild[s] == 0) {
+      if (FILL) near_list[on + cn] = s;
+      ++cn;
+    } else {
+      const int c0 = child[s], nc = nchild[s];
+      if (sp + nc > kStack) {   // cannot happen for 21 Morton levels (7·21 + 1 entries)
+        atomicOr(&counters[2], 2);
+        break;
+      }
+      for (int k = nc - 1; k >= 0; --k) stack[sp++] = c0 + k;
+    }
+  }
+  if (!FILL) {
+    nfar[t] = cf;
+    nnear[t] = cn;
+  }
+}
+
+// --------------------------------------------------------------- near field --
+// One CTA per target leaf: the leaf's targets (kTreeBlock at a time, one per
+// thread) against every particle of its near leaves, staged in shared memory.
+// FP32: positions relative to the leaf's first particle from the packed
+// records, the FP32 pair routines of the direct sum, sums folded into (hi, lo)
+// pairs after each staged block.  Raw sums (U 3, A 9, W 3) go to raw[k·ldr + i]
+// in Morton order.
+template <int KERNEL>
+__global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
+    const int* __restrict__ leaves, const int* __restrict__ lo, const int* __restrict__ hi,
+    const int* __restrict__ onear, const int* __restrict__ nnear, const int* __restrict__ near_list,
+    const float4* __restrict__ rec, double* raw, int64_t ldr, int ncells, int* counters) {
+  __shared__ float4 sA[kTreeBlock], sB[kTreeBlock];
+  const int tid = threadIdx.x;
+  const int tc = leaves[blockIdx.x];
+  const int a = lo[tc], b = hi[tc];
+  const float4 c0 = rec[3 * int64_t(a)], c1 = rec[3 * int64_t(a) + 1];
+  const int l0 = onear[blockIdx.x], ln = nnear[blockIdx.x];
+  for (int t0 = a; t0 < b; t0 += kTreeBlock) {
+    const int i = t0 + tid;
+    float tx[1] = {0.f}, ty[1] = {0.f}, tz[1] = {0.f};
+    if (i < b) {
+      const float4 r0 = rec[3 * int64_t(i)], r1 = rec[3 * int64_t(i) + 1];
+      tx[0] = rel_f32(r0.x, r1.x, c0.x, c1.x);
+      ty[0] = rel_f32(r0.y, r1.y, c0.y, c1.y);
+      tz[0] = rel_f32(r0.z, r1.z, c0.z, c1.z);
+    }
+    float acc[1][15], shi[15], slo[15];
+#pragma unroll
+    for (int v = 0; v < 15; ++v) acc[0][v] = shi[v] = slo[v] = 0.f;
+    for (int l = 0; l < ln; ++l) {
+      const int sc = near_list[l0 + l];
+      if (sc < 0 || sc >= ncells) {   // uniform over the CTA: every thread skips it
+        if (tid == 0) atomicOr(&counters[2], 8);
+        continue;
+      }
+      const int sa = lo[sc], sb = hi[sc];
+      for (int s0 = sa; s0 < sb; s0 += kTreeBlock) {
+        __syncthreads();
+        const int j = s0 + tid;
+        float4 qa, qb;
+        if (j < sb) {
+          const float4 r0 = rec[3 * int64_t(j)], r1 = rec[3 * int64_t(j) + 1],
+                       r2 = rec[3 * int64_t(j) + 2];
+          qa = make_float4(rel_f32(r0.x, r1.x, c0.x, c1.x), rel_f32(r0.y, r1.y, c0.y, c1.y),
+                           rel_f32(r0.z, r1.z, c0.z, c1.z), r0.w);
+          qb = make_float4(r2.x, r2.y, r2.z, r1.w);
+        } else {
+          qa = make_float4(0.f, 0.f, 0.f, 0.f);
+          qb = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        sA[tid] = qa;
+        sB[tid] = qb;
+        __syncthreads();
+        const int cnt = min(kTreeBlock, sb - s0);
+        if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+          for (int js = 0; js < cnt; ++js) uj_source_winck<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+        } else {
+          for (int js = 0; js < cnt; ++js) uj_source_gauss<1, false>(sA[js], sB[js], tx, ty, tz, acc);
+        }
+#pragma unroll
+        for (int v = 0; v < 15; ++v) {
+          float s, e;
+          two_sum(shi[v], acc[0][v], s, e);
+          shi[v] = s;
+          slo[v] += e;
+          acc[0][v] = 0.f;
+        }
+      }
+    }
+    if (i < b) {
+      double v[15];
+#pragma unroll
+      for (int k = 0; k < 15; ++k) v[k] = double(shi[k]) + double(slo[k]);
+      v[11] = -(v[3] + v[7]);   // A22: the FP32 pair routines keep J trace-free
+#pragma unroll
+      for (int k = 0; k < 15; ++k) raw[k * ldr + i] = v[k];
+    }
+  }
+}
+
+// FP64 near field on the sorted FP64 state (positions relative to the leaf's
+// first particle; pairs with r = 0 skipped as in the direct FP64 sum).
+template <int KERNEL>
+__global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
+    const int* __restrict__ leaves, const int* __restrict__ lo, const int* __restrict__ hi,
+    const int* __restrict__ onear, const int* __restrict__ nnear, const int* __restrict__ near_list,
+    const double* __restrict__ sorted, int64_t ldw, double* raw, int64_t ldr, int ncells,
+    int* counters) {
+  __shared__ double sx[kTreeBlock], sy[kTreeBlock], sz[kTreeBlock], sa_[kTreeBlock];
+  __shared__ double sg0[kTreeBlock], sg1[kTreeBlock], sg2[kTreeBlock], sb_[kTreeBlock];
+  const int tid = threadIdx.x;
+  const int tc = leaves[blockIdx.x];
+  const int a = lo[tc], b = hi[tc];
+  const double cx = sorted[a], cy = sorted[ldw + a], cz = sorted[2 * ldw + a];
+  const int l0 = onear[blockIdx.x], ln = nnear[blockIdx.x];
+  for (int t0 = a; t0 < b; t0 += kTreeBlock) {
+    const int i = t0 + tid;
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    if (i < b) {
+      tx = sorted[i] - cx;
+      ty = sorted[ldw + i] - cy;
+      tz = sorted[2 * ldw + i] - cz;
+    }
+    double acc[15];
+#pragma unroll
+    for (int v = 0; v < 15; ++v) acc[v] = 0.0;
+    for (int l = 0; l < ln; ++l) {
+      const int sc = near_list[l0 + l];
+      if (sc < 0 || sc >= ncells) {
+        if (tid == 0) atomicOr(&counters[2], 8);
+        continue;
+      }
+      const int s_lo = lo[sc], s_hi = hi[sc];
+      for (int s0 = s_lo; s0 < s_hi; s0 += kTreeBlock) {
+        __syncthreads();
+        const int j = s0 + tid;
+        if (j < s_hi) {
+          sx[tid] = sorted[j] - cx;
+          sy[tid] = sorted[ldw + j] - cy;
+          sz[tid] = sorted[2 * ldw + j] - cz;
+          sg0[tid] = sorted[3 * ldw + j];
+          sg1[tid] = sorted[4 * ldw + j];
+          sg2[tid] = sorted[5 * ldw + j];
+          double ka, kb;
+          source_consts<KERNEL, double>(sorted[6 * ldw + j], ka, kb);
+          sa_[tid] = ka;
+          sb_[tid] = kb;
+        }
+        __syncthreads();
+        const int cnt = min(kTreeBlock, s_hi - s0);
+        for (int js = 0; js < cnt; ++js) {
+          const double dx = tx - sx[js], dy = ty - sy[js], dz = tz - sz[js];
+          const double r2 = dx * dx + dy * dy + dz * dz;
+          double q, p;
+          pair_qp<KERNEL>(r2, sa_[js], sb_[js], q, p);
+          if (r2 == 0.0) q = p = 0.0;
+          const double gx = sg0[js], gy = sg1[js], gz = sg2[js];
+          const double c0 = dy * gz - dz * gy, c1 = dz * gx - dx * gz, c2 = dx * gy - dy * gx;
+          acc[0] += q * c0; acc[1] += q * c1; acc[2] += q * c2;
+          const double p0 = p * c0, p1 = p * c1, p2 = p * c2;
+          acc[3] += p0 * dx; acc[4] += p0 * dy; acc[5] += p0 * dz;
+          acc[6] += p1 * dx; acc[7] += p1 * dy; acc[8] += p1 * dz;
+          acc[9] += p2 * dx; acc[10] += p2 * dy; acc[11] += p2 * dz;
+          acc[12] += q * gx; acc[13] += q * gy; acc[14] += q * gz;
+        }
+      }
+    }
+    if (i < b) {
+#pragma unroll
+      for (int k = 0; k < 15; ++k) raw[k * ldr + i] = acc[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- far field --
+// One thread per target (CTA per target leaf): moments of the leaf's far
+// cells at the target, plus the near-field raw sums; U and J are written at
+// the target's original index.
+template <int P, int KERNEL, typename R, typename M>
+__global__ void __launch_bounds__(kTreeBlock) far_kernel(
+    const int* __restrict__ leaves, const int* __restrict__ lo, const int* __restrict__ hi,
+    const int* __restrict__ ofar, const int* __restrict__ nfar, const int* __restrict__ far_list,
+    const double* __restrict__ geom, const M* __restrict__ mom, const double* __restrict__ sorted,
+    int64_t ldw, const double* __restrict__ raw, int64_t ldr, const int* __restrict__ perm,
+    double* U, double* J, int64_t ldo, int ncells, int* counters) {
+  constexpr int NC = ncoef(P);
+  const int tc = leaves[blockIdx.x];
+  const int a = lo[tc], b = hi[tc];
+  const int f0 = ofar[blockIdx.x], fn = nfar[blockIdx.x];
+  for (int i = a + int(threadIdx.x); i < b; i += kTreeBlock) {
+    const double x = sorted[i], y = sorted[ldw + i], z = sorted[2 * ldw + i];
+    R dp[9], dd[18];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dp[k] = R(0);
+#pragma unroll
+    for (int k = 0; k < 18; ++k) dd[k] = R(0);
+    for (int f = 0; f < fn; ++f) {
+      const int s = far_list[f0 + f];
+      if (s < 0 || s >= ncells) {   // a list entry outside the tree: record, skip
+        atomicOr(&counters[2], 4);
+        continue;
+      }
+      double sx, sy, sz, sr;
+      cell_centre(geom + int64_t(s) * kGeom, sx, sy, sz, sr);
+      R bk[ncoef(P + 2)];
+      taylor_coefficients<P + 2, R>(R(x - sx), R(y - sy), R(z - sz), bk);
+      m2p_accumulate<P, R, M>(bk, mom + int64_t(s) * 3 * NC, dp, dd);
+    }
+    R uf[3], jf[9];
+    curl_from_potential<R>(dp, dd, uf, jf);
+    double v[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) v[k] = raw[k * ldr + i];
+    const double w = kInv4Pi, kp = kp_to_qr<KERNEL>();
+    const int64_t o = perm[i];
+    U[o] = -w * v[0] + w * double(uf[0]);
+    U[ldo + o] = -w * v[1] + w * double(uf[1]);
+    U[2 * ldo + o] = -w * v[2] + w * double(uf[2]);
+    const double w0 = v[12], w1 = v[13], w2 = v[14];
+    const double jn[9] = {kp * v[3],      kp * v[4] + w2, kp * v[5] - w1,
+                          kp * v[6] - w2, kp * v[7],      kp * v[8] + w0,
+                          kp * v[9] + w1, kp * v[10] - w0, kp * v[11]};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) J[k * ldo + o] = -w * jn[k] + w * double(jf[k]);
+  }
+}
+
+// ------------------------------------------------------------------- host --
+namespace {
+
+template <typename T>
+cudaError_t grow(T*& p, size_t& have, size_t need) {
+  if (need <= have) return cudaSuccess;
+  cudaFree(p);
+  p = nullptr;
+  have = 0;
+  cudaError_t e = cudaMalloc(&p, need * sizeof(T));
+  if (e == cudaSuccess) have = need;
+  return e;
+}
+
+cudaError_t reserve_particles(FmmWork* w, int64_t n) {
+  if (n <= w->cap) return cudaSuccess;
+  const int64_t cap = std::max<int64_t>(n, 1024);
+  const int64_t cells = 2 * cap + 8;
+  void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
+                  w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->counters, w->box,
+                  w->box_part, w->nfar, w->nnear, w->ofar, w->onear, w->cub_tmp};
+  for (void* p : ptrs) cudaFree(p);
+  cudaError_t e = cudaSuccess;
+  auto al = [&](auto*& p, size_t count) {
+    if (e == cudaSuccess) e = cudaMalloc(&p, count * sizeof(*p));
+  };
+  al(w->codes, cap); al(w->codes_alt, cap); al(w->idx, cap); al(w->perm, cap);
+  al(w->sorted, 7 * size_t(cap)); al(w->rec, 3 * size_t(cap)); al(w->near_raw, 15 * size_t(cap));
+  al(w->lo, cells); al(w->hi, cells); al(w->child, cells); al(w->nchild, cells);
+  al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells);
+  al(w->counters, 3 + kMaxGen + 3); al(w->box, 4); al(w->box_part, kBoxBlocks * 6);
+  al(w->nfar, cells); al(w->nnear, cells); al(w->ofar, cells); al(w->onear, cells);
+  if (e != cudaSuccess) {
+    w->cap = 0;
+    return e;
+  }
+  size_t sort_bytes = 0, scan_bytes = 0;
+  e = cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, w->codes, w->codes_alt, w->idx, w->perm,
+                                      int(cap), 0, 63);
+  if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, w->nfar, w->ofar, int(cells));
+  if (e == cudaSuccess) {
+    w->cub_bytes = std::max(sort_bytes, scan_bytes);
+    e = cudaMalloc(&w->cub_tmp, w->cub_bytes);
+  }
+  if (e != cudaSuccess) {
+    w->cap = 0;
+    return e;
+  }
+  w->cap = cap;
+  w->cell_cap = cells;
+  return cudaSuccess;
+}
+
+template <int P>
+void launch_upward(FmmWork* w, int g, int ncells_in_gen, int64_t ldw, cudaStream_t st) {
+  const int grid = std::max(1, std::min((ncells_in_gen + 63) / 64, 4096));
+  tree_upward_kernel<P><<<grid, 64, 0, st>>>(g, w->counters, w->lo, w->hi, w->child, w->nchild,
+                                             w->sorted, ldw, w->geom, w->mom);
+}
+
+template <int P>
+cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int nleaves, int ncells, int64_t ldw,
+                       double* U, double* J, int64_t ldo, cudaStream_t st) {
+  const dim3 grid(nleaves), block(kTreeBlock);
+#define VPM_FAR(K, R, M, mp)                                                                        \
+  far_kernel<P, K, R, M><<<grid, block, 0, st>>>(w->leaves, w->lo, w->hi, w->ofar, w->nfar,       \
+                                                 w->far_list, w->geom, mp, w->sorted, ldw,        \
+                                                 w->near_raw, ldw, w->perm, U, J, ldo, ncells, \
+                                                 w->counters)
+  if (kernel == VPM_KERNEL_WINCKELMANS) {
+    if (f64) VPM_FAR(VPM_KERNEL_WINCKELMANS, double, double, w->mom);
+    else VPM_FAR(VPM_KERNEL_WINCKELMANS, float, float, w->momf);
+  } else {
+    if (f64) VPM_FAR(VPM_KERNEL_GAUSSIANERF, double, double, w->mom);
+    else VPM_FAR(VPM_KERNEL_GAUSSIANERF, float, float, w->momf);
+  }
+#undef VPM_FAR
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool fmm_order_supported(int p) { return p == 2 || p == 4 || p == 6; }
+
+void fmm_stats(const FmmWork* w, int64_t* cells, int64_t* leaves, int64_t* far_entries,
+               int64_t* near_entries) {
+  if (cells) *cells = w ? w->last_cells : 0;
+  if (leaves) *leaves = w ? w->last_leaves : 0;
+  if (far_entries) *far_entries = w ? w->last_far : 0;
+  if (near_entries) *near_entries = w ? w->last_near : 0;
+}
+
+// U and J of every particle of the context by the treecode (see the header).
+// Returns a CUDA error, or cudaErrorInvalidValue with *why set for a tree that
+// outgrew its bounds (cannot happen for the 2n + 8 cells reserved).
+cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
+                     double sfac, const char** why) {
+  *why = nullptr;
+  const int64_t n = c->n;
+  if (n == 0) return cudaSuccess;
+  if (!c->fmm) c->fmm = new FmmWork();
+  FmmWork* w = c->fmm;
+  cudaError_t e = reserve_particles(w, n);
+  if (e != cudaSuccess) return e;
+  cudaStream_t st = c->st;
+  const int64_t ldw = w->cap;
+  const bool f64 = prec == VPM_PREC_FP64;
+  // VPM_FMM_SYNC=1: synchronise after every stage so that an error names it.
+  static const bool stage_sync = [] {
+    const char* v = std::getenv("VPM_FMM_SYNC");
+    return v && v[0] && v[0] != '0';
+  }();
+  const char* stage = "codes";
+  auto launched = [&](int k) {
+    c->launches += k;
+    cudaError_t le = cudaGetLastError();
+    if (le == cudaSuccess && stage_sync) le = cudaStreamSynchronize(st);
+    if (le != cudaSuccess) *why = stage;
+    return le;
+  };
+
+  // 1. codes, sort, gather
+  box_partial_kernel<<<kBoxBlocks, 256, 0, st>>>(n, c->X, c->ld, w->box_part);
+  box_final_kernel<<<1, 1, 0, st>>>(w->box_part, kBoxBlocks, w->box);
+  morton_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, c->X, c->ld, w->box, w->codes, w->idx);
+  if ((e = launched(3)) != cudaSuccess) return e;
+  size_t bytes = w->cub_bytes;
+  e = cub::DeviceRadixSort::SortPairs(w->cub_tmp, bytes, w->codes, w->codes_alt, w->idx, w->perm,
+                                      int(n), 0, 63, st);
+  if (e != cudaSuccess) return e;
+  c->launches += 4;   // the radix sort's passes (counted approximately)
+  const uint64_t* codes = w->codes_alt;
+  gather_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, w->perm, c->X, c->G, c->S, c->ld,
+                                                     w->sorted, ldw);
+  if ((e = launched(1)) != cudaSuccess) return e;
+  if (!f64) {
+    e = launch_pack_sources(kernel, n, w->sorted, w->sorted + 3 * ldw, w->sorted + 6 * ldw, ldw,
+                            1.0, w->rec, nullptr, st);
+    if ((e = e == cudaSuccess ? launched(1) : e) != cudaSuccess) return e;
+  }
+
+  // 2. tree, generation by generation
+  stage = "tree build";
+  tree_init_kernel<<<1, 1, 0, st>>>(n, w->lo, w->hi, w->counters);
+  const int split_grid = int(std::min<int64_t>((w->cell_cap + 255) / 256, 4 * 152));
+  for (int g = 0; g < kMaxGen - 1; ++g) {
+    tree_split_kernel<<<split_grid, 256, 0, st>>>(g, ncrit, w->cell_cap, codes, w->lo, w->hi,
+                                                  w->child, w->nchild, w->leaves, w->counters);
+    tree_advance_kernel<<<1, 1, 0, st>>>(g, w->counters);
+  }
+  if ((e = launched(1 + 2 * (kMaxGen - 1))) != cudaSuccess) return e;
+  int* hc = w->h_counters;
+  e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * (3 + kMaxGen + 1), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (hc[2] != 0) {
+    *why = "tree outgrew its cell bounds";
+    return cudaErrorInvalidValue;
+  }
+  const int ncells = hc[0], nleaves = hc[1];
+
+  // 3. upward pass (deepest generation first)
+  const int NC = p == 2 ? ncoef(2) : p == 4 ? ncoef(4) : ncoef(6);
+  if (w->mom_cells < ncells || w->mom_p != p) {
+    cudaFree(w->mom);
+    cudaFree(w->momf);
+    w->mom = nullptr;
+    w->momf = nullptr;
+    w->mom_cells = 0;
+    e = cudaMalloc(&w->mom, size_t(ncells) * 3 * NC * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&w->momf, size_t(ncells) * 3 * NC * sizeof(float));
+    if (e != cudaSuccess) return e;
+    w->mom_cells = ncells;
+    w->mom_p = p;
+  }
+  stage = "upward pass";
+  int last_gen = 0;
+  for (int g = 0; g < kMaxGen; ++g)
+    if (hc[3 + g + 1] > hc[3 + g]) last_gen = g;
+  for (int g = last_gen; g >= 0; --g) {
+    const int cnt = hc[3 + g + 1] - hc[3 + g];
+    if (cnt <= 0) continue;
+    if (p == 2) launch_upward<2>(w, g, cnt, ldw, st);
+    else if (p == 4) launch_upward<4>(w, g, cnt, ldw, st);
+    else launch_upward<6>(w, g, cnt, ldw, st);
+    if ((e = launched(1)) != cudaSuccess) return e;
+  }
+  if (!f64) {
+    const int64_t nm = int64_t(ncells) * 3 * NC;
+    moments_to_f32_kernel<<<int((nm + 255) / 256), 256, 0, st>>>(nm, w->mom, w->momf);
+    if ((e = launched(1)) != cudaSuccess) return e;
+  }
+
+  // 4. interaction lists: count, scan, fill
+  stage = "traversal";
+  const int tgrid = (nleaves + 127) / 128;
+  traverse_kernel<false><<<tgrid, 128, 0, st>>>(nleaves, w->leaves, w->child, w->nchild, w->geom,
+                                                theta, sfac, w->nfar, w->nnear, nullptr, nullptr,
+                                                nullptr, nullptr, w->counters, ncells);
+  if ((e = launched(1)) != cudaSuccess) return e;
+  bytes = w->cub_bytes;
+  e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nfar, w->ofar, nleaves, st);
+  if (e == cudaSuccess) {
+    bytes = w->cub_bytes;
+    e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nnear, w->onear, nleaves, st);
+  }
+  if (e != cudaSuccess) return e;
+  c->launches += 2;
+  int tail[4];
+  e = cudaMemcpyAsync(&tail[0], w->ofar + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&tail[1], w->nfar + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&tail[2], w->onear + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&tail[3], w->nnear + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  const int64_t nf = int64_t(tail[0]) + tail[1], nn = int64_t(tail[2]) + tail[3];
+  const int64_t need = std::max<int64_t>(std::max(nf, nn), 1);
+  if (need > w->list_cap) {
+    cudaFree(w->far_list);
+    cudaFree(w->near_list);
+    w->far_list = w->near_list = nullptr;
+    w->list_cap = 0;
+    e = cudaMalloc(&w->far_list, need * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&w->near_list, need * sizeof(int));
+    if (e != cudaSuccess) return e;
+    w->list_cap = need;
+  }
+  traverse_kernel<true><<<tgrid, 128, 0, st>>>(nleaves, w->leaves, w->child, w->nchild, w->geom,
+                                               theta, sfac, w->nfar, w->nnear, w->ofar, w->onear,
+                                               w->far_list, w->near_list, w->counters, ncells);
+  if ((e = launched(1)) != cudaSuccess) return e;
+
+  // 5. near field, 6. far field + output
+  stage = "near field";
+  if (f64) {
+    if (kernel == VPM_KERNEL_WINCKELMANS)
+      near_f64_kernel<VPM_KERNEL_WINCKELMANS><<<nleaves, kTreeBlock, 0, st>>>(
+          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, ncells,
+          w->counters);
+    else
+      near_f64_kernel<VPM_KERNEL_GAUSSIANERF><<<nleaves, kTreeBlock, 0, st>>>(
+          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, ncells,
+          w->counters);
+  } else {
+    if (kernel == VPM_KERNEL_WINCKELMANS)
+      near_f32_kernel<VPM_KERNEL_WINCKELMANS><<<nleaves, kTreeBlock, 0, st>>>(
+          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, ncells, w->counters);
+    else
+      near_f32_kernel<VPM_KERNEL_GAUSSIANERF><<<nleaves, kTreeBlock, 0, st>>>(
+          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, ncells, w->counters);
+  }
+  if ((e = launched(1)) != cudaSuccess) return e;
+  if (p == 2) e = launch_far<2>(w, kernel, f64, nleaves, ncells, ldw, c->U, c->J, c->ld, st);
+  else if (p == 4) e = launch_far<4>(w, kernel, f64, nleaves, ncells, ldw, c->U, c->J, c->ld, st);
+  else e = launch_far<6>(w, kernel, f64, nleaves, ncells, ldw, c->U, c->J, c->ld, st);
+  stage = "far field";
+  if ((e = e == cudaSuccess ? launched(1) : e) != cudaSuccess) return e;
+  e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * 3, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (hc[2] != 0) {
+    *why = (hc[2] & 2) ? "tree traversal stack overflow" : "treecode index out of range (checked, skipped)";
+    return cudaErrorInvalidValue;
+  }
+  w->last_cells = ncells;
+  w->last_leaves = nleaves;
+  w->last_far = nf;
+  w->last_near = nn;
+  return cudaSuccess;
+}
+
+}  // namespace vpm

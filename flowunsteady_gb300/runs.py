@@ -306,6 +306,56 @@ def run_large(args):
             "max_rel_l2_J": max(c["rel_l2_J"] for c in checks), "final_diagnostics": d}
 
 
+# ------------------------------------------------------------------------- fmm --
+def run_fmm(args):
+    """Treecode (vpm_eval_UJ_fmm, FLOWUnsteady's default settings p=4,
+    ncrit=50, θ=0.4) against the direct FP32C sum on a helical wake: time per
+    evaluation of both, and the FP32C/FP64 accuracy of both on 4,096 sampled
+    targets against the GPU FP64 direct sum."""
+    import torch
+    n = args.n or 1048576
+    X, G, S = helical_wake(n, turns=12 if n > 500000 else 4)
+    f = Field(X, G, S)
+    k = L.KERNEL_GAUSSIANERF
+    fm = L.default_fmm()
+    L.check(f.lib.vpm_eval_UJ_fmm(f.p, k, L.PREC_FP32C, ctypes.byref(fm)), f.p)   # warm-up
+    ts = []
+    for _ in range(3):
+        _, t = timed(lambda: L.check(f.lib.vpm_eval_UJ_fmm(f.p, k, L.PREC_FP32C, ctypes.byref(fm)), f.p))
+        ts.append(t)
+    st = [ctypes.c_int64() for _ in range(4)]
+    L.check(f.lib.vpm_fmm_stats(f.p, *[ctypes.byref(v) for v in st]), f.p)
+    Uf, Jf = np.empty((n, 3)), np.empty((n, 3, 3))
+    L.check(f.lib.vpm_get_UJ(f.p, 0, n, L.dptr(Uf), 3, L.dptr(Jf), 9), f.p)
+    _, t_direct = timed(lambda: L.check(f.lib.vpm_eval_UJ(f.p, k, L.PREC_FP32C), f.p))
+    Ud, Jd = np.empty((n, 3)), np.empty((n, 3, 3))
+    L.check(f.lib.vpm_get_UJ(f.p, 0, n, L.dptr(Ud), 3, L.dptr(Jd), 9), f.p)
+    f.close()
+    rng = np.random.default_rng(20261207)
+    idx = np.sort(rng.choice(n, 4096, replace=False))
+    dev = torch.device("cuda:0")
+    Xd = torch.tensor(X.T.copy(), device=dev)
+    Gd = torch.tensor(G.T.copy(), device=dev)
+    Sd = torch.tensor(S, device=dev)
+    Td = torch.tensor(X[idx].T.copy(), device=dev)
+    U = torch.empty((3, 4096), dtype=torch.float64, device=dev)
+    J = torch.empty((9, 4096), dtype=torch.float64, device=dev)
+    L.check(L.lib().vpm_uj_device_async(k, L.PREC_FP64, n, Xd.data_ptr(), Gd.data_ptr(),
+                                        Sd.data_ptr(), n, 4096, Td.data_ptr(), 4096, U.data_ptr(),
+                                        J.data_ptr(), 4096, None))
+    torch.cuda.synchronize()
+    U64, J64 = U.cpu().numpy().T, J.cpu().numpy().T.reshape(4096, 3, 3)
+    return {"workload": f"helical wake N={n}", "kernel": "gaussianerf", "precision": "fp32c",
+            "fmm": {"p": fm.p, "ncrit": fm.ncrit, "theta": fm.theta,
+                    "sigma_factor": fm.sigma_factor},
+            "seconds_fmm": min(ts), "seconds_direct": t_direct,
+            "speedup": t_direct / min(ts),
+            "cells": st[0].value, "leaves": st[1].value, "far_entries": st[2].value,
+            "near_entries": st[3].value,
+            "fmm_rel_l2_U": rel_l2(Uf[idx], U64), "fmm_rel_l2_J": rel_l2(Jf[idx], J64),
+            "direct_rel_l2_U": rel_l2(Ud[idx], U64), "direct_rel_l2_J": rel_l2(Jd[idx], J64)}
+
+
 # ------------------------------------------------------------------------ step --
 def run_step(args):
     """k full RK3 steps (Gaussian-erf, dynamic SFS with analytic ∂/∂σ, ν = 1e-4,
@@ -332,7 +382,7 @@ def run_step(args):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("run", choices=["sweep", "rings", "batch", "large", "step"])
+    p.add_argument("run", choices=["sweep", "rings", "batch", "large", "step", "fmm"])
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--steps", type=int, default=None)
     p.add_argument("--fields", type=int, default=None)
@@ -343,7 +393,7 @@ def main(argv=None):
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,
-          "step": run_step}[args.run]
+          "step": run_step, "fmm": run_fmm}[args.run]
     res = fn(args)
     txt = json.dumps(res)
     if args.out:

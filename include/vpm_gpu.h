@@ -245,6 +245,36 @@ int vpm_ffv_direct(vpm_ctx* ctx, int kernel, int64_t nb, const double* Xb, int64
                    const double* Gb, int64_t stride_g, const double* Sb, int64_t stride_s,
                    double* M, int64_t stride_m);
 
+/* ------------------------------------------------------------- treecode -- */
+/* Settings of the treecode evaluation (the role of FLOWVPM's UJ_fmm with
+ * vpm.FMM(p, ncrit, theta), src/FLOWUnsteady_simulation.jl:38,43). */
+typedef struct vpm_fmm {
+  int32_t p;             /* expansion order of the cell moments: 2, 4 or 6 (4)          */
+  int32_t ncrit;         /* at most this many particles per leaf cell (50)               */
+  double theta;          /* a cell is far for a target leaf when (R_t+R_s) < theta·d (0.4) */
+  double sigma_factor;   /* ... and when d - R_t - R_s >= sigma_factor·(largest σ of the
+                            cell): the far field uses the singular kernel, so this keeps
+                            regularised pairs in the direct near field (7.1: Gaussian-erf
+                            cores agree with the singular kernel to FP32 rounding there;
+                            0 = as FLOWVPM's nonzero_sigma=false)                         */
+} vpm_fmm;
+
+/* p 4, ncrit 50, theta 0.4 (FLOWUnsteady's defaults), sigma_factor 7.1. */
+void vpm_fmm_default(vpm_fmm* f);
+
+/* U and J at every particle of the context by the treecode (replaces
+ * pfield.UJ = vpm.UJ_fmm): particles sorted along a Morton curve, an octree
+ * of leaves of at most ncrit particles, far cells from their order-p moments
+ * of the singular kernel, near leaves by the direct regularised sum in the
+ * given precision (FP32/FP32C: the FP32 pair routines with compensated sums;
+ * FP64).  Results as from vpm_eval_UJ (read them with vpm_get_UJ). */
+int vpm_eval_UJ_fmm(vpm_ctx* ctx, int kernel, int precision, const vpm_fmm* fmm);
+
+/* Size of the last treecode evaluation: cells, leaves, far-cell and near-leaf
+ * list entries (any pointer may be NULL). */
+int vpm_fmm_stats(const vpm_ctx* ctx, int64_t* cells, int64_t* leaves, int64_t* far_entries,
+                  int64_t* near_entries);
+
 /* Σ|Γ|-weighted centroids of index ranges: for r in [0, nranges) particles
  * [starts[r], ends[r]) -> centroid out[3r..3r+2]. */
 int vpm_centroids(vpm_ctx* ctx, int nranges, const int64_t* starts, const int64_t* ends,

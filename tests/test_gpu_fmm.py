@@ -1,0 +1,102 @@
+"""GPU treecode (vpm_eval_UJ_fmm, the role of FLOWVPM's UJ_fmm): against the
+FP64 oracle's direct sum, its convergence in θ and p, and the near-field limit
+where it must reproduce the direct FP32C sum."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from flowunsteady_gb300 import _lib as L
+from flowunsteady_gb300.workloads import helical_wake, uniform_box
+from tests.helpers import Ctx, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def fmm(p=4, ncrit=50, theta=0.4, sigma_factor=7.1):
+    f = L.Fmm()
+    f.p, f.ncrit, f.theta, f.sigma_factor = p, ncrit, theta, sigma_factor
+    return f
+
+
+def eval_fmm(c, k, prec, f):
+    c.rc(c.lib.vpm_eval_UJ_fmm(c.p, k, prec, ctypes.byref(f)))
+    n = c.np()
+    U, J = np.empty((n, 3)), np.empty((n, 3, 3))
+    c.rc(c.lib.vpm_get_UJ(c.p, 0, n, L.dptr(U), 3, L.dptr(J), 9))
+    return U, J
+
+
+def stats(c):
+    v = [ctypes.c_int64() for _ in range(4)]
+    c.rc(c.lib.vpm_fmm_stats(c.p, *[ctypes.byref(x) for x in v]))
+    return [x.value for x in v]
+
+
+def test_defaults_follow_flowunsteady():
+    f = L.default_fmm()
+    assert (f.p, f.ncrit, f.theta) == (4, 50, 0.4) and f.sigma_factor == 7.1
+
+
+@pytest.mark.parametrize("k", [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF])
+def test_treecode_matches_direct_sum_helical_wake(oracle, k):
+    X, G, S = helical_wake(40000)
+    idx = np.sort(np.random.default_rng(3).choice(40000, 500, replace=False))
+    U0, J0 = oracle.uj_direct(k, X, G, S, Xt=X[idx])
+    with Ctx(40000) as c:
+        c.set(X, G, S)
+        U, J = eval_fmm(c, k, L.PREC_FP32C, fmm())
+        cells, leaves, nfar, nnear = stats(c)
+        assert leaves > 40000 // 50 and cells > leaves and nfar > 0 and nnear > 0
+        eu, ej = rel_l2(U[idx], U0), rel_l2(J[idx], J0)
+        assert eu <= 1e-4 and ej <= 1e-4, (eu, ej)
+        # Tighter settings converge to the direct sum.  Winckelmans cores
+        # differ from the singular far-field kernel by 1.875 (σ/r)^4, so far
+        # cells also have to be further away in core sizes.
+        tight = fmm(p=6, theta=0.25, sigma_factor=30.0 if k == L.KERNEL_WINCKELMANS else 7.1)
+        U6, J6 = eval_fmm(c, k, L.PREC_FP32C, tight)
+        e6u, e6j = rel_l2(U6[idx], U0), rel_l2(J6[idx], J0)
+        assert e6u <= 0.2 * eu + 2e-6 and e6j <= 0.2 * ej + 2e-6, (eu, ej, e6u, e6j)
+
+
+def test_near_field_limit_equals_direct_fp32c():
+    # With every cell too close to be far, the treecode is the direct sum.
+    X, G, S = uniform_box(6000, seed_index=140)
+    with Ctx(6000) as c:
+        c.set(X, G, S)
+        Ud, Jd = c.uj(1, L.PREC_FP32C)
+        U, J = eval_fmm(c, 1, L.PREC_FP32C, fmm(theta=0.01))
+        assert stats(c)[2] == 0
+    assert rel_l2(U, Ud) <= 1e-6 and rel_l2(J, Jd) <= 1e-6
+
+
+def test_fp64_treecode_converges_with_order(oracle):
+    X, G, S = helical_wake(12000)
+    U0, J0 = oracle.uj_direct(1, X, G, S)
+    errs = []
+    with Ctx(12000) as c:
+        c.set(X, G, S)
+        for p in (2, 4, 6):
+            U, J = eval_fmm(c, 1, L.PREC_FP64, fmm(p=p, theta=0.4))
+            errs.append((rel_l2(U, U0), rel_l2(J, J0)))
+        # near-field limit in FP64: the oracle to FP64 rounding
+        U, J = eval_fmm(c, 1, L.PREC_FP64, fmm(theta=0.01))
+        assert rel_l2(U, U0) <= 1e-12 and rel_l2(J, J0) <= 1e-12
+    assert errs[1][0] < errs[0][0] and errs[2][0] < errs[1][0]
+    assert errs[2][0] < 1e-5
+
+
+def test_coincident_and_tiny_fields():
+    X, G, S = uniform_box(300, seed_index=141)
+    X[299] = X[0]
+    with Ctx(400) as c:
+        c.set(X[:1], G[:1], S[:1])
+        U, J = eval_fmm(c, 1, L.PREC_FP32C, fmm())
+        assert np.all(U == 0) and np.all(J == 0)
+        c.set(X, G, S)
+        Ud, Jd = c.uj(1, L.PREC_FP32C)
+        U, J = eval_fmm(c, 1, L.PREC_FP32C, fmm(ncrit=8))
+        assert np.all(np.isfinite(U)) and np.all(np.isfinite(J))
+        assert rel_l2(U, Ud) <= 1e-3 and rel_l2(J, Jd) <= 1e-2
+        bad = fmm(p=3)
+        assert c.lib.vpm_eval_UJ_fmm(c.p, 1, L.PREC_FP32C, ctypes.byref(bad)) == L.ERR_UNSUPPORTED

@@ -1,0 +1,50 @@
+"""CPU checks of the treecode's far-field arithmetic (the NumPy restatement in
+oracle/np_multipole.py of what csrc/tree.cuh computes): the Taylor recurrence
+against finite differences, the graded multi-index layout, and the cell
+expansion against the direct singular Biot-Savart sum."""
+import numpy as np
+import pytest
+
+from oracle import np_multipole as mp
+
+
+def test_graded_index_layout_is_a_bijection():
+    for q in range(9):
+        ks = mp.multi_indices(q)
+        assert len(ks) == (q + 1) * (q + 2) * (q + 3) // 6
+        assert [mp.midx(*k) for k in ks] == list(range(len(ks)))
+
+
+def test_taylor_recurrence_matches_finite_differences():
+    R = np.array([0.7, -0.4, 0.5])
+    b = mp.taylor_coefficients(3, R)
+    f = lambda y: 1.0 / np.linalg.norm(R - y)
+    h = 1e-3
+    e = np.eye(3)
+    d1 = (f(h * e[0]) - f(-h * e[0])) / (2 * h)
+    d11 = (f(h * e[0]) - 2 * f(0 * e[0]) + f(-h * e[0])) / (h * h) / 2.0
+    d12 = (f(h * (e[0] + e[1])) - f(h * (e[0] - e[1])) - f(h * (e[1] - e[0])) + f(-h * (e[0] + e[1]))) / (4 * h * h)
+    assert abs(b[mp.midx(1, 0, 0)] - d1) < 1e-6
+    assert abs(b[mp.midx(2, 0, 0)] - d11) < 1e-5
+    assert abs(b[mp.midx(1, 1, 0)] - d12) < 1e-5
+
+
+@pytest.mark.parametrize("dist", [0.6, 1.2])
+def test_cell_expansion_converges_to_the_direct_sum(dist):
+    rng = np.random.default_rng(11)
+    Y = rng.uniform(-0.1, 0.1, (300, 3))
+    G = rng.normal(0.0, 1.0, (300, 3))
+    c = np.zeros(3)
+    x = dist * np.array([1.0, 0.3, -0.2])
+    U0, J0 = mp.direct_singular(Y, G, x)
+    errs = []
+    for p in (0, 2, 4, 6):
+        U, J = mp.far_field(p, mp.moments(p, Y, G, c), c, x)
+        errs.append((np.linalg.norm(U - U0) / np.linalg.norm(U0),
+                     np.linalg.norm(J - J0) / np.linalg.norm(J0)))
+    for (eu0, ej0), (eu1, ej1) in zip(errs, errs[1:]):
+        assert eu1 < 0.3 * eu0 and ej1 < 0.3 * ej0
+    assert errs[2][0] < 1e-3 and errs[3][0] < 1e-4
+    # J is the gradient of U: trace-free
+    U, J = mp.far_field(4, mp.moments(4, Y, G, c), c, x)
+    assert abs(np.trace(J)) < 1e-9 * np.abs(J).max()
