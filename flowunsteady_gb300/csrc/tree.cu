@@ -12,14 +12,17 @@
 //   3. upward pass, deepest generation first: leaves take their bounding box,
 //      largest core and moments (order P) from their particles, parents from
 //      their children (box union; moments shifted to the parent centre);
-//   4. one thread per target leaf walks the tree: a cell s is far for leaf t
+//   4. targets are taken in groups: the largest cells with at most 64
+//      particles (and leaves that cannot be split), one CTA of 64 threads
+//      each.  One thread per group walks the tree: a cell s is far for group t
 //      when (R_t + R_s) < θ·d and d - R_t - R_s >= sigma_factor·σmax_s
 //      (d = distance of the centres), then it is evaluated from its moments;
-//      otherwise its leaves are summed directly (two passes: count, fill);
-//   5. the direct near field: one CTA per target leaf over its near leaves,
-//      with the regularised kernels of the direct sum (FP32 pair routines on
-//      positions relative to the leaf's first particle, or FP64);
-//   6. the far field: one thread per target over the far cells of its leaf
+//      otherwise its leaves are summed directly, consecutive leaves merged
+//      into one range of particles (two passes: count, fill);
+//   5. the direct near field: one CTA per group over its near ranges, with the
+//      regularised kernels of the direct sum (FP32 pair routines on positions
+//      relative to the group's first particle, or FP64);
+//   6. the far field: one thread per target over the far cells of its group
 //      (tree.cuh), added to the near field; results go to the original order.
 // The far field uses the singular kernel, as FLOWVPM's nonzero_sigma=false;
 // sigma_factor keeps regularised pairs out of it (Gaussian-erf: beyond 7.1 σ
@@ -41,6 +44,10 @@
 namespace vpm {
 
 constexpr int kMaxGen = 23;        // root + at most 21 Morton digits (+1 spare)
+// Device counters: cells, leaves, error flags, target groups, then the first
+// cell of every generation (generation g starts at counters[kGenBase + g]).
+constexpr int kCntCells = 0, kCntLeaves = 1, kCntFlags = 2, kCntGroups = 3, kGenBase = 4;
+constexpr int kNumCounters = kGenBase + kMaxGen + 2;
 constexpr int kStack = 256;        // traversal stack (cells)
 constexpr int kTreeBlock = 64;     // threads of the near/far evaluation CTAs
 
@@ -63,25 +70,27 @@ struct FmmWork {
   double* mom = nullptr;      // per cell: 3·ncoef(P) FP64 moments
   float* momf = nullptr;      // FP32 copy
   int* leaves = nullptr;      // leaf cell ids
-  int* counters = nullptr;    // [0] cells, [1] leaves, [2] overflow, [3..3+kMaxGen] generation starts
+  int* counters = nullptr;    // see kCntCells .. kGenBase
+  int* groups = nullptr;      // target-group cell ids
   double* box = nullptr;      // bounding cube: min x y z, size
   double* box_part = nullptr; // per-block min/max partials
   // interaction lists
   int *nfar = nullptr, *nnear = nullptr, *ofar = nullptr, *onear = nullptr;
-  int *far_list = nullptr, *near_list = nullptr;
+  int* far_list = nullptr;    // far cell ids per target group
+  int2* near_list = nullptr;  // near source ranges [x, y) per target group
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
-  int h_counters[3 + kMaxGen + 1];
+  int h_counters[kNumCounters];
   // statistics of the last evaluation
-  int64_t last_cells = 0, last_leaves = 0, last_far = 0, last_near = 0;
+  int64_t last_cells = 0, last_leaves = 0, last_groups = 0, last_far = 0, last_near = 0;
 };
 
 void fmm_free(FmmWork* w) {
   if (!w) return;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
                   w->lo, w->hi, w->child, w->nchild, w->geom, w->mom, w->momf, w->leaves,
-                  w->counters, w->box, w->box_part, w->nfar, w->nnear, w->ofar, w->onear,
-                  w->far_list, w->near_list, w->cub_tmp};
+                  w->groups, w->counters, w->box, w->box_part, w->nfar, w->nnear, w->ofar,
+                  w->onear, w->far_list, w->near_list, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   delete w;
 }
@@ -175,14 +184,21 @@ __global__ void gather_kernel(int64_t n, const int* __restrict__ perm, const dou
 }
 
 // ------------------------------------------------------------- tree build --
-__global__ void tree_init_kernel(int64_t n, int* lo, int* hi, int* counters) {
+// Target groups (the units of traversal and evaluation) are the largest cells
+// with at most kTreeBlock particles, and leaves that cannot be split.
+__global__ void tree_init_kernel(int64_t n, int* lo, int* hi, int* groups, int* counters) {
   lo[0] = 0;
   hi[0] = int(n);
-  counters[0] = 1;   // cells
-  counters[1] = 0;   // leaves
-  counters[2] = 0;   // overflow
-  counters[3] = 0;   // generation 0 starts at cell 0
-  counters[4] = 1;   // generation 1 starts at cell 1
+  counters[kCntCells] = 1;
+  counters[kCntLeaves] = 0;
+  counters[kCntFlags] = 0;
+  counters[kCntGroups] = 0;
+  counters[kGenBase + 0] = 0;   // generation 0 is the root
+  counters[kGenBase + 1] = 1;
+  if (n <= kTreeBlock) {
+    groups[0] = 0;
+    counters[kCntGroups] = 1;
+  }
 }
 
 __device__ __forceinline__ int lower_bound_code(const uint64_t* codes, int lo, int hi,
@@ -195,11 +211,11 @@ __device__ __forceinline__ int lower_bound_code(const uint64_t* codes, int lo, i
   return lo;
 }
 
-// Split or close the cells of generation g: [counters[3+g], counters[4+g]).
+// Split or close the cells of generation g.
 __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint64_t* __restrict__ codes,
                                   int* lo, int* hi, int* child, int* nchild, int* leaves,
-                                  int* counters) {
-  const int begin = counters[3 + g], end = counters[4 + g];
+                                  int* groups, int* counters) {
+  const int begin = counters[kGenBase + g], end = counters[kGenBase + g + 1];
   for (int cell = begin + int(blockIdx.x * blockDim.x + threadIdx.x); cell < end;
        cell += int(gridDim.x * blockDim.x)) {
     const int a = lo[cell], b = hi[cell];
@@ -207,7 +223,8 @@ __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint
     if (b - a <= ncrit || first == last) {
       child[cell] = -1;
       nchild[cell] = 0;
-      leaves[atomicAdd(&counters[1], 1)] = cell;
+      leaves[atomicAdd(&counters[kCntLeaves], 1)] = cell;
+      if (b - a > kTreeBlock) groups[atomicAdd(&counters[kCntGroups], 1)] = cell;   // unsplittable
       continue;
     }
     const int bit = 63 - __clzll((long long)(first ^ last));   // highest differing bit
@@ -219,9 +236,9 @@ __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint
     for (int v = 1; v < 8; ++v) bounds[v] = lower_bound_code(codes, a, b, prefix | (uint64_t(v) << shift));
     int nc = 0;
     for (int v = 0; v < 8; ++v) nc += bounds[v + 1] > bounds[v];
-    const int first_child = atomicAdd(&counters[0], nc);
+    const int first_child = atomicAdd(&counters[kCntCells], nc);
     if (first_child + nc > cell_cap) {
-      atomicOr(&counters[2], 1);
+      atomicOr(&counters[kCntFlags], 1);
       child[cell] = -1;
       nchild[cell] = 0;
       continue;
@@ -231,6 +248,8 @@ __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint
       if (bounds[v + 1] > bounds[v]) {
         lo[k] = bounds[v];
         hi[k] = bounds[v + 1];
+        if (b - a > kTreeBlock && bounds[v + 1] - bounds[v] <= kTreeBlock)
+          groups[atomicAdd(&counters[kCntGroups], 1)] = k;
         ++k;
       }
     }
@@ -240,7 +259,9 @@ __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint
 }
 
 // Generation g+1 ends where the cells appended while splitting generation g end.
-__global__ void tree_advance_kernel(int g, int* counters) { counters[5 + g] = counters[0]; }
+__global__ void tree_advance_kernel(int g, int* counters) {
+  counters[kGenBase + g + 2] = counters[kCntCells];
+}
 
 // ------------------------------------------------------------ upward pass --
 // Cell geometry record (8 doubles): box min x y z, box max x y z, σmax, unused.
@@ -273,7 +294,7 @@ __global__ void tree_upward_kernel(int g, const int* __restrict__ counters, cons
                                    const int* __restrict__ nchild, const double* __restrict__ sorted,
                                    int64_t ldw, double* geom, double* mom) {
   constexpr int NC = ncoef(P);
-  const int begin = counters[3 + g], end = counters[4 + g];
+  const int begin = counters[kGenBase + g], end = counters[kGenBase + g + 1];
   for (int cell = begin + int(blockIdx.x * blockDim.x + threadIdx.x); cell < end;
        cell += int(gridDim.x * blockDim.x)) {
     double* gc = geom + int64_t(cell) * kGeom;
@@ -292,8 +313,8 @@ __global__ void tree_upward_kernel(int g, const int* __restrict__ counters, cons
       }
     } else {
       for (int k = 0; k < nc; ++k) {
-        if (child[cell] + k >= counters[0]) {
-          atomicOr(const_cast<int*>(&counters[2]), 32);
+        if (child[cell] + k >= counters[kCntCells]) {
+          atomicOr(const_cast<int*>(&counters[kCntFlags]), 32);
           break;
         }
         const double* gk = geom + int64_t(child[cell] + k) * kGeom;
@@ -365,28 +386,31 @@ __global__ void moments_to_f32_kernel(int64_t n, const double* __restrict__ a, f
 }
 
 // -------------------------------------------------------------- traversal --
-// One thread per target leaf; FILL = false counts the far cells and near
-// leaves, FILL = true writes them at the scanned offsets (same order).
+// One thread per target group; FILL = false counts the far cells and near
+// source ranges, FILL = true writes them at the scanned offsets (same order).
+// Near leaves that continue the previous near range in Morton order extend it,
+// so siblings become one range of particles.
 template <bool FILL>
-__global__ void traverse_kernel(int nleaves, const int* __restrict__ leaves, const int* __restrict__ child,
+__global__ void traverse_kernel(int ngroups, const int* __restrict__ groups, const int* __restrict__ lo,
+                                const int* __restrict__ hi, const int* __restrict__ child,
                                 const int* __restrict__ nchild, const double* __restrict__ geom,
                                 double theta, double sfac, int* nfar, int* nnear,
                                 const int* __restrict__ ofar, const int* __restrict__ onear,
-                                int* far_list, int* near_list, int* counters, int ncells) {
+                                int* far_list, int2* near_list, int* counters, int ncells) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nleaves) return;
-  const int tc = leaves[t];
+  if (t >= ngroups) return;
+  const int tc = groups[t];
   double tx, ty, tz, tr;
   cell_centre(geom + int64_t(tc) * kGeom, tx, ty, tz, tr);
   int stack[kStack];
   int sp = 0;
   stack[sp++] = 0;
-  int cf = 0, cn = 0;
+  int cf = 0, cn = 0, last_hi = -1;
   const int of = FILL ? ofar[t] : 0, on = FILL ? onear[t] : 0;
   while (sp > 0) {
     const int s = stack[--sp];
     if (s < 0 || s >= ncells) {
-      atomicOr(&counters[2], 16);
+      atomicOr(&counters[kCntFlags], 16);
       break;
     }
     const double* gs = geom + int64_t(s) * kGeom;
@@ -398,12 +422,17 @@ __global__ void traverse_kernel(int nleaves, const int* __restrict__ leaves, con
       if (FILL) far_list[of + cf] = s;
       ++cf;
     } else if (nchild[s] == 0) {
-      if (FILL) near_list[on + cn] = s;
-      ++cn;
+      if (cn > 0 && lo[s] == last_hi) {
+        if (FILL) near_list[on + cn - 1].y = hi[s];
+      } else {
+        if (FILL) near_list[on + cn] = make_int2(lo[s], hi[s]);
+        ++cn;
+      }
+      last_hi = hi[s];
     } else {
       const int c0 = child[s], nc = nchild[s];
       if (sp + nc > kStack) {   // cannot happen for 21 Morton levels (7·21 + 1 entries)
-        atomicOr(&counters[2], 2);
+        atomicOr(&counters[kCntFlags], 2);
         break;
       }
       for (int k = nc - 1; k >= 0; --k) stack[sp++] = c0 + k;
@@ -416,20 +445,20 @@ __global__ void traverse_kernel(int nleaves, const int* __restrict__ leaves, con
 }
 
 // --------------------------------------------------------------- near field --
-// One CTA per target leaf: the leaf's targets (kTreeBlock at a time, one per
-// thread) against every particle of its near leaves, staged in shared memory.
-// FP32: positions relative to the leaf's first particle from the packed
-// records, the FP32 pair routines of the direct sum, sums folded into (hi, lo)
-// pairs after each staged block.  Raw sums (U 3, A 9, W 3) go to raw[k·ldr + i]
-// in Morton order.
+// One CTA per target group: the group's targets (kTreeBlock at a time, one
+// per thread) against every particle of its near source ranges, staged in
+// shared memory.  FP32: positions relative to the group's first particle from
+// the packed records, the FP32 pair routines of the direct sum, sums folded
+// into (hi, lo) pairs after each staged block.  Raw sums (U 3, A 9, W 3) go to
+// raw[k·ldr + i] in Morton order.
 template <int KERNEL>
 __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
-    const int* __restrict__ leaves, const int* __restrict__ lo, const int* __restrict__ hi,
-    const int* __restrict__ onear, const int* __restrict__ nnear, const int* __restrict__ near_list,
-    const float4* __restrict__ rec, double* raw, int64_t ldr, int ncells, int* counters) {
+    const int* __restrict__ groups, const int* __restrict__ lo, const int* __restrict__ hi,
+    const int* __restrict__ onear, const int* __restrict__ nnear, const int2* __restrict__ near_list,
+    const float4* __restrict__ rec, double* raw, int64_t ldr, int64_t n, int* counters) {
   __shared__ float4 sA[kTreeBlock], sB[kTreeBlock];
   const int tid = threadIdx.x;
-  const int tc = leaves[blockIdx.x];
+  const int tc = groups[blockIdx.x];
   const int a = lo[tc], b = hi[tc];
   const float4 c0 = rec[3 * int64_t(a)], c1 = rec[3 * int64_t(a) + 1];
   const int l0 = onear[blockIdx.x], ln = nnear[blockIdx.x];
@@ -446,12 +475,12 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
 #pragma unroll
     for (int v = 0; v < 15; ++v) acc[0][v] = shi[v] = slo[v] = 0.f;
     for (int l = 0; l < ln; ++l) {
-      const int sc = near_list[l0 + l];
-      if (sc < 0 || sc >= ncells) {   // uniform over the CTA: every thread skips it
-        if (tid == 0) atomicOr(&counters[2], 8);
+      const int2 rg = near_list[l0 + l];
+      const int sa = rg.x, sb = rg.y;
+      if (sa < 0 || sb > n || sa > sb) {   // uniform over the CTA: every thread skips it
+        if (tid == 0) atomicOr(&counters[kCntFlags], 8);
         continue;
       }
-      const int sa = lo[sc], sb = hi[sc];
       for (int s0 = sa; s0 < sb; s0 += kTreeBlock) {
         __syncthreads();
         const int j = s0 + tid;
@@ -500,14 +529,14 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
 // first particle; pairs with r = 0 skipped as in the direct FP64 sum).
 template <int KERNEL>
 __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
-    const int* __restrict__ leaves, const int* __restrict__ lo, const int* __restrict__ hi,
-    const int* __restrict__ onear, const int* __restrict__ nnear, const int* __restrict__ near_list,
-    const double* __restrict__ sorted, int64_t ldw, double* raw, int64_t ldr, int ncells,
+    const int* __restrict__ groups, const int* __restrict__ lo, const int* __restrict__ hi,
+    const int* __restrict__ onear, const int* __restrict__ nnear, const int2* __restrict__ near_list,
+    const double* __restrict__ sorted, int64_t ldw, double* raw, int64_t ldr, int64_t n,
     int* counters) {
   __shared__ double sx[kTreeBlock], sy[kTreeBlock], sz[kTreeBlock], sa_[kTreeBlock];
   __shared__ double sg0[kTreeBlock], sg1[kTreeBlock], sg2[kTreeBlock], sb_[kTreeBlock];
   const int tid = threadIdx.x;
-  const int tc = leaves[blockIdx.x];
+  const int tc = groups[blockIdx.x];
   const int a = lo[tc], b = hi[tc];
   const double cx = sorted[a], cy = sorted[ldw + a], cz = sorted[2 * ldw + a];
   const int l0 = onear[blockIdx.x], ln = nnear[blockIdx.x];
@@ -523,12 +552,12 @@ __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
 #pragma unroll
     for (int v = 0; v < 15; ++v) acc[v] = 0.0;
     for (int l = 0; l < ln; ++l) {
-      const int sc = near_list[l0 + l];
-      if (sc < 0 || sc >= ncells) {
-        if (tid == 0) atomicOr(&counters[2], 8);
+      const int2 rg = near_list[l0 + l];
+      const int s_lo = rg.x, s_hi = rg.y;
+      if (s_lo < 0 || s_hi > n || s_lo > s_hi) {
+        if (tid == 0) atomicOr(&counters[kCntFlags], 8);
         continue;
       }
-      const int s_lo = lo[sc], s_hi = hi[sc];
       for (int s0 = s_lo; s0 < s_hi; s0 += kTreeBlock) {
         __syncthreads();
         const int j = s0 + tid;
@@ -571,18 +600,18 @@ __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
 }
 
 // ---------------------------------------------------------------- far field --
-// One thread per target (CTA per target leaf): moments of the leaf's far
+// One thread per target (CTA per target group): moments of the group's far
 // cells at the target, plus the near-field raw sums; U and J are written at
 // the target's original index.
 template <int P, int KERNEL, typename R, typename M>
 __global__ void __launch_bounds__(kTreeBlock) far_kernel(
-    const int* __restrict__ leaves, const int* __restrict__ lo, const int* __restrict__ hi,
+    const int* __restrict__ groups, const int* __restrict__ lo, const int* __restrict__ hi,
     const int* __restrict__ ofar, const int* __restrict__ nfar, const int* __restrict__ far_list,
     const double* __restrict__ geom, const M* __restrict__ mom, const double* __restrict__ sorted,
     int64_t ldw, const double* __restrict__ raw, int64_t ldr, const int* __restrict__ perm,
     double* U, double* J, int64_t ldo, int ncells, int* counters) {
   constexpr int NC = ncoef(P);
-  const int tc = leaves[blockIdx.x];
+  const int tc = groups[blockIdx.x];
   const int a = lo[tc], b = hi[tc];
   const int f0 = ofar[blockIdx.x], fn = nfar[blockIdx.x];
   for (int i = a + int(threadIdx.x); i < b; i += kTreeBlock) {
@@ -595,7 +624,7 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
     for (int f = 0; f < fn; ++f) {
       const int s = far_list[f0 + f];
       if (s < 0 || s >= ncells) {   // a list entry outside the tree: record, skip
-        atomicOr(&counters[2], 4);
+        atomicOr(&counters[kCntFlags], 4);
         continue;
       }
       double sx, sy, sz, sr;
@@ -642,8 +671,8 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   const int64_t cap = std::max<int64_t>(n, 1024);
   const int64_t cells = 2 * cap + 8;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
-                  w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->counters, w->box,
-                  w->box_part, w->nfar, w->nnear, w->ofar, w->onear, w->cub_tmp};
+                  w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->groups, w->counters,
+                  w->box, w->box_part, w->nfar, w->nnear, w->ofar, w->onear, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   cudaError_t e = cudaSuccess;
   auto al = [&](auto*& p, size_t count) {
@@ -652,8 +681,8 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   al(w->codes, cap); al(w->codes_alt, cap); al(w->idx, cap); al(w->perm, cap);
   al(w->sorted, 7 * size_t(cap)); al(w->rec, 3 * size_t(cap)); al(w->near_raw, 15 * size_t(cap));
   al(w->lo, cells); al(w->hi, cells); al(w->child, cells); al(w->nchild, cells);
-  al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells);
-  al(w->counters, 3 + kMaxGen + 3); al(w->box, 4); al(w->box_part, kBoxBlocks * 6);
+  al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells); al(w->groups, cells);
+  al(w->counters, kNumCounters); al(w->box, 4); al(w->box_part, kBoxBlocks * 6);
   al(w->nfar, cells); al(w->nnear, cells); al(w->ofar, cells); al(w->onear, cells);
   if (e != cudaSuccess) {
     w->cap = 0;
@@ -684,11 +713,11 @@ void launch_upward(FmmWork* w, int g, int ncells_in_gen, int64_t ldw, cudaStream
 }
 
 template <int P>
-cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int nleaves, int ncells, int64_t ldw,
+cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int ngroups, int ncells, int64_t ldw,
                        double* U, double* J, int64_t ldo, cudaStream_t st) {
-  const dim3 grid(nleaves), block(kTreeBlock);
+  const dim3 grid(ngroups), block(kTreeBlock);
 #define VPM_FAR(K, R, M, mp)                                                                        \
-  far_kernel<P, K, R, M><<<grid, block, 0, st>>>(w->leaves, w->lo, w->hi, w->ofar, w->nfar,       \
+  far_kernel<P, K, R, M><<<grid, block, 0, st>>>(w->groups, w->lo, w->hi, w->ofar, w->nfar,       \
                                                  w->far_list, w->geom, mp, w->sorted, ldw,        \
                                                  w->near_raw, ldw, w->perm, U, J, ldo, ncells, \
                                                  w->counters)
@@ -766,23 +795,24 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
 
   // 2. tree, generation by generation
   stage = "tree build";
-  tree_init_kernel<<<1, 1, 0, st>>>(n, w->lo, w->hi, w->counters);
+  tree_init_kernel<<<1, 1, 0, st>>>(n, w->lo, w->hi, w->groups, w->counters);
   const int split_grid = int(std::min<int64_t>((w->cell_cap + 255) / 256, 4 * 152));
   for (int g = 0; g < kMaxGen - 1; ++g) {
     tree_split_kernel<<<split_grid, 256, 0, st>>>(g, ncrit, w->cell_cap, codes, w->lo, w->hi,
-                                                  w->child, w->nchild, w->leaves, w->counters);
+                                                  w->child, w->nchild, w->leaves, w->groups,
+                                                  w->counters);
     tree_advance_kernel<<<1, 1, 0, st>>>(g, w->counters);
   }
   if ((e = launched(1 + 2 * (kMaxGen - 1))) != cudaSuccess) return e;
   int* hc = w->h_counters;
-  e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * (3 + kMaxGen + 1), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * kNumCounters, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
-  if (hc[2] != 0) {
+  if (hc[kCntFlags] != 0) {
     *why = "tree outgrew its cell bounds";
     return cudaErrorInvalidValue;
   }
-  const int ncells = hc[0], nleaves = hc[1];
+  const int ncells = hc[kCntCells], nleaves = hc[kCntLeaves], ngroups = hc[kCntGroups];
 
   // 3. upward pass (deepest generation first)
   const int NC = p == 2 ? ncoef(2) : p == 4 ? ncoef(4) : ncoef(6);
@@ -801,9 +831,9 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   stage = "upward pass";
   int last_gen = 0;
   for (int g = 0; g < kMaxGen; ++g)
-    if (hc[3 + g + 1] > hc[3 + g]) last_gen = g;
+    if (hc[kGenBase + g + 1] > hc[kGenBase + g]) last_gen = g;
   for (int g = last_gen; g >= 0; --g) {
-    const int cnt = hc[3 + g + 1] - hc[3 + g];
+    const int cnt = hc[kGenBase + g + 1] - hc[kGenBase + g];
     if (cnt <= 0) continue;
     if (p == 2) launch_upward<2>(w, g, cnt, ldw, st);
     else if (p == 4) launch_upward<4>(w, g, cnt, ldw, st);
@@ -818,27 +848,28 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
 
   // 4. interaction lists: count, scan, fill
   stage = "traversal";
-  const int tgrid = (nleaves + 127) / 128;
-  traverse_kernel<false><<<tgrid, 128, 0, st>>>(nleaves, w->leaves, w->child, w->nchild, w->geom,
-                                                theta, sfac, w->nfar, w->nnear, nullptr, nullptr,
-                                                nullptr, nullptr, w->counters, ncells);
+  const int tgrid = (ngroups + 127) / 128;
+  traverse_kernel<false><<<tgrid, 128, 0, st>>>(ngroups, w->groups, w->lo, w->hi, w->child,
+                                                w->nchild, w->geom, theta, sfac, w->nfar, w->nnear,
+                                                nullptr, nullptr, nullptr, nullptr, w->counters,
+                                                ncells);
   if ((e = launched(1)) != cudaSuccess) return e;
   bytes = w->cub_bytes;
-  e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nfar, w->ofar, nleaves, st);
+  e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nfar, w->ofar, ngroups, st);
   if (e == cudaSuccess) {
     bytes = w->cub_bytes;
-    e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nnear, w->onear, nleaves, st);
+    e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nnear, w->onear, ngroups, st);
   }
   if (e != cudaSuccess) return e;
   c->launches += 2;
   int tail[4];
-  e = cudaMemcpyAsync(&tail[0], w->ofar + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(&tail[0], w->ofar + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&tail[1], w->nfar + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&tail[1], w->nfar + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&tail[2], w->onear + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&tail[2], w->onear + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&tail[3], w->nnear + nleaves - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&tail[3], w->nnear + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
   const int64_t nf = int64_t(tail[0]) + tail[1], nn = int64_t(tail[2]) + tail[3];
@@ -846,52 +877,57 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   if (need > w->list_cap) {
     cudaFree(w->far_list);
     cudaFree(w->near_list);
-    w->far_list = w->near_list = nullptr;
+    w->far_list = nullptr;
+    w->near_list = nullptr;
     w->list_cap = 0;
     e = cudaMalloc(&w->far_list, need * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&w->near_list, need * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&w->near_list, need * sizeof(int2));
     if (e != cudaSuccess) return e;
     w->list_cap = need;
   }
-  traverse_kernel<true><<<tgrid, 128, 0, st>>>(nleaves, w->leaves, w->child, w->nchild, w->geom,
-                                               theta, sfac, w->nfar, w->nnear, w->ofar, w->onear,
-                                               w->far_list, w->near_list, w->counters, ncells);
+  traverse_kernel<true><<<tgrid, 128, 0, st>>>(ngroups, w->groups, w->lo, w->hi, w->child,
+                                               w->nchild, w->geom, theta, sfac, w->nfar, w->nnear,
+                                               w->ofar, w->onear, w->far_list, w->near_list,
+                                               w->counters, ncells);
   if ((e = launched(1)) != cudaSuccess) return e;
 
   // 5. near field, 6. far field + output
   stage = "near field";
   if (f64) {
     if (kernel == VPM_KERNEL_WINCKELMANS)
-      near_f64_kernel<VPM_KERNEL_WINCKELMANS><<<nleaves, kTreeBlock, 0, st>>>(
-          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, ncells,
-          w->counters);
+      near_f64_kernel<VPM_KERNEL_WINCKELMANS><<<ngroups, kTreeBlock, 0, st>>>(
+          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw,
+          ldw, n, w->counters);
     else
-      near_f64_kernel<VPM_KERNEL_GAUSSIANERF><<<nleaves, kTreeBlock, 0, st>>>(
-          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, ncells,
-          w->counters);
+      near_f64_kernel<VPM_KERNEL_GAUSSIANERF><<<ngroups, kTreeBlock, 0, st>>>(
+          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw,
+          ldw, n, w->counters);
   } else {
     if (kernel == VPM_KERNEL_WINCKELMANS)
-      near_f32_kernel<VPM_KERNEL_WINCKELMANS><<<nleaves, kTreeBlock, 0, st>>>(
-          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, ncells, w->counters);
+      near_f32_kernel<VPM_KERNEL_WINCKELMANS><<<ngroups, kTreeBlock, 0, st>>>(
+          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n,
+          w->counters);
     else
-      near_f32_kernel<VPM_KERNEL_GAUSSIANERF><<<nleaves, kTreeBlock, 0, st>>>(
-          w->leaves, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, ncells, w->counters);
+      near_f32_kernel<VPM_KERNEL_GAUSSIANERF><<<ngroups, kTreeBlock, 0, st>>>(
+          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n,
+          w->counters);
   }
   if ((e = launched(1)) != cudaSuccess) return e;
-  if (p == 2) e = launch_far<2>(w, kernel, f64, nleaves, ncells, ldw, c->U, c->J, c->ld, st);
-  else if (p == 4) e = launch_far<4>(w, kernel, f64, nleaves, ncells, ldw, c->U, c->J, c->ld, st);
-  else e = launch_far<6>(w, kernel, f64, nleaves, ncells, ldw, c->U, c->J, c->ld, st);
+  if (p == 2) e = launch_far<2>(w, kernel, f64, ngroups, ncells, ldw, c->U, c->J, c->ld, st);
+  else if (p == 4) e = launch_far<4>(w, kernel, f64, ngroups, ncells, ldw, c->U, c->J, c->ld, st);
+  else e = launch_far<6>(w, kernel, f64, ngroups, ncells, ldw, c->U, c->J, c->ld, st);
   stage = "far field";
   if ((e = e == cudaSuccess ? launched(1) : e) != cudaSuccess) return e;
-  e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * 3, cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * kGenBase, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
-  if (hc[2] != 0) {
+  if (hc[kCntFlags] != 0) {
     *why = (hc[2] & 2) ? "tree traversal stack overflow" : "treecode index out of range (checked, skipped)";
     return cudaErrorInvalidValue;
   }
   w->last_cells = ncells;
   w->last_leaves = nleaves;
+  w->last_groups = ngroups;
   w->last_far = nf;
   w->last_near = nn;
   return cudaSuccess;
