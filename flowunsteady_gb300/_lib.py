@@ -96,6 +96,10 @@ class Fmm(ctypes.Structure):
                 ("sigma_factor", ctypes.c_double)]
 
 
+FMM_STATS = ["cells", "leaves", "groups", "far_entries", "near_entries", "near_pairs",
+             "far_evaluations"]
+
+
 def default_fmm():
     f = Fmm()
     lib().vpm_fmm_default(ctypes.byref(f))
@@ -139,7 +143,7 @@ def _declare(lib):
         "vpm_centroids": (ctypes.c_int, [_vp, ctypes.c_int, P(_i64), P(_i64), _dp]),
         "vpm_fmm_default": (None, [P(Fmm)]),
         "vpm_eval_UJ_fmm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Fmm)]),
-        "vpm_fmm_stats": (ctypes.c_int, [_vp, P(_i64), P(_i64), P(_i64), P(_i64)]),
+        "vpm_fmm_stats": (ctypes.c_int, [_vp, P(_i64)]),
         "vpm_ffv_direct": (ctypes.c_int, [_vp, ctypes.c_int, _i64, _dp, _i64, _dp, _i64, _dp, _i64,
                                           _dp, _i64]),
         "vpm_uj_device_async": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,

@@ -795,10 +795,10 @@ int vpm_eval_UJ_fmm(vpm_ctx* c, int kernel, int precision, const vpm_fmm* f) {
   return VPM_OK;
 }
 
-int vpm_fmm_stats(const vpm_ctx* c, int64_t* cells, int64_t* leaves, int64_t* far_entries,
-                  int64_t* near_entries) {
+int vpm_fmm_stats(const vpm_ctx* c, int64_t* out) {
   if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
-  fmm_stats(c->fmm, cells, leaves, far_entries, near_entries);
+  if (!out) return set_error(nullptr, VPM_ERR_INVALID, "null output");
+  fmm_stats(c->fmm, out);
   return VPM_OK;
 }
 

@@ -98,8 +98,7 @@ void fmm_free(FmmWork* w);
 bool fmm_order_supported(int p);
 cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
                      double sfac, const char** why);
-void fmm_stats(const FmmWork* w, int64_t* cells, int64_t* leaves, int64_t* far_entries,
-               int64_t* near_entries);
+void fmm_stats(const FmmWork* w, int64_t* out);
 }  // namespace vpm
 
 struct vpm_ctx {

@@ -12,13 +12,15 @@
 //   3. upward pass, deepest generation first: leaves take their bounding box,
 //      largest core and moments (order P) from their particles, parents from
 //      their children (box union; moments shifted to the parent centre);
-//   4. targets are taken in groups: the largest cells with at most 64
-//      particles (and leaves that cannot be split), one CTA of 64 threads
-//      each.  One thread per group walks the tree: a cell s is far for group t
-//      when (R_t + R_s) < θ·d and d - R_t - R_s >= sigma_factor·σmax_s
-//      (d = distance of the centres), then it is evaluated from its moments;
-//      otherwise its leaves are summed directly, consecutive leaves merged
-//      into one range of particles (two passes: count, fill);
+//   4. targets are taken in groups of 64 consecutive particles of the Morton
+//      order (compact boxes, one full CTA each).  The walk for a group is
+//      split over the subtrees of a frontier of at most 73 cells (the leaves
+//      of generations 0-1 and generation 2), one thread per (group, subtree):
+//      a cell s is far for group t when (R_t + R_s) < θ·d and
+//      d - R_t - R_s >= sigma_factor·σmax_s (d = distance of the centres, FP32
+//      boxes), then it is evaluated from its moments; otherwise its leaves are
+//      summed directly, consecutive leaves merged into one range of particles
+//      (two passes: count, fill);
 //   5. the direct near field: one CTA per group over its near ranges, with the
 //      regularised kernels of the direct sum (FP32 pair routines on positions
 //      relative to the group's first particle, or FP64);
@@ -49,7 +51,8 @@ constexpr int kMaxGen = 23;        // root + at most 21 Morton digits (+1 spare)
 constexpr int kCntCells = 0, kCntLeaves = 1, kCntFlags = 2, kCntGroups = 3, kGenBase = 4;
 constexpr int kNumCounters = kGenBase + kMaxGen + 2;
 constexpr int kStack = 256;        // traversal stack (cells)
-constexpr int kTreeBlock = 64;     // threads of the near/far evaluation CTAs
+constexpr int kTreeBlock = 64;     // threads of the near/far evaluation CTAs = group size
+constexpr int kMaxFront = 1 + 8 + 64;   // walk roots: leaves of generations 0-1, generation 2
 
 // ------------------------------------------------------------- workspace --
 struct FmmWork {
@@ -71,7 +74,12 @@ struct FmmWork {
   float* momf = nullptr;      // FP32 copy
   int* leaves = nullptr;      // leaf cell ids
   int* counters = nullptr;    // see kCntCells .. kGenBase
-  int* groups = nullptr;      // target-group cell ids
+  int64_t meta_cap = 0;       // (group, frontier cell) walk slots
+  float4* ggeom = nullptr;    // target-group boxes (centre, radius), FP32
+  float4* cgeom = nullptr;    // cell boxes (centre, radius), FP32
+  float* csig = nullptr;      // largest core per cell, FP32
+  int* front = nullptr;       // frontier cells (walk roots)
+  unsigned long long* pairs = nullptr;   // [0] near source pairs, [1] far (target, cell) pairs
   double* box = nullptr;      // bounding cube: min x y z, size
   double* box_part = nullptr; // per-block min/max partials
   // interaction lists
@@ -83,14 +91,15 @@ struct FmmWork {
   int h_counters[kNumCounters];
   // statistics of the last evaluation
   int64_t last_cells = 0, last_leaves = 0, last_groups = 0, last_far = 0, last_near = 0;
+  unsigned long long h_pairs[2] = {0, 0};
 };
 
 void fmm_free(FmmWork* w) {
   if (!w) return;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
                   w->lo, w->hi, w->child, w->nchild, w->geom, w->mom, w->momf, w->leaves,
-                  w->groups, w->counters, w->box, w->box_part, w->nfar, w->nnear, w->ofar,
-                  w->onear, w->far_list, w->near_list, w->cub_tmp};
+                  w->ggeom, w->cgeom, w->csig, w->front, w->pairs, w->counters, w->box, w->box_part,
+                  w->nfar, w->nnear, w->ofar, w->onear, w->far_list, w->near_list, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   delete w;
 }
@@ -184,9 +193,7 @@ __global__ void gather_kernel(int64_t n, const int* __restrict__ perm, const dou
 }
 
 // ------------------------------------------------------------- tree build --
-// Target groups (the units of traversal and evaluation) are the largest cells
-// with at most kTreeBlock particles, and leaves that cannot be split.
-__global__ void tree_init_kernel(int64_t n, int* lo, int* hi, int* groups, int* counters) {
+__global__ void tree_init_kernel(int64_t n, int* lo, int* hi, int* counters) {
   lo[0] = 0;
   hi[0] = int(n);
   counters[kCntCells] = 1;
@@ -195,10 +202,6 @@ __global__ void tree_init_kernel(int64_t n, int* lo, int* hi, int* groups, int* 
   counters[kCntGroups] = 0;
   counters[kGenBase + 0] = 0;   // generation 0 is the root
   counters[kGenBase + 1] = 1;
-  if (n <= kTreeBlock) {
-    groups[0] = 0;
-    counters[kCntGroups] = 1;
-  }
 }
 
 __device__ __forceinline__ int lower_bound_code(const uint64_t* codes, int lo, int hi,
@@ -214,7 +217,7 @@ __device__ __forceinline__ int lower_bound_code(const uint64_t* codes, int lo, i
 // Split or close the cells of generation g.
 __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint64_t* __restrict__ codes,
                                   int* lo, int* hi, int* child, int* nchild, int* leaves,
-                                  int* groups, int* counters) {
+                                  int* counters) {
   const int begin = counters[kGenBase + g], end = counters[kGenBase + g + 1];
   for (int cell = begin + int(blockIdx.x * blockDim.x + threadIdx.x); cell < end;
        cell += int(gridDim.x * blockDim.x)) {
@@ -224,7 +227,6 @@ __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint
       child[cell] = -1;
       nchild[cell] = 0;
       leaves[atomicAdd(&counters[kCntLeaves], 1)] = cell;
-      if (b - a > kTreeBlock) groups[atomicAdd(&counters[kCntGroups], 1)] = cell;   // unsplittable
       continue;
     }
     const int bit = 63 - __clzll((long long)(first ^ last));   // highest differing bit
@@ -248,8 +250,6 @@ __global__ void tree_split_kernel(int g, int ncrit, int64_t cell_cap, const uint
       if (bounds[v + 1] > bounds[v]) {
         lo[k] = bounds[v];
         hi[k] = bounds[v + 1];
-        if (b - a > kTreeBlock && bounds[v + 1] - bounds[v] <= kTreeBlock)
-          groups[atomicAdd(&counters[kCntGroups], 1)] = k;
         ++k;
       }
     }
@@ -386,25 +386,63 @@ __global__ void moments_to_f32_kernel(int64_t n, const double* __restrict__ a, f
 }
 
 // -------------------------------------------------------------- traversal --
-// One thread per target group; FILL = false counts the far cells and near
-// source ranges, FILL = true writes them at the scanned offsets (same order).
-// Near leaves that continue the previous near range in Morton order extend it,
-// so siblings become one range of particles.
+// Targets are taken in groups of kTreeBlock consecutive particles of the Morton
+// order (the last one shorter): compact boxes, full CTAs.  Each group's box
+// (centre, radius) and each cell's (centre, radius) and largest core go to
+// FP32 records for the walk; radii are inflated by 1e-6 of the coordinates'
+// magnitude so that rounding cannot shrink them.
+__global__ void group_geom_kernel(int64_t n, const double* __restrict__ sorted, int64_t ldw,
+                                  float4* ggeom) {
+  const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t a = g * kTreeBlock;
+  if (a >= n) return;
+  const int64_t b = a + kTreeBlock < n ? a + kTreeBlock : n;
+  double bx[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = a; i < b; ++i)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double x = sorted[d * ldw + i];
+      bx[d] = fmin(bx[d], x);
+      bx[3 + d] = fmax(bx[3 + d], x);
+    }
+  double cx, cy, cz, r;
+  cell_centre(bx, cx, cy, cz, r);
+  const double pad = 1e-6 * (fabs(cx) + fabs(cy) + fabs(cz) + r);
+  ggeom[g] = make_float4(float(cx), float(cy), float(cz), float(r + pad));
+}
+
+__global__ void cell_geom_f32_kernel(int ncells, const double* __restrict__ geom, float4* cgeom,
+                                     float* csig) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  double cx, cy, cz, r;
+  cell_centre(geom + int64_t(c) * kGeom, cx, cy, cz, r);
+  const double pad = 1e-6 * (fabs(cx) + fabs(cy) + fabs(cz) + r);
+  cgeom[c] = make_float4(float(cx), float(cy), float(cz), float(r + pad));
+  csig[c] = float(geom[int64_t(c) * kGeom + 6]);
+}
+
+// One thread per (target group g, frontier cell j), t = g·nfront + j: the
+// walk of the subtree below frontier cell j for group g.  FILL = false counts
+// the far cells and near source ranges, FILL = true writes them at the
+// scanned offsets (same order); a group's lists are the concatenation over j.
+// Near leaves that continue the previous near range in Morton order extend it.
 template <bool FILL>
-__global__ void traverse_kernel(int ngroups, const int* __restrict__ groups, const int* __restrict__ lo,
+__global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restrict__ front,
+                                const float4* __restrict__ ggeom, const float4* __restrict__ cgeom,
+                                const float* __restrict__ csig, const int* __restrict__ lo,
                                 const int* __restrict__ hi, const int* __restrict__ child,
-                                const int* __restrict__ nchild, const double* __restrict__ geom,
-                                double theta, double sfac, int* nfar, int* nnear,
-                                const int* __restrict__ ofar, const int* __restrict__ onear,
-                                int* far_list, int2* near_list, int* counters, int ncells) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ngroups) return;
-  const int tc = groups[t];
-  double tx, ty, tz, tr;
-  cell_centre(geom + int64_t(tc) * kGeom, tx, ty, tz, tr);
+                                const int* __restrict__ nchild, float theta, float sfac, int* nfar,
+                                int* nnear, const int* __restrict__ ofar,
+                                const int* __restrict__ onear, int* far_list, int2* near_list,
+                                int* counters, int ncells) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= nthreads) return;
+  const int64_t g = t / nfront;
+  const float4 tg = ggeom[g];
   int stack[kStack];
   int sp = 0;
-  stack[sp++] = 0;
+  stack[sp++] = front[t % nfront];
   int cf = 0, cn = 0, last_hi = -1;
   const int of = FILL ? ofar[t] : 0, on = FILL ? onear[t] : 0;
   while (sp > 0) {
@@ -413,12 +451,10 @@ __global__ void traverse_kernel(int ngroups, const int* __restrict__ groups, con
       atomicOr(&counters[kCntFlags], 16);
       break;
     }
-    const double* gs = geom + int64_t(s) * kGeom;
-    double sx, sy, sz, sr;
-    cell_centre(gs, sx, sy, sz, sr);
-    const double dx = tx - sx, dy = ty - sy, dz = tz - sz;
-    const double d = sqrt(dx * dx + dy * dy + dz * dz);
-    if (tr + sr < theta * d && d - tr - sr >= sfac * gs[6]) {
+    const float4 cs = cgeom[s];
+    const float dx = tg.x - cs.x, dy = tg.y - cs.y, dz = tg.z - cs.z;
+    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+    if (tg.w + cs.w < theta * d && d - tg.w - cs.w >= sfac * csig[s]) {
       if (FILL) far_list[of + cf] = s;
       ++cf;
     } else if (nchild[s] == 0) {
@@ -445,65 +481,95 @@ __global__ void traverse_kernel(int ngroups, const int* __restrict__ groups, con
 }
 
 // --------------------------------------------------------------- near field --
-// One CTA per target group: the group's targets (kTreeBlock at a time, one
-// per thread) against every particle of its near source ranges, staged in
-// shared memory.  FP32: positions relative to the group's first particle from
+// One CTA per target group (one target per thread) against every particle of
+// its near source ranges, staged in shared memory.  FP32: positions relative to the group's first particle from
 // the packed records, the FP32 pair routines of the direct sum, sums folded
 // into (hi, lo) pairs after each staged block.  Raw sums (U 3, A 9, W 3) go to
 // raw[k·ldr + i] in Morton order.
 template <int KERNEL>
 __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
-    const int* __restrict__ groups, const int* __restrict__ lo, const int* __restrict__ hi,
-    const int* __restrict__ onear, const int* __restrict__ nnear, const int2* __restrict__ near_list,
-    const float4* __restrict__ rec, double* raw, int64_t ldr, int64_t n, int* counters) {
+    int nfront, const int* __restrict__ onear, const int* __restrict__ nnear,
+    const int2* __restrict__ near_list, const float4* __restrict__ rec, double* raw, int64_t ldr,
+    int64_t n, int* counters, unsigned long long* pairs) {
+  static_assert(kTreeBlock == 64, "two-warp scan below");
   __shared__ float4 sA[kTreeBlock], sB[kTreeBlock];
-  const int tid = threadIdx.x;
-  const int tc = groups[blockIdx.x];
-  const int a = lo[tc], b = hi[tc];
+  __shared__ int s_start[kTreeBlock], s_pref[kTreeBlock + 1], s_w0;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
   const float4 c0 = rec[3 * int64_t(a)], c1 = rec[3 * int64_t(a) + 1];
-  const int l0 = onear[blockIdx.x], ln = nnear[blockIdx.x];
-  for (int t0 = a; t0 < b; t0 += kTreeBlock) {
-    const int i = t0 + tid;
-    float tx[1] = {0.f}, ty[1] = {0.f}, tz[1] = {0.f};
-    if (i < b) {
-      const float4 r0 = rec[3 * int64_t(i)], r1 = rec[3 * int64_t(i) + 1];
-      tx[0] = rel_f32(r0.x, r1.x, c0.x, c1.x);
-      ty[0] = rel_f32(r0.y, r1.y, c0.y, c1.y);
-      tz[0] = rel_f32(r0.z, r1.z, c0.z, c1.z);
-    }
-    float acc[1][15], shi[15], slo[15];
+  const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
+  const int l0 = onear[t0s], ln = onear[t1s] + nnear[t1s] - l0;
+  const int i = a + tid;
+  float tx[1] = {0.f}, ty[1] = {0.f}, tz[1] = {0.f};
+  if (i < b) {
+    const float4 r0 = rec[3 * int64_t(i)], r1 = rec[3 * int64_t(i) + 1];
+    tx[0] = rel_f32(r0.x, r1.x, c0.x, c1.x);
+    ty[0] = rel_f32(r0.y, r1.y, c0.y, c1.y);
+    tz[0] = rel_f32(r0.z, r1.z, c0.z, c1.z);
+  }
+  float acc[1][15], shi[15], slo[15];
 #pragma unroll
-    for (int v = 0; v < 15; ++v) acc[0][v] = shi[v] = slo[v] = 0.f;
-    for (int l = 0; l < ln; ++l) {
-      const int2 rg = near_list[l0 + l];
-      const int sa = rg.x, sb = rg.y;
-      if (sa < 0 || sb > n || sa > sb) {   // uniform over the CTA: every thread skips it
-        if (tid == 0) atomicOr(&counters[kCntFlags], 8);
-        continue;
+  for (int v = 0; v < 15; ++v) acc[0][v] = shi[v] = slo[v] = 0.f;
+  int tiles = 0;
+  // The near ranges, kTreeBlock at a time: their lengths' prefix sums in shared
+  // memory; the concatenated sources are then staged in full tiles, each slot
+  // finding its range by binary search.
+  for (int rc0 = 0; rc0 < ln; rc0 += kTreeBlock) {
+    const int nr = min(kTreeBlock, ln - rc0);
+    int len = 0;
+    __syncthreads();   // previous chunk's tiles consumed
+    if (tid < nr) {
+      const int2 rg = near_list[l0 + rc0 + tid];
+      if (rg.x < 0 || rg.y > n || rg.x > rg.y) {
+        atomicOr(&counters[kCntFlags], 8);
+      } else {
+        len = rg.y - rg.x;
       }
-      for (int s0 = sa; s0 < sb; s0 += kTreeBlock) {
-        __syncthreads();
-        const int j = s0 + tid;
-        float4 qa, qb;
-        if (j < sb) {
-          const float4 r0 = rec[3 * int64_t(j)], r1 = rec[3 * int64_t(j) + 1],
-                       r2 = rec[3 * int64_t(j) + 2];
-          qa = make_float4(rel_f32(r0.x, r1.x, c0.x, c1.x), rel_f32(r0.y, r1.y, c0.y, c1.y),
-                           rel_f32(r0.z, r1.z, c0.z, c1.z), r0.w);
-          qb = make_float4(r2.x, r2.y, r2.z, r1.w);
-        } else {
-          qa = make_float4(0.f, 0.f, 0.f, 0.f);
-          qb = make_float4(0.f, 0.f, 0.f, 0.f);
+      s_start[tid] = rg.x;
+    }
+    int incl = len;   // inclusive scan over the 64 threads
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (tid == 31) s_w0 = incl;
+    __syncthreads();
+    if (tid >= 32) incl += s_w0;
+    s_pref[tid + 1] = incl;
+    if (tid == 0) s_pref[0] = 0;
+    __syncthreads();
+    const int total = s_pref[nr];
+    if (tid == 0 && pairs) atomicAdd(&pairs[0], (unsigned long long)total * (unsigned long long)(b - a));
+    for (int q0 = 0; q0 < total; q0 += kTreeBlock) {
+      const int q = q0 + tid;
+      float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (q < total) {
+        int lo_r = 0, hi_r = nr - 1;   // last range r with s_pref[r] <= q
+        while (lo_r < hi_r) {
+          const int mid = (lo_r + hi_r + 1) >> 1;
+          if (s_pref[mid] <= q) lo_r = mid;
+          else hi_r = mid - 1;
         }
-        sA[tid] = qa;
-        sB[tid] = qb;
-        __syncthreads();
-        const int cnt = min(kTreeBlock, sb - s0);
-        if (KERNEL == VPM_KERNEL_WINCKELMANS) {
-          for (int js = 0; js < cnt; ++js) uj_source_winck<1, true>(sA[js], sB[js], tx, ty, tz, acc);
-        } else {
-          for (int js = 0; js < cnt; ++js) uj_source_gauss<1, false>(sA[js], sB[js], tx, ty, tz, acc);
-        }
+        const int64_t j = s_start[lo_r] + (q - s_pref[lo_r]);
+        const float4 r0 = rec[3 * j], r1 = rec[3 * j + 1], r2 = rec[3 * j + 2];
+        qa = make_float4(rel_f32(r0.x, r1.x, c0.x, c1.x), rel_f32(r0.y, r1.y, c0.y, c1.y),
+                         rel_f32(r0.z, r1.z, c0.z, c1.z), r0.w);
+        qb = make_float4(r2.x, r2.y, r2.z, r1.w);
+      }
+      __syncthreads();   // previous tile consumed
+      sA[tid] = qa;
+      sB[tid] = qb;
+      __syncthreads();
+      const int cnt = min(kTreeBlock, total - q0);
+      if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+        for (int js = 0; js < cnt; ++js) uj_source_winck<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+      } else {
+        // A warp's 32 targets are consecutive along the Morton curve: a vote per
+        // source takes the far form where all of them are beyond ρ² = 50.
+        for (int js = 0; js < cnt; ++js) uj_source_gauss<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+      }
+      if (++tiles % 4 == 0) {
 #pragma unroll
         for (int v = 0; v < 15; ++v) {
           float s, e;
@@ -514,14 +580,21 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
         }
       }
     }
-    if (i < b) {
-      double v[15];
+  }
 #pragma unroll
-      for (int k = 0; k < 15; ++k) v[k] = double(shi[k]) + double(slo[k]);
-      v[11] = -(v[3] + v[7]);   // A22: the FP32 pair routines keep J trace-free
+  for (int v = 0; v < 15; ++v) {
+    float s, e;
+    two_sum(shi[v], acc[0][v], s, e);
+    shi[v] = s;
+    slo[v] += e;
+  }
+  if (i < b) {
+    double v[15];
 #pragma unroll
-      for (int k = 0; k < 15; ++k) raw[k * ldr + i] = v[k];
-    }
+    for (int k = 0; k < 15; ++k) v[k] = double(shi[k]) + double(slo[k]);
+    v[11] = -(v[3] + v[7]);   // A22: the FP32 pair routines keep J trace-free
+#pragma unroll
+    for (int k = 0; k < 15; ++k) raw[k * ldr + i] = v[k];
   }
 }
 
@@ -529,17 +602,16 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
 // first particle; pairs with r = 0 skipped as in the direct FP64 sum).
 template <int KERNEL>
 __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
-    const int* __restrict__ groups, const int* __restrict__ lo, const int* __restrict__ hi,
-    const int* __restrict__ onear, const int* __restrict__ nnear, const int2* __restrict__ near_list,
-    const double* __restrict__ sorted, int64_t ldw, double* raw, int64_t ldr, int64_t n,
-    int* counters) {
+    int nfront, const int* __restrict__ onear, const int* __restrict__ nnear,
+    const int2* __restrict__ near_list, const double* __restrict__ sorted, int64_t ldw, double* raw,
+    int64_t ldr, int64_t n, int* counters) {
   __shared__ double sx[kTreeBlock], sy[kTreeBlock], sz[kTreeBlock], sa_[kTreeBlock];
   __shared__ double sg0[kTreeBlock], sg1[kTreeBlock], sg2[kTreeBlock], sb_[kTreeBlock];
   const int tid = threadIdx.x;
-  const int tc = groups[blockIdx.x];
-  const int a = lo[tc], b = hi[tc];
+  const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
   const double cx = sorted[a], cy = sorted[ldw + a], cz = sorted[2 * ldw + a];
-  const int l0 = onear[blockIdx.x], ln = nnear[blockIdx.x];
+  const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
+  const int l0 = onear[t0s], ln = onear[t1s] + nnear[t1s] - l0;
   for (int t0 = a; t0 < b; t0 += kTreeBlock) {
     const int i = t0 + tid;
     double tx = 0.0, ty = 0.0, tz = 0.0;
@@ -605,15 +677,16 @@ __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
 // the target's original index.
 template <int P, int KERNEL, typename R, typename M>
 __global__ void __launch_bounds__(kTreeBlock) far_kernel(
-    const int* __restrict__ groups, const int* __restrict__ lo, const int* __restrict__ hi,
+    int64_t n, int nfront,
     const int* __restrict__ ofar, const int* __restrict__ nfar, const int* __restrict__ far_list,
     const double* __restrict__ geom, const M* __restrict__ mom, const double* __restrict__ sorted,
     int64_t ldw, const double* __restrict__ raw, int64_t ldr, const int* __restrict__ perm,
-    double* U, double* J, int64_t ldo, int ncells, int* counters) {
+    double* U, double* J, int64_t ldo, int ncells, int* counters, unsigned long long* pairs) {
   constexpr int NC = ncoef(P);
-  const int tc = groups[blockIdx.x];
-  const int a = lo[tc], b = hi[tc];
-  const int f0 = ofar[blockIdx.x], fn = nfar[blockIdx.x];
+  const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
+  const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
+  const int f0 = ofar[t0s], fn = ofar[t1s] + nfar[t1s] - f0;
+  if (threadIdx.x == 0) atomicAdd(&pairs[1], (unsigned long long)fn * (unsigned long long)(b - a));
   for (int i = a + int(threadIdx.x); i < b; i += kTreeBlock) {
     const double x = sorted[i], y = sorted[ldw + i], z = sorted[2 * ldw + i];
     R dp[9], dd[18];
@@ -671,8 +744,9 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   const int64_t cap = std::max<int64_t>(n, 1024);
   const int64_t cells = 2 * cap + 8;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
-                  w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->groups, w->counters,
-                  w->box, w->box_part, w->nfar, w->nnear, w->ofar, w->onear, w->cub_tmp};
+                  w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->ggeom, w->cgeom,
+                  w->csig, w->front, w->pairs, w->counters, w->box, w->box_part, w->nfar, w->nnear,
+                  w->ofar, w->onear, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   cudaError_t e = cudaSuccess;
   auto al = [&](auto*& p, size_t count) {
@@ -681,9 +755,12 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   al(w->codes, cap); al(w->codes_alt, cap); al(w->idx, cap); al(w->perm, cap);
   al(w->sorted, 7 * size_t(cap)); al(w->rec, 3 * size_t(cap)); al(w->near_raw, 15 * size_t(cap));
   al(w->lo, cells); al(w->hi, cells); al(w->child, cells); al(w->nchild, cells);
-  al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells); al(w->groups, cells);
+  const int64_t meta = (cap / kTreeBlock + 2) * kMaxFront;
+  al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells);
+  al(w->ggeom, cap / kTreeBlock + 2); al(w->cgeom, cells); al(w->csig, cells);
+  al(w->front, kMaxFront); al(w->pairs, 2);
   al(w->counters, kNumCounters); al(w->box, 4); al(w->box_part, kBoxBlocks * 6);
-  al(w->nfar, cells); al(w->nnear, cells); al(w->ofar, cells); al(w->onear, cells);
+  al(w->nfar, meta); al(w->nnear, meta); al(w->ofar, meta); al(w->onear, meta);
   if (e != cudaSuccess) {
     w->cap = 0;
     return e;
@@ -691,7 +768,7 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   size_t sort_bytes = 0, scan_bytes = 0;
   e = cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, w->codes, w->codes_alt, w->idx, w->perm,
                                       int(cap), 0, 63);
-  if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, w->nfar, w->ofar, int(cells));
+  if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, w->nfar, w->ofar, int(meta));
   if (e == cudaSuccess) {
     w->cub_bytes = std::max(sort_bytes, scan_bytes);
     e = cudaMalloc(&w->cub_tmp, w->cub_bytes);
@@ -702,6 +779,7 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   }
   w->cap = cap;
   w->cell_cap = cells;
+  w->meta_cap = meta;
   return cudaSuccess;
 }
 
@@ -713,14 +791,14 @@ void launch_upward(FmmWork* w, int g, int ncells_in_gen, int64_t ldw, cudaStream
 }
 
 template <int P>
-cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int ngroups, int ncells, int64_t ldw,
-                       double* U, double* J, int64_t ldo, cudaStream_t st) {
+cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int64_t n, int ngroups, int nfront,
+                       int ncells, int64_t ldw, double* U, double* J, int64_t ldo, cudaStream_t st) {
   const dim3 grid(ngroups), block(kTreeBlock);
 #define VPM_FAR(K, R, M, mp)                                                                        \
-  far_kernel<P, K, R, M><<<grid, block, 0, st>>>(w->groups, w->lo, w->hi, w->ofar, w->nfar,       \
+  far_kernel<P, K, R, M><<<grid, block, 0, st>>>(n, nfront, w->ofar, w->nfar,                     \
                                                  w->far_list, w->geom, mp, w->sorted, ldw,        \
                                                  w->near_raw, ldw, w->perm, U, J, ldo, ncells, \
-                                                 w->counters)
+                                                 w->counters, w->pairs)
   if (kernel == VPM_KERNEL_WINCKELMANS) {
     if (f64) VPM_FAR(VPM_KERNEL_WINCKELMANS, double, double, w->mom);
     else VPM_FAR(VPM_KERNEL_WINCKELMANS, float, float, w->momf);
@@ -736,12 +814,14 @@ cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int ngroups, int ncells
 
 bool fmm_order_supported(int p) { return p == 2 || p == 4 || p == 6; }
 
-void fmm_stats(const FmmWork* w, int64_t* cells, int64_t* leaves, int64_t* far_entries,
-               int64_t* near_entries) {
-  if (cells) *cells = w ? w->last_cells : 0;
-  if (leaves) *leaves = w ? w->last_leaves : 0;
-  if (far_entries) *far_entries = w ? w->last_far : 0;
-  if (near_entries) *near_entries = w ? w->last_near : 0;
+void fmm_stats(const FmmWork* w, int64_t* out) {
+  out[0] = w ? w->last_cells : 0;
+  out[1] = w ? w->last_leaves : 0;
+  out[2] = w ? w->last_groups : 0;
+  out[3] = w ? w->last_far : 0;
+  out[4] = w ? w->last_near : 0;
+  out[5] = w ? int64_t(w->h_pairs[0]) : 0;
+  out[6] = w ? int64_t(w->h_pairs[1]) : 0;
 }
 
 // U and J of every particle of the context by the treecode (see the header).
@@ -795,12 +875,11 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
 
   // 2. tree, generation by generation
   stage = "tree build";
-  tree_init_kernel<<<1, 1, 0, st>>>(n, w->lo, w->hi, w->groups, w->counters);
+  tree_init_kernel<<<1, 1, 0, st>>>(n, w->lo, w->hi, w->counters);
   const int split_grid = int(std::min<int64_t>((w->cell_cap + 255) / 256, 4 * 152));
   for (int g = 0; g < kMaxGen - 1; ++g) {
     tree_split_kernel<<<split_grid, 256, 0, st>>>(g, ncrit, w->cell_cap, codes, w->lo, w->hi,
-                                                  w->child, w->nchild, w->leaves, w->groups,
-                                                  w->counters);
+                                                  w->child, w->nchild, w->leaves, w->counters);
     tree_advance_kernel<<<1, 1, 0, st>>>(g, w->counters);
   }
   if ((e = launched(1 + 2 * (kMaxGen - 1))) != cudaSuccess) return e;
@@ -812,7 +891,32 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     *why = "tree outgrew its cell bounds";
     return cudaErrorInvalidValue;
   }
-  const int ncells = hc[kCntCells], nleaves = hc[kCntLeaves], ngroups = hc[kCntGroups];
+  const int ncells = hc[kCntCells], nleaves = hc[kCntLeaves];
+  const int ngroups = int((n + kTreeBlock - 1) / kTreeBlock);
+  // Walk roots: the leaves among generations 0 and 1, and generation 2.
+  int nfront = 0;
+  {
+    const int g2 = hc[kGenBase + 2], g3 = hc[kGenBase + 3];
+    std::vector<int> nch(g2);
+    e = cudaMemcpy(nch.data(), w->nchild, sizeof(int) * g2, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    int hf[kMaxFront];
+    for (int cidx = 0; cidx < g2 && nfront < kMaxFront; ++cidx)
+      if (nch[cidx] == 0) hf[nfront++] = cidx;
+    const int leaves01 = nfront;
+    for (int cidx = g2; cidx < g3 && nfront < kMaxFront; ++cidx) hf[nfront++] = cidx;
+    if (nfront == 0 || nfront != leaves01 + (g3 - g2)) {   // at most 9 + 64 by construction
+      *why = "tree frontier larger than expected";
+      return cudaErrorInvalidValue;
+    }
+    e = cudaMemcpyAsync(w->front, hf, sizeof(int) * nfront, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
+  const int64_t nwalk = int64_t(ngroups) * nfront;
+  if (nwalk > w->meta_cap) {
+    *why = "treecode walk table too small";
+    return cudaErrorInvalidValue;
+  }
 
   // 3. upward pass (deepest generation first)
   const int NC = p == 2 ? ncoef(2) : p == 4 ? ncoef(4) : ncoef(6);
@@ -846,33 +950,42 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     if ((e = launched(1)) != cudaSuccess) return e;
   }
 
+  cell_geom_f32_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, w->geom, w->cgeom, w->csig);
+  group_geom_kernel<<<(ngroups + 127) / 128, 128, 0, st>>>(n, w->sorted, ldw, w->ggeom);
+  if ((e = launched(2)) != cudaSuccess) return e;
+
   // 4. interaction lists: count, scan, fill
   stage = "traversal";
-  const int tgrid = (ngroups + 127) / 128;
-  traverse_kernel<false><<<tgrid, 128, 0, st>>>(ngroups, w->groups, w->lo, w->hi, w->child,
-                                                w->nchild, w->geom, theta, sfac, w->nfar, w->nnear,
+  const int tgrid = int((nwalk + 127) / 128);
+  traverse_kernel<false><<<tgrid, 128, 0, st>>>(nwalk, nfront, w->front, w->ggeom, w->cgeom,
+                                                w->csig, w->lo, w->hi, w->child, w->nchild,
+                                                float(theta), float(sfac), w->nfar, w->nnear,
                                                 nullptr, nullptr, nullptr, nullptr, w->counters,
                                                 ncells);
   if ((e = launched(1)) != cudaSuccess) return e;
   bytes = w->cub_bytes;
-  e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nfar, w->ofar, ngroups, st);
+  e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nfar, w->ofar, int(nwalk), st);
   if (e == cudaSuccess) {
     bytes = w->cub_bytes;
-    e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nnear, w->onear, ngroups, st);
+    e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nnear, w->onear, int(nwalk), st);
   }
   if (e != cudaSuccess) return e;
   c->launches += 2;
   int tail[4];
-  e = cudaMemcpyAsync(&tail[0], w->ofar + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(&tail[0], w->ofar + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&tail[1], w->nfar + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&tail[1], w->nfar + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&tail[2], w->onear + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&tail[2], w->onear + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&tail[3], w->nnear + ngroups - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&tail[3], w->nnear + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
   const int64_t nf = int64_t(tail[0]) + tail[1], nn = int64_t(tail[2]) + tail[3];
+  if (nf > INT32_MAX || nn > INT32_MAX) {
+    *why = "treecode interaction lists exceed 2^31 entries";
+    return cudaErrorInvalidValue;
+  }
   const int64_t need = std::max<int64_t>(std::max(nf, nn), 1);
   if (need > w->list_cap) {
     cudaFree(w->far_list);
@@ -885,40 +998,45 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     if (e != cudaSuccess) return e;
     w->list_cap = need;
   }
-  traverse_kernel<true><<<tgrid, 128, 0, st>>>(ngroups, w->groups, w->lo, w->hi, w->child,
-                                               w->nchild, w->geom, theta, sfac, w->nfar, w->nnear,
+  traverse_kernel<true><<<tgrid, 128, 0, st>>>(nwalk, nfront, w->front, w->ggeom, w->cgeom,
+                                               w->csig, w->lo, w->hi, w->child, w->nchild,
+                                               float(theta), float(sfac), w->nfar, w->nnear,
                                                w->ofar, w->onear, w->far_list, w->near_list,
                                                w->counters, ncells);
   if ((e = launched(1)) != cudaSuccess) return e;
 
   // 5. near field, 6. far field + output
   stage = "near field";
+  e = cudaMemsetAsync(w->pairs, 0, 2 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
   if (f64) {
     if (kernel == VPM_KERNEL_WINCKELMANS)
       near_f64_kernel<VPM_KERNEL_WINCKELMANS><<<ngroups, kTreeBlock, 0, st>>>(
-          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw,
-          ldw, n, w->counters);
+          nfront, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, n,
+          w->counters);
     else
       near_f64_kernel<VPM_KERNEL_GAUSSIANERF><<<ngroups, kTreeBlock, 0, st>>>(
-          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw,
-          ldw, n, w->counters);
+          nfront, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, n,
+          w->counters);
   } else {
     if (kernel == VPM_KERNEL_WINCKELMANS)
       near_f32_kernel<VPM_KERNEL_WINCKELMANS><<<ngroups, kTreeBlock, 0, st>>>(
-          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n,
-          w->counters);
+          nfront, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n, w->counters,
+          w->pairs);
     else
       near_f32_kernel<VPM_KERNEL_GAUSSIANERF><<<ngroups, kTreeBlock, 0, st>>>(
-          w->groups, w->lo, w->hi, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n,
-          w->counters);
+          nfront, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n, w->counters,
+          w->pairs);
   }
   if ((e = launched(1)) != cudaSuccess) return e;
-  if (p == 2) e = launch_far<2>(w, kernel, f64, ngroups, ncells, ldw, c->U, c->J, c->ld, st);
-  else if (p == 4) e = launch_far<4>(w, kernel, f64, ngroups, ncells, ldw, c->U, c->J, c->ld, st);
-  else e = launch_far<6>(w, kernel, f64, ngroups, ncells, ldw, c->U, c->J, c->ld, st);
+  if (p == 2) e = launch_far<2>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, c->ld, st);
+  else if (p == 4) e = launch_far<4>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, c->ld, st);
+  else e = launch_far<6>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, c->ld, st);
   stage = "far field";
   if ((e = e == cudaSuccess ? launched(1) : e) != cudaSuccess) return e;
   e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * kGenBase, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(w->h_pairs, w->pairs, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
   if (hc[kCntFlags] != 0) {

@@ -323,8 +323,9 @@ def run_fmm(args):
     for _ in range(3):
         _, t = timed(lambda: L.check(f.lib.vpm_eval_UJ_fmm(f.p, k, L.PREC_FP32C, ctypes.byref(fm)), f.p))
         ts.append(t)
-    st = [ctypes.c_int64() for _ in range(4)]
-    L.check(f.lib.vpm_fmm_stats(f.p, *[ctypes.byref(v) for v in st]), f.p)
+    st = (ctypes.c_int64 * len(L.FMM_STATS))()
+    L.check(f.lib.vpm_fmm_stats(f.p, st), f.p)
+    stats = dict(zip(L.FMM_STATS, st))
     Uf, Jf = np.empty((n, 3)), np.empty((n, 3, 3))
     L.check(f.lib.vpm_get_UJ(f.p, 0, n, L.dptr(Uf), 3, L.dptr(Jf), 9), f.p)
     _, t_direct = timed(lambda: L.check(f.lib.vpm_eval_UJ(f.p, k, L.PREC_FP32C), f.p))
@@ -350,8 +351,9 @@ def run_fmm(args):
                     "sigma_factor": fm.sigma_factor},
             "seconds_fmm": min(ts), "seconds_direct": t_direct,
             "speedup": t_direct / min(ts),
-            "cells": st[0].value, "leaves": st[1].value, "far_entries": st[2].value,
-            "near_entries": st[3].value,
+            **stats,
+            "near_sources_per_target": stats["near_pairs"] / n,
+            "far_cells_per_target": stats["far_evaluations"] / n,
             "fmm_rel_l2_U": rel_l2(Uf[idx], U64), "fmm_rel_l2_J": rel_l2(Jf[idx], J64),
             "direct_rel_l2_U": rel_l2(Ud[idx], U64), "direct_rel_l2_J": rel_l2(Jd[idx], J64)}
 

@@ -270,10 +270,11 @@ void vpm_fmm_default(vpm_fmm* f);
  * FP64).  Results as from vpm_eval_UJ (read them with vpm_get_UJ). */
 int vpm_eval_UJ_fmm(vpm_ctx* ctx, int kernel, int precision, const vpm_fmm* fmm);
 
-/* Size of the last treecode evaluation: cells, leaves, far-cell and near-leaf
- * list entries (any pointer may be NULL). */
-int vpm_fmm_stats(const vpm_ctx* ctx, int64_t* cells, int64_t* leaves, int64_t* far_entries,
-                  int64_t* near_entries);
+/* Size of the last treecode evaluation into out[VPM_FMM_STATS]: cells, leaves,
+ * target groups, far-cell list entries, near-range list entries, near
+ * (target, source) pairs, far (target, cell) evaluations. */
+enum { VPM_FMM_STATS = 7 };
+int vpm_fmm_stats(const vpm_ctx* ctx, int64_t* out);
 
 /* Σ|Γ|-weighted centroids of index ranges: for r in [0, nranges) particles
  * [starts[r], ends[r]) -> centroid out[3r..3r+2]. */

@@ -28,9 +28,10 @@ def eval_fmm(c, k, prec, f):
 
 
 def stats(c):
-    v = [ctypes.c_int64() for _ in range(4)]
-    c.rc(c.lib.vpm_fmm_stats(c.p, *[ctypes.byref(x) for x in v]))
-    return [x.value for x in v]
+    out = (ctypes.c_int64 * len(L.FMM_STATS))()
+    c.rc(c.lib.vpm_fmm_stats(c.p, out))
+    d = dict(zip(L.FMM_STATS, out))
+    return d["cells"], d["leaves"], d["far_entries"], d["near_entries"]
 
 
 def test_defaults_follow_flowunsteady():
