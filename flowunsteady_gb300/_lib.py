@@ -53,6 +53,7 @@ EXPORTS = [
     "vpm_truncate", "vpm_get_np", "vpm_get_state", "vpm_get_sfs", "vpm_eval_UJ",
     "vpm_eval_UJ_targets", "vpm_get_UJ", "vpm_eval_sfs", "vpm_step", "vpm_diagnostics",
     "vpm_centroids", "vpm_ffv_direct", "vpm_fmm_default", "vpm_eval_UJ_fmm", "vpm_fmm_stats",
+    "vpm_save", "vpm_load",
     "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
     "vpm_batch_last_error", "vpm_batch_set_stream", "vpm_batch_set_field",
     "vpm_batch_get_field", "vpm_batch_eval_UJ", "vpm_batch_get_UJ", "vpm_batch_step",
@@ -144,6 +145,8 @@ def _declare(lib):
         "vpm_fmm_default": (None, [P(Fmm)]),
         "vpm_eval_UJ_fmm": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Fmm)]),
         "vpm_fmm_stats": (ctypes.c_int, [_vp, P(_i64)]),
+        "vpm_save": (ctypes.c_int, [_vp, ctypes.c_char_p, _i64]),
+        "vpm_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
         "vpm_ffv_direct": (ctypes.c_int, [_vp, ctypes.c_int, _i64, _dp, _i64, _dp, _i64, _dp, _i64,
                                           _dp, _i64]),
         "vpm_uj_device_async": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _i64, _vp, _vp, _vp,

@@ -21,6 +21,7 @@ uploaded before the next device call.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 from typing import Callable, List, Optional, Sequence
 
@@ -350,6 +351,32 @@ def Ffv_direct(pfield: ParticleField, Xb, Gb, Sb) -> np.ndarray:
     L.check(L.lib().vpm_ffv_direct(pfield._ctx, pfield.kernel.id, Xb.shape[0], L.dptr(Xb), 3,
                                    L.dptr(Gb), 3, L.dptr(Sb), 1, L.dptr(M), 6), pfield._ctx)
     return M
+
+
+def save(pfield: ParticleField, file_name: str, *, path: str = "", num: Optional[int] = None,
+         add_num: bool = True) -> str:
+    """Write the particle field (vpm.save, src/FLOWUnsteady_simulation.jl:436-440):
+    <path>/<file_name>.pfield[.<num>].xmf and .bin (XDMF + raw FP64, see
+    vpm_save).  num defaults to the step counter when add_num; returns the
+    .xmf path."""
+    pfield._flush()
+    if num is None and add_num:
+        num = pfield.nt
+    prefix = os.path.join(path, file_name) if path else file_name
+    L.check(L.lib().vpm_save(pfield._ctx, prefix.encode(), -1 if num is None else int(num)),
+            pfield._ctx)
+    return prefix + ".pfield" + ("" if num is None else f".{int(num)}") + ".xmf"
+
+
+def read(pfield: ParticleField, file: str, *, load_time: bool = False):
+    """Restore a field written by save (vpm.read!(pfield, file; overwrite=true,
+    load_time), src/FLOWUnsteady_simulation.jl:264).  `file` is the .xmf or
+    the .bin path."""
+    if file.endswith(".xmf"):
+        file = file[:-4] + ".bin"
+    pfield._pend = []
+    L.check(L.lib().vpm_load(pfield._ctx, file.encode(), 1 if load_time else 0), pfield._ctx)
+    pfield._uj_valid = False
 
 
 def add_particle(pfield: ParticleField, X, Gamma, sigma, *, static: bool = False):

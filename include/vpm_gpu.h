@@ -276,6 +276,21 @@ int vpm_eval_UJ_fmm(vpm_ctx* ctx, int kernel, int precision, const vpm_fmm* fmm)
 enum { VPM_FMM_STATS = 7 };
 int vpm_fmm_stats(const vpm_ctx* ctx, int64_t* out);
 
+/* ------------------------------------------------------------ state files -- */
+/* Write the particle field (the role of vpm.save, src/FLOWUnsteady_simulation.jl:436-440)
+ * to <path>.pfield.<num>.bin and <path>.pfield.<num>.xmf (".<num>" left out
+ * when num < 0).  The .bin file is a 64-byte header (magic "VPMFIELD", version
+ * 1, n, n_static, t, nt) followed by X (n×3), Gamma (n×3), sigma (n), the SFS
+ * memory C (n×3) and a static flag (n), all little-endian FP64, particle-major;
+ * the .xmf file describes it for ParaView (XDMF 3, binary data items). */
+int vpm_save(vpm_ctx* ctx, const char* path, int64_t num);
+
+/* Restore a field written by vpm_save (the role of
+ * vpm.read!(pfield, file; overwrite=true, load_time), :264): replaces the
+ * particles (free, then static), their SFS memory and, when load_time != 0,
+ * the time and step counter. */
+int vpm_load(vpm_ctx* ctx, const char* bin_file, int load_time);
+
 /* Σ|Γ|-weighted centroids of index ranges: for r in [0, nranges) particles
  * [starts[r], ends[r]) -> centroid out[3r..3r+2]. */
 int vpm_centroids(vpm_ctx* ctx, int nranges, const int64_t* starts, const int64_t* ends,
