@@ -38,6 +38,8 @@ SFS_CONSTANT = 2
 SFS_CLIP_BACKSCATTER = 1
 SFS_FORCE_POSITIVE = 2
 SFS_ANALYTIC_DSIGMA = 4
+UJ_DIRECT = 0
+UJ_TREE = 1
 RELAX_NONE = 0
 RELAX_PEDRIZZETTI = 1
 
@@ -62,6 +64,12 @@ EXPORTS = [
 ]
 
 
+class Fmm(ctypes.Structure):
+    """Mirror of struct vpm_fmm (treecode settings)."""
+    _fields_ = [("p", ctypes.c_int32), ("ncrit", ctypes.c_int32), ("theta", ctypes.c_double),
+                ("sigma_factor", ctypes.c_double)]
+
+
 class Scheme(ctypes.Structure):
     """Mirror of struct vpm_scheme."""
     _fields_ = [
@@ -83,18 +91,15 @@ class Scheme(ctypes.Structure):
         ("relaxation", ctypes.c_int32),
         ("relax_nsteps", ctypes.c_int32),
         ("relax_factor", ctypes.c_double),
+        ("uj_method", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("fmm", Fmm),
     ]
 
 
 class Tile(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("tpt", ctypes.c_int32), ("chunk", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]
-
-
-class Fmm(ctypes.Structure):
-    """Mirror of struct vpm_fmm (treecode settings)."""
-    _fields_ = [("p", ctypes.c_int32), ("ncrit", ctypes.c_int32), ("theta", ctypes.c_double),
-                ("sigma_factor", ctypes.c_double)]
 
 
 FMM_STATS = ["cells", "leaves", "groups", "far_entries", "near_entries", "near_pairs",

@@ -322,6 +322,15 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
   if (s->sfs == VPM_SFS_DYNAMIC && !(s->sfs_alpha > 0.0 && s->sfs_alpha != 1.0))
     return ctx_fail(c, VPM_ERR_INVALID, "dynamic SFS needs 0 < alpha != 1");
   if (!(1.0 + 3.0 * s->f != 0.0)) return ctx_fail(c, VPM_ERR_INVALID, "bad formulation f");
+  if (s->uj_method != VPM_UJ_DIRECT && s->uj_method != VPM_UJ_TREE)
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown U/J method");
+  if (s->uj_method == VPM_UJ_TREE) {
+    if (!fmm_order_supported(s->fmm.p))
+      return ctx_fail(c, VPM_ERR_UNSUPPORTED, "expansion order not compiled (2, 4, 6)");
+    if (s->fmm.ncrit < 1 || !(s->fmm.theta > 0.0 && s->fmm.theta < 1.0) ||
+        !(s->fmm.sigma_factor >= 0.0))
+      return ctx_fail(c, VPM_ERR_INVALID, "treecode settings out of range");
+  }
   return VPM_OK;
 }
 
@@ -420,6 +429,21 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     if (e_ != cudaSuccess) return e_;                       \
   } while (0)
 
+// The plain U/J pass of a step at σ (U, J of every particle): the direct pair
+// pass, or the treecode when the scheme asks for it (synchronous; nothing to
+// plan in the dry pass).
+static cudaError_t uj_pass(vpm_ctx* c, const vpm_scheme* s) {
+  if (s->uj_method == VPM_UJ_TREE) {
+    if (c->dry) return cudaSuccess;
+    const char* why = nullptr;
+    cudaError_t e = fmm_eval(c, s->kernel, s->precision, s->fmm.p, s->fmm.ncrit, s->fmm.theta,
+                             s->fmm.sigma_factor, &why);
+    if (e != cudaSuccess && why) c->err = why;
+    return e;
+  }
+  return ctx_pair(c, PASS_UJ, s->kernel, s->precision, 0, c->n, 1.0, nullptr, c->U, c->J);
+}
+
 // U/J and the SFS pass of a stage (the first stage of a dynamic step also
 // computes C_d).  In the analytic form the first stage runs the α-derivative
 // passes (U/J + DJ, then ζ + Dζ) instead of separate passes at σ and ασ.
@@ -437,7 +461,7 @@ static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
     ENQP(c, ctx_pair(c, PASS_ZETAD, K, P, 0, n, 1.0, c->V, c->raw, nullptr, W, nullptr));
     ENQ(c, launch_estr_finish_d(n, ld, c->raw, c->J, c->Jt, s->transposed, c->E, c->Et, c->st));
   } else {
-    ENQP(c, ctx_pair(c, PASS_UJ, K, P, 0, n, 1.0, nullptr, c->U, c->J));
+    ENQP(c, uj_pass(c, s));
     if (sfs) {
       ENQ(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
       ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
@@ -498,7 +522,7 @@ static cudaError_t enqueue_step(vpm_ctx* c, const vpm_scheme* s, double dt, bool
   }
   if (relax) {
     // Relaxation after the step on a fresh U/J (vpm.pedrizzetti).
-    ENQP(c, ctx_pair(c, PASS_UJ, s->kernel, s->precision, 0, c->n, 1.0, nullptr, c->U, c->J));
+    ENQP(c, uj_pass(c, s));
     ENQ(c, launch_relax(c->n - c->n_static, c->ld, c->J, c->G, s->relax_factor, c->st));
   }
   return cudaSuccess;
@@ -554,6 +578,8 @@ void vpm_scheme_default(vpm_scheme* s) {
   s->kernel = VPM_KERNEL_GAUSSIANERF;
   s->precision = VPM_PREC_FP32C;
   s->integration = VPM_INTEGRATION_RK3;
+  s->uj_method = VPM_UJ_DIRECT;
+  vpm_fmm_default(&s->fmm);
   s->transposed = 1;
   s->f = 0.0;
   s->g = 0.2;
@@ -848,6 +874,7 @@ int vpm_step(vpm_ctx* c, double dt, const vpm_scheme* s, int64_t nsteps, int use
     return VPM_OK;
   }
   DeviceGuard dg(c->device);
+  if (s->uj_method == VPM_UJ_TREE) use_graph = 0;   // the treecode reads sizes back on the host
   if (s->sfs == VPM_SFS_DYNAMIC && (rc = ensure_test_filter(c))) return rc;
   c->dry = true;
   c->part_need = 0;

@@ -100,6 +100,22 @@ enum {
 enum { VPM_RELAX_NONE = 0, VPM_RELAX_PEDRIZZETTI = 1 };
 
 /* The scheme of one time step.  Fill with vpm_scheme_default() and edit. */
+/* Settings of the treecode evaluation (the role of FLOWVPM's UJ_fmm with
+ * vpm.FMM(p, ncrit, theta), src/FLOWUnsteady_simulation.jl:38,43). */
+typedef struct vpm_fmm {
+  int32_t p;             /* expansion order of the cell moments: 2, 4 or 6 (4)          */
+  int32_t ncrit;         /* at most this many particles per leaf cell (50)               */
+  double theta;          /* a cell is far for a target leaf when (R_t+R_s) < theta·d (0.4) */
+  double sigma_factor;   /* ... and when d - R_t - R_s >= sigma_factor·(largest σ of the
+                            cell): the far field uses the singular kernel, so this keeps
+                            regularised pairs in the direct near field (7.1: Gaussian-erf
+                            cores agree with the singular kernel to FP32 rounding there;
+                            0 = as FLOWVPM's nonzero_sigma=false)                         */
+} vpm_fmm;
+
+/* U/J evaluation of the plain pair passes of vpm_step (FLOWUnsteady's vpm_UJ). */
+enum { VPM_UJ_DIRECT = 0, VPM_UJ_TREE = 1 };
+
 typedef struct vpm_scheme {
   int32_t kernel;        /* VPM_KERNEL_*                                            */
   int32_t precision;     /* VPM_PREC_* used by every pair pass of the step          */
@@ -119,11 +135,16 @@ typedef struct vpm_scheme {
   int32_t relaxation;    /* VPM_RELAX_*                                             */
   int32_t relax_nsteps;  /* relax every this many steps                             */
   double relax_factor;   /* Pedrizzetti relaxation factor                           */
+  int32_t uj_method;     /* VPM_UJ_DIRECT, or VPM_UJ_TREE: the U/J passes (and the
+                            relaxation's) by the treecode with `fmm`; the α-derivative
+                            and ζ passes of SFS stay direct; no CUDA graphs        */
+  int32_t reserved;
+  vpm_fmm fmm;           /* treecode settings when uj_method == VPM_UJ_TREE          */
 } vpm_scheme;
 
 /* Defaults: Gaussian-erf, FP32C, RK3, transposed, rVPM (f=0, g=1/5), inviscid,
  * no SFS (alpha=0.999, rlxf=1, minC=0, maxC=1 preset for the dynamic model),
- * no relaxation. */
+ * no relaxation, direct U/J (treecode settings preset to vpm_fmm_default). */
 void vpm_scheme_default(vpm_scheme* s);
 
 /* ----------------------------------------------------------- diagnostics -- */
@@ -246,19 +267,6 @@ int vpm_ffv_direct(vpm_ctx* ctx, int kernel, int64_t nb, const double* Xb, int64
                    double* M, int64_t stride_m);
 
 /* ------------------------------------------------------------- treecode -- */
-/* Settings of the treecode evaluation (the role of FLOWVPM's UJ_fmm with
- * vpm.FMM(p, ncrit, theta), src/FLOWUnsteady_simulation.jl:38,43). */
-typedef struct vpm_fmm {
-  int32_t p;             /* expansion order of the cell moments: 2, 4 or 6 (4)          */
-  int32_t ncrit;         /* at most this many particles per leaf cell (50)               */
-  double theta;          /* a cell is far for a target leaf when (R_t+R_s) < theta·d (0.4) */
-  double sigma_factor;   /* ... and when d - R_t - R_s >= sigma_factor·(largest σ of the
-                            cell): the far field uses the singular kernel, so this keeps
-                            regularised pairs in the direct near field (7.1: Gaussian-erf
-                            cores agree with the singular kernel to FP32 rounding there;
-                            0 = as FLOWVPM's nonzero_sigma=false)                         */
-} vpm_fmm;
-
 /* p 4, ncrit 50, theta 0.4 (FLOWUnsteady's defaults), sigma_factor 7.1. */
 void vpm_fmm_default(vpm_fmm* f);
 

@@ -35,6 +35,9 @@ def test_scheme_defaults():
     assert s.kernel == L.KERNEL_GAUSSIANERF and s.precision == L.PREC_FP32C
     assert s.integration == L.INTEGRATION_RK3 and s.transposed == 1
     assert s.f == 0.0 and abs(s.g - 0.2) < 1e-15 and s.sfs_alpha == 0.999
+    # the struct's tail (treecode selection) lines up with the C layout
+    assert s.uj_method == L.UJ_DIRECT and (s.fmm.p, s.fmm.ncrit, s.fmm.theta) == (4, 50, 0.4)
+    assert s.fmm.sigma_factor == 7.1
 
 
 def test_bad_calls_are_rejected_without_launch():

@@ -101,3 +101,29 @@ def test_coincident_and_tiny_fields():
         assert rel_l2(U, Ud) <= 1e-3 and rel_l2(J, Jd) <= 1e-2
         bad = fmm(p=3)
         assert c.lib.vpm_eval_UJ_fmm(c.p, 1, L.PREC_FP32C, ctypes.byref(bad)) == L.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("sfs", [False, True])
+def test_step_with_treecode_tracks_direct_step(sfs):
+    # vpm_step with uj_method = VPM_UJ_TREE: the plain U/J passes by the
+    # treecode (the α-derivative and ζ passes of the dynamic SFS stay direct).
+    from tests.helpers import scheme
+    X, G, S = helical_wake(20000)
+    flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
+    kw = dict(kernel=1, prec=L.PREC_FP32C, nu=1e-4)
+    if sfs:
+        kw.update(sfs=L.SFS_DYNAMIC, flags=flags)
+    sd = scheme(**kw)
+    st = scheme(**kw)
+    st.uj_method = L.UJ_TREE
+    st.fmm = L.default_fmm()
+    with Ctx(20000) as a, Ctx(20000) as b:
+        a.set(X, G, S)
+        b.set(X, G, S)
+        a.step(sd, 1e-4, nsteps=3)
+        b.step(st, 1e-4, nsteps=3)
+        Xa, Ga, Sa = a.state()
+        Xb, Gb, Sb = b.state()
+    assert np.all(np.isfinite(Xb)) and np.all(np.isfinite(Gb))
+    assert np.abs(Xb - Xa).max() <= 1e-6
+    assert rel_l2(Gb, Ga) <= 1e-4 and rel_l2(Sb, Sa) <= 1e-6
