@@ -432,16 +432,52 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
 // The plain U/J pass of a step at σ (U, J of every particle): the direct pair
 // pass, or the treecode when the scheme asks for it (synchronous; nothing to
 // plan in the dry pass).
-static cudaError_t uj_pass(vpm_ctx* c, const vpm_scheme* s) {
-  if (s->uj_method == VPM_UJ_TREE) {
+static cudaError_t uj_pass(vpm_ctx* c, const vpm_scheme* s, bool direct = false) {
+  if (s->uj_method == VPM_UJ_TREE && !direct) {
     if (c->dry) return cudaSuccess;
     const char* why = nullptr;
     cudaError_t e = fmm_eval(c, s->kernel, s->precision, s->fmm.p, s->fmm.ncrit, s->fmm.theta,
-                             s->fmm.sigma_factor, &why);
+                             s->fmm.sigma_factor, nullptr, &why);
     if (e != cudaSuccess && why) c->err = why;
     return e;
   }
   return ctx_pair(c, PASS_UJ, s->kernel, s->precision, 0, c->n, 1.0, nullptr, c->U, c->J);
+}
+
+// The SFS passes can follow the treecode for Gaussian-erf cores in FP32: DJ,
+// ζ and Dζ vanish beyond the near field (7.1σ) to FP32 significance.
+static bool tree_sfs(const vpm_scheme* s) {
+  return s->uj_method == VPM_UJ_TREE && s->kernel == VPM_KERNEL_GAUSSIANERF &&
+         s->precision != VPM_PREC_FP64 && s->fmm.sigma_factor >= 7.1;
+}
+
+// U/J + DJ of the analytic dynamic SFS (stage 1).
+static cudaError_t ujd_pass(vpm_ctx* c, const vpm_scheme* s) {
+  if (tree_sfs(s)) {
+    if (c->dry) return cudaSuccess;
+    const char* why = nullptr;
+    cudaError_t e = fmm_eval(c, s->kernel, s->precision, s->fmm.p, s->fmm.ncrit, s->fmm.theta,
+                             s->fmm.sigma_factor, c->Jt, &why);
+    if (e != cudaSuccess && why) c->err = why;
+    return e;
+  }
+  return ctx_pair(c, PASS_UJD, s->kernel, s->precision, 0, c->n, 1.0, nullptr, c->U, c->J,
+                  nullptr, c->Jt);
+}
+
+// ζ sums at σ (PASS_ZETA, or PASS_ZETAD with w rows) into c->raw.
+static cudaError_t zeta_pass(vpm_ctx* c, const vpm_scheme* s, bool d, const double* W,
+                             bool direct = false) {
+  if (tree_sfs(s) && !direct) {
+    if (c->dry) return cudaSuccess;
+    const char* why = nullptr;
+    cudaError_t e = fmm_zeta(c, d, c->V, W, c->raw, &why);
+    if (e != cudaSuccess && why) c->err = why;
+    return e;
+  }
+  if (d) return ctx_pair(c, PASS_ZETAD, s->kernel, s->precision, 0, c->n, 1.0, c->V, c->raw,
+                         nullptr, W, nullptr);
+  return ctx_pair(c, PASS_ZETA, s->kernel, s->precision, 0, c->n, 1.0, c->V, c->raw, nullptr);
 }
 
 // U/J and the SFS pass of a stage (the first stage of a dynamic step also
@@ -456,15 +492,18 @@ static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
   double* W = c->V + 3 * ld;
   if (analytic) {
     // Jt := DJ, Et := DE.
-    ENQP(c, ctx_pair(c, PASS_UJD, K, P, 0, n, 1.0, nullptr, c->U, c->J, nullptr, c->Jt));
+    ENQP(c, ujd_pass(c, s));
     ENQ(c, launch_stretch_vw(n, ld, c->J, c->Jt, c->G, s->transposed, c->V, W, c->st));
-    ENQP(c, ctx_pair(c, PASS_ZETAD, K, P, 0, n, 1.0, c->V, c->raw, nullptr, W, nullptr));
+    ENQP(c, zeta_pass(c, s, true, W));
     ENQ(c, launch_estr_finish_d(n, ld, c->raw, c->J, c->Jt, s->transposed, c->E, c->Et, c->st));
   } else {
-    ENQP(c, uj_pass(c, s));
+    // The finite-difference C_d takes the difference of the passes at σ and at
+    // ασ (amplifying errors by 1/(1-α)): both come from the direct sum.
+    const bool fd = dyn0 && !analytic;
+    ENQP(c, uj_pass(c, s, fd));
     if (sfs) {
       ENQ(c, launch_stretch_v(n, ld, c->J, c->G, s->transposed, c->V, c->st));
-      ENQP(c, ctx_pair(c, PASS_ZETA, K, P, 0, n, 1.0, c->V, c->raw, nullptr));
+      ENQP(c, zeta_pass(c, s, false, nullptr, fd));
       ENQ(c, launch_estr_finish(n, ld, c->raw, c->J, s->transposed, c->E, c->st));
     }
   }
@@ -812,7 +851,8 @@ int vpm_eval_UJ_fmm(vpm_ctx* c, int kernel, int precision, const vpm_fmm* f) {
   if (rc) return rc;
   DeviceGuard dg(c->device);
   const char* why = nullptr;
-  cudaError_t e = fmm_eval(c, kernel, precision, f->p, f->ncrit, f->theta, f->sigma_factor, &why);
+  cudaError_t e =
+      fmm_eval(c, kernel, precision, f->p, f->ncrit, f->theta, f->sigma_factor, nullptr, &why);
   if (e == cudaErrorInvalidValue && why) return ctx_fail(c, VPM_ERR_CUDA, why);
   if (e != cudaSuccess)
     return cuda_fail(c, e, why ? (std::string("treecode evaluation, ") + why).c_str() : "treecode evaluation");

@@ -96,8 +96,13 @@ namespace vpm {
 struct FmmWork;
 void fmm_free(FmmWork* w);
 bool fmm_order_supported(int p);
+// U and J (and, when dj is given, the near-field α-derivative DJ: FP32
+// Gaussian-erf only) of every particle by the treecode.
 cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
-                     double sfac, const char** why);
+                     double sfac, double* dj, const char** why);
+// ζ sums over the near lists of the last fmm_eval of the same field.
+cudaError_t fmm_zeta(vpm_ctx* c, bool d, const double* vs, const double* ws, double* out,
+                     const char** why);
 void fmm_stats(const FmmWork* w, int64_t* out);
 }  // namespace vpm
 

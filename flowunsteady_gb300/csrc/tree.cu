@@ -66,7 +66,8 @@ struct FmmWork {
   int *idx = nullptr, *perm = nullptr;
   double* sorted = nullptr;   // X 3, Γ 3, σ 1 rows of length cap
   float4* rec = nullptr;      // packed FP32 source records of the sorted particles
-  double* near_raw = nullptr; // 15 raw near-field sums per sorted particle
+  double* near_raw = nullptr; // up to 27 raw near-field sums per sorted particle
+  double* vw = nullptr;       // v_q, w_q rows of the ζ passes in Morton order
   // cells
   int *lo = nullptr, *hi = nullptr, *child = nullptr, *nchild = nullptr;
   double* geom = nullptr;     // per cell: box min x y z, box max x y z, σmax, unused
@@ -91,13 +92,14 @@ struct FmmWork {
   int h_counters[kNumCounters];
   // statistics of the last evaluation
   int64_t last_cells = 0, last_leaves = 0, last_groups = 0, last_far = 0, last_near = 0;
+  int64_t last_nfront = 0, last_n = -1;
   unsigned long long h_pairs[2] = {0, 0};
 };
 
 void fmm_free(FmmWork* w) {
   if (!w) return;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
-                  w->lo, w->hi, w->child, w->nchild, w->geom, w->mom, w->momf, w->leaves,
+                  w->vw, w->lo, w->hi, w->child, w->nchild, w->geom, w->mom, w->momf, w->leaves,
                   w->ggeom, w->cgeom, w->csig, w->front, w->pairs, w->counters, w->box, w->box_part,
                   w->nfar, w->nnear, w->ofar, w->onear, w->far_list, w->near_list, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
@@ -482,17 +484,27 @@ __global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restr
 
 // --------------------------------------------------------------- near field --
 // One CTA per target group (one target per thread) against every particle of
-// its near source ranges, staged in shared memory.  FP32: positions relative to the group's first particle from
-// the packed records, the FP32 pair routines of the direct sum, sums folded
-// into (hi, lo) pairs after each staged block.  Raw sums (U 3, A 9, W 3) go to
-// raw[k·ldr + i] in Morton order.
-template <int KERNEL>
+// its near source ranges, staged in shared memory.  FP32: positions relative
+// to the group's first particle from the packed records, the FP32 pair
+// routines of the direct sum, sums folded into (hi, lo) pairs every four
+// tiles.  Raw sums go to raw[k·ldr + i] in Morton order:
+//   PASS_UJ    U 3, A 9, W 3 (with the kernel's own routines);
+//   PASS_UJD   those plus DA 9, DW 3 (Gaussian-erf: Dq, Dp vanish beyond the
+//              near field's 7.1σ to FP32 significance);
+//   PASS_ZETA  Ω 3, V 3; PASS_ZETAD also DΩ 3, DV 3 (Gaussian-erf: ζ likewise),
+//              with v_q (and w_q) taken from vw rows of the Morton order.
+template <int KERNEL, int PASS>
 __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
     int nfront, const int* __restrict__ onear, const int* __restrict__ nnear,
-    const int2* __restrict__ near_list, const float4* __restrict__ rec, double* raw, int64_t ldr,
-    int64_t n, int* counters, unsigned long long* pairs) {
+    const int2* __restrict__ near_list, const float4* __restrict__ rec,
+    const double* __restrict__ vw, int64_t ldv, double* raw, int64_t ldr, int64_t n,
+    int* counters, unsigned long long* pairs) {
   static_assert(kTreeBlock == 64, "two-warp scan below");
-  __shared__ float4 sA[kTreeBlock], sB[kTreeBlock];
+  constexpr int NV = nval_of(PASS);
+  constexpr bool UJ = PASS == PASS_UJ || PASS == PASS_UJD;
+  constexpr bool D = PASS == PASS_UJD || PASS == PASS_ZETAD;
+  __shared__ float4 sA[kTreeBlock], sB[kTreeBlock], sC[UJ ? 1 : kTreeBlock],
+      sD[D && !UJ ? kTreeBlock : 1];
   __shared__ int s_start[kTreeBlock], s_pref[kTreeBlock + 1], s_w0;
   const int tid = threadIdx.x, lane = tid & 31;
   const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
@@ -507,9 +519,9 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
     ty[0] = rel_f32(r0.y, r1.y, c0.y, c1.y);
     tz[0] = rel_f32(r0.z, r1.z, c0.z, c1.z);
   }
-  float acc[1][15], shi[15], slo[15];
+  float acc[1][NV], shi[NV], slo[NV];
 #pragma unroll
-  for (int v = 0; v < 15; ++v) acc[0][v] = shi[v] = slo[v] = 0.f;
+  for (int v = 0; v < NV; ++v) acc[0][v] = shi[v] = slo[v] = 0.f;
   int tiles = 0;
   // The near ranges, kTreeBlock at a time: their lengths' prefix sums in shared
   // memory; the concatenated sources are then staged in full tiles, each slot
@@ -543,7 +555,7 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
     if (tid == 0 && pairs) atomicAdd(&pairs[0], (unsigned long long)total * (unsigned long long)(b - a));
     for (int q0 = 0; q0 < total; q0 += kTreeBlock) {
       const int q = q0 + tid;
-      float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = qa, qc = qa, qd = qa;
       if (q < total) {
         int lo_r = 0, hi_r = nr - 1;   // last range r with s_pref[r] <= q
         while (lo_r < hi_r) {
@@ -555,23 +567,42 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
         const float4 r0 = rec[3 * j], r1 = rec[3 * j + 1], r2 = rec[3 * j + 2];
         qa = make_float4(rel_f32(r0.x, r1.x, c0.x, c1.x), rel_f32(r0.y, r1.y, c0.y, c1.y),
                          rel_f32(r0.z, r1.z, c0.z, c1.z), r0.w);
-        qb = make_float4(r2.x, r2.y, r2.z, r1.w);
+        if (UJ) {
+          qb = make_float4(r2.x, r2.y, r2.z, r1.w);
+        } else {
+          // Gaussian-erf ζ constants: a = -log2(e)/(2σ²) (as for U/J), b = ζ(0)/σ³.
+          const float is1 = r1.w;
+          qb = make_float4(r2.x, r2.y, r2.z, float(kZeta0Gauss) * is1 * is1 * is1);
+          qc = make_float4(float(vw[j]), float(vw[ldv + j]), float(vw[2 * ldv + j]), 0.f);
+          if (D) qd = make_float4(float(vw[3 * ldv + j]), float(vw[4 * ldv + j]),
+                                  float(vw[5 * ldv + j]), 0.f);
+        }
       }
       __syncthreads();   // previous tile consumed
       sA[tid] = qa;
       sB[tid] = qb;
+      if constexpr (!UJ) sC[tid] = qc;
+      if constexpr (D && !UJ) sD[tid] = qd;
       __syncthreads();
       const int cnt = min(kTreeBlock, total - q0);
-      if (KERNEL == VPM_KERNEL_WINCKELMANS) {
-        for (int js = 0; js < cnt; ++js) uj_source_winck<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+      if constexpr (PASS == PASS_UJ) {
+        if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+          for (int js = 0; js < cnt; ++js) uj_source_winck<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+        } else {
+          // A warp's 32 targets are consecutive along the Morton curve: a vote
+          // per source takes the far form where all of them are beyond ρ² = 50.
+          for (int js = 0; js < cnt; ++js) uj_source_gauss<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+        }
+      } else if constexpr (PASS == PASS_UJD) {
+        for (int js = 0; js < cnt; ++js) ujd_source_gauss<1, true>(sA[js], sB[js], tx, ty, tz, acc);
       } else {
-        // A warp's 32 targets are consecutive along the Morton curve: a vote per
-        // source takes the far form where all of them are beyond ρ² = 50.
-        for (int js = 0; js < cnt; ++js) uj_source_gauss<1, true>(sA[js], sB[js], tx, ty, tz, acc);
+        for (int js = 0; js < cnt; ++js)
+          zeta_source<VPM_KERNEL_GAUSSIANERF, 1, true, D, true>(sA[js], sB[js], sC[js],
+                                                               D ? sD[js] : sC[js], tx, ty, tz, acc);
       }
       if (++tiles % 4 == 0) {
 #pragma unroll
-        for (int v = 0; v < 15; ++v) {
+        for (int v = 0; v < NV; ++v) {
           float s, e;
           two_sum(shi[v], acc[0][v], s, e);
           shi[v] = s;
@@ -582,20 +613,41 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
     }
   }
 #pragma unroll
-  for (int v = 0; v < 15; ++v) {
+  for (int v = 0; v < NV; ++v) {
     float s, e;
     two_sum(shi[v], acc[0][v], s, e);
     shi[v] = s;
     slo[v] += e;
   }
   if (i < b) {
-    double v[15];
+    double v[NV];
 #pragma unroll
-    for (int k = 0; k < 15; ++k) v[k] = double(shi[k]) + double(slo[k]);
-    v[11] = -(v[3] + v[7]);   // A22: the FP32 pair routines keep J trace-free
+    for (int k = 0; k < NV; ++k) v[k] = double(shi[k]) + double(slo[k]);
+    if constexpr (UJ) v[11] = -(v[3] + v[7]);   // A22: the FP32 routines keep J trace-free
+    if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
 #pragma unroll
-    for (int k = 0; k < 15; ++k) raw[k * ldr + i] = v[k];
+    for (int k = 0; k < NV; ++k) raw[k * ldr + i] = v[k];
   }
+}
+
+// Rows of a Morton-ordered array back to the original order.
+__global__ void scatter_rows_kernel(int64_t n, int rows, const int* __restrict__ perm,
+                                    const double* __restrict__ src, int64_t lds, double* dst,
+                                    int64_t ldd) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = perm[i];
+  for (int r = 0; r < rows; ++r) dst[r * ldd + o] = src[r * lds + i];
+}
+
+// Rows of an array in the original order into the Morton order.
+__global__ void gather_rows_kernel(int64_t n, int rows, const int* __restrict__ perm,
+                                   const double* __restrict__ src, int64_t lds, double* dst,
+                                   int64_t ldd) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = perm[i];
+  for (int r = 0; r < rows; ++r) dst[r * ldd + i] = src[r * lds + o];
 }
 
 // FP64 near field on the sorted FP64 state (positions relative to the leaf's
@@ -675,13 +727,14 @@ __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
 // One thread per target (CTA per target group): moments of the group's far
 // cells at the target, plus the near-field raw sums; U and J are written at
 // the target's original index.
-template <int P, int KERNEL, typename R, typename M>
+template <int P, int KERNEL, typename R, typename M, bool D>
 __global__ void __launch_bounds__(kTreeBlock) far_kernel(
     int64_t n, int nfront,
     const int* __restrict__ ofar, const int* __restrict__ nfar, const int* __restrict__ far_list,
     const double* __restrict__ geom, const M* __restrict__ mom, const double* __restrict__ sorted,
     int64_t ldw, const double* __restrict__ raw, int64_t ldr, const int* __restrict__ perm,
-    double* U, double* J, int64_t ldo, int ncells, int* counters, unsigned long long* pairs) {
+    double* U, double* J, double* DJ, int64_t ldo, int ncells, int* counters,
+    unsigned long long* pairs) {
   constexpr int NC = ncoef(P);
   const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
   const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
@@ -722,6 +775,15 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
                           kp * v[9] + w1, kp * v[10] - w0, kp * v[11]};
 #pragma unroll
     for (int k = 0; k < 9; ++k) J[k * ldo + o] = -w * jn[k] + w * double(jf[k]);
+    if constexpr (D) {   // α-derivative: near field only (see near_f32_kernel)
+      const double d0 = raw[24 * ldr + i], d1 = raw[25 * ldr + i], d2 = raw[26 * ldr + i];
+      const double* a9 = raw + 15 * ldr + i;
+      const double jd[9] = {kp * a9[0],          kp * a9[ldr] + d2,     kp * a9[2 * ldr] - d1,
+                            kp * a9[3 * ldr] - d2, kp * a9[4 * ldr],    kp * a9[5 * ldr] + d0,
+                            kp * a9[6 * ldr] + d1, kp * a9[7 * ldr] - d0, kp * a9[8 * ldr]};
+#pragma unroll
+      for (int k = 0; k < 9; ++k) DJ[k * ldo + o] = -w * jd[k];
+    }
   }
 }
 
@@ -744,7 +806,7 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   const int64_t cap = std::max<int64_t>(n, 1024);
   const int64_t cells = 2 * cap + 8;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
-                  w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->ggeom, w->cgeom,
+                  w->vw, w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->ggeom, w->cgeom,
                   w->csig, w->front, w->pairs, w->counters, w->box, w->box_part, w->nfar, w->nnear,
                   w->ofar, w->onear, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
@@ -753,7 +815,8 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
     if (e == cudaSuccess) e = cudaMalloc(&p, count * sizeof(*p));
   };
   al(w->codes, cap); al(w->codes_alt, cap); al(w->idx, cap); al(w->perm, cap);
-  al(w->sorted, 7 * size_t(cap)); al(w->rec, 3 * size_t(cap)); al(w->near_raw, 15 * size_t(cap));
+  al(w->sorted, 7 * size_t(cap)); al(w->rec, 3 * size_t(cap)); al(w->near_raw, 27 * size_t(cap));
+  al(w->vw, 6 * size_t(cap));
   al(w->lo, cells); al(w->hi, cells); al(w->child, cells); al(w->nchild, cells);
   const int64_t meta = (cap / kTreeBlock + 2) * kMaxFront;
   al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells);
@@ -792,19 +855,22 @@ void launch_upward(FmmWork* w, int g, int ncells_in_gen, int64_t ldw, cudaStream
 
 template <int P>
 cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int64_t n, int ngroups, int nfront,
-                       int ncells, int64_t ldw, double* U, double* J, int64_t ldo, cudaStream_t st) {
+                       int ncells, int64_t ldw, double* U, double* J, double* DJ, int64_t ldo,
+                       cudaStream_t st) {
   const dim3 grid(ngroups), block(kTreeBlock);
-#define VPM_FAR(K, R, M, mp)                                                                        \
-  far_kernel<P, K, R, M><<<grid, block, 0, st>>>(n, nfront, w->ofar, w->nfar,                     \
-                                                 w->far_list, w->geom, mp, w->sorted, ldw,        \
-                                                 w->near_raw, ldw, w->perm, U, J, ldo, ncells, \
-                                                 w->counters, w->pairs)
-  if (kernel == VPM_KERNEL_WINCKELMANS) {
-    if (f64) VPM_FAR(VPM_KERNEL_WINCKELMANS, double, double, w->mom);
-    else VPM_FAR(VPM_KERNEL_WINCKELMANS, float, float, w->momf);
+#define VPM_FAR(K, R, M, DD, mp)                                                                   \
+  far_kernel<P, K, R, M, DD><<<grid, block, 0, st>>>(n, nfront, w->ofar, w->nfar,                 \
+                                                     w->far_list, w->geom, mp, w->sorted, ldw,    \
+                                                     w->near_raw, ldw, w->perm, U, J, DJ, ldo,    \
+                                                     ncells, w->counters, w->pairs)
+  if (DJ) {   // FP32 Gaussian-erf only (checked by the caller)
+    VPM_FAR(VPM_KERNEL_GAUSSIANERF, float, float, true, w->momf);
+  } else if (kernel == VPM_KERNEL_WINCKELMANS) {
+    if (f64) VPM_FAR(VPM_KERNEL_WINCKELMANS, double, double, false, w->mom);
+    else VPM_FAR(VPM_KERNEL_WINCKELMANS, float, float, false, w->momf);
   } else {
-    if (f64) VPM_FAR(VPM_KERNEL_GAUSSIANERF, double, double, w->mom);
-    else VPM_FAR(VPM_KERNEL_GAUSSIANERF, float, float, w->momf);
+    if (f64) VPM_FAR(VPM_KERNEL_GAUSSIANERF, double, double, false, w->mom);
+    else VPM_FAR(VPM_KERNEL_GAUSSIANERF, float, float, false, w->momf);
   }
 #undef VPM_FAR
   return cudaGetLastError();
@@ -828,7 +894,7 @@ void fmm_stats(const FmmWork* w, int64_t* out) {
 // Returns a CUDA error, or cudaErrorInvalidValue with *why set for a tree that
 // outgrew its bounds (cannot happen for the 2n + 8 cells reserved).
 cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
-                     double sfac, const char** why) {
+                     double sfac, double* dj, const char** why) {
   *why = nullptr;
   const int64_t n = c->n;
   if (n == 0) return cudaSuccess;
@@ -1019,19 +1085,26 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
           nfront, w->onear, w->nnear, w->near_list, w->sorted, ldw, w->near_raw, ldw, n,
           w->counters);
   } else {
-    if (kernel == VPM_KERNEL_WINCKELMANS)
-      near_f32_kernel<VPM_KERNEL_WINCKELMANS><<<ngroups, kTreeBlock, 0, st>>>(
-          nfront, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n, w->counters,
-          w->pairs);
+    if (dj)
+      near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_UJD><<<ngroups, kTreeBlock, 0, st>>>(
+          nfront, w->onear, w->nnear, w->near_list, w->rec, nullptr, 0, w->near_raw, ldw, n,
+          w->counters, w->pairs);
+    else if (kernel == VPM_KERNEL_WINCKELMANS)
+      near_f32_kernel<VPM_KERNEL_WINCKELMANS, PASS_UJ><<<ngroups, kTreeBlock, 0, st>>>(
+          nfront, w->onear, w->nnear, w->near_list, w->rec, nullptr, 0, w->near_raw, ldw, n,
+          w->counters, w->pairs);
     else
-      near_f32_kernel<VPM_KERNEL_GAUSSIANERF><<<ngroups, kTreeBlock, 0, st>>>(
-          nfront, w->onear, w->nnear, w->near_list, w->rec, w->near_raw, ldw, n, w->counters,
-          w->pairs);
+      near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_UJ><<<ngroups, kTreeBlock, 0, st>>>(
+          nfront, w->onear, w->nnear, w->near_list, w->rec, nullptr, 0, w->near_raw, ldw, n,
+          w->counters, w->pairs);
   }
   if ((e = launched(1)) != cudaSuccess) return e;
-  if (p == 2) e = launch_far<2>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, c->ld, st);
-  else if (p == 4) e = launch_far<4>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, c->ld, st);
-  else e = launch_far<6>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, c->ld, st);
+  if (p == 2)
+    e = launch_far<2>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj, c->ld, st);
+  else if (p == 4)
+    e = launch_far<4>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj, c->ld, st);
+  else
+    e = launch_far<6>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj, c->ld, st);
   stage = "far field";
   if ((e = e == cudaSuccess ? launched(1) : e) != cudaSuccess) return e;
   e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * kGenBase, cudaMemcpyDeviceToHost, st);
@@ -1046,9 +1119,43 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   w->last_cells = ncells;
   w->last_leaves = nleaves;
   w->last_groups = ngroups;
+  w->last_nfront = nfront;
   w->last_far = nf;
   w->last_near = nn;
+  w->last_n = n;
   return cudaSuccess;
+}
+
+// The ζ sums of a pair pass (PASS_ZETA: Ω, V; PASS_ZETAD: also DΩ, DV; raw
+// rows as the direct pass writes them) over the near lists of the last
+// treecode evaluation, which must be of the same particle positions and cores
+// (Gaussian-erf: ζ beyond the near field's 7.1σ is below FP32 significance).
+cudaError_t fmm_zeta(vpm_ctx* c, bool d, const double* vs, const double* ws, double* out,
+                     const char** why) {
+  *why = nullptr;
+  FmmWork* w = c->fmm;
+  const int64_t n = c->n;
+  if (!w || w->last_n != n || n == 0) {
+    *why = "the treecode ζ pass needs a treecode U/J evaluation of the same field";
+    return cudaErrorInvalidValue;
+  }
+  cudaStream_t st = c->st;
+  const int64_t ldw = w->cap;
+  const int ngroups = int(w->last_groups), nfront = int(w->last_nfront);
+  const int grid = int((n + 255) / 256);
+  gather_rows_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, vs, c->ld, w->vw, ldw);
+  if (d) gather_rows_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, ws, c->ld, w->vw + 3 * ldw, ldw);
+  if (d)
+    near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_ZETAD><<<ngroups, kTreeBlock, 0, st>>>(
+        nfront, w->onear, w->nnear, w->near_list, w->rec, w->vw, ldw, w->near_raw, ldw, n,
+        w->counters, nullptr);
+  else
+    near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_ZETA><<<ngroups, kTreeBlock, 0, st>>>(
+        nfront, w->onear, w->nnear, w->near_list, w->rec, w->vw, ldw, w->near_raw, ldw, n,
+        w->counters, nullptr);
+  scatter_rows_kernel<<<grid, 256, 0, st>>>(n, d ? 12 : 6, w->perm, w->near_raw, ldw, out, c->ld);
+  c->launches += d ? 4 : 3;
+  return cudaGetLastError();
 }
 
 }  // namespace vpm

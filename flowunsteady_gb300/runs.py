@@ -368,6 +368,9 @@ def run_step(args):
     X, G, S = helical_wake(n, turns=12 if n > 500000 else 4)
     f = Field(X, G, S)
     sc = scheme_for(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    if args.tree:
+        sc.uj_method = L.UJ_TREE
+        sc.fmm = L.default_fmm()
     tuned = None
     if args.autotune:
         tile, ms = L.Tile(), ctypes.c_double()
@@ -378,8 +381,9 @@ def run_step(args):
     d = f.diag(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
     f.close()
     return {"workload": f"helical wake N={n}", "steps": nsteps, "seconds": t,
-            "seconds_per_step": t / nsteps, "tile": tuned, "sigma_mean": d["sigma_mean"],
-            "nonfinite": d["nonfinite"]}
+            "seconds_per_step": t / nsteps, "tile": tuned,
+            "uj": "treecode p4 ncrit50 theta0.4" if args.tree else "direct",
+            "sigma_mean": d["sigma_mean"], "nonfinite": d["nonfinite"]}
 
 
 def main(argv=None):
@@ -392,6 +396,7 @@ def main(argv=None):
     p.add_argument("--keep", action="store_true", help="include the final state (rings)")
     p.add_argument("--no-reference", action="store_true", help="batch: skip the FP64 fields")
     p.add_argument("--autotune", action="store_true", help="step: tune the tile shapes first")
+    p.add_argument("--tree", action="store_true", help="step: U/J passes by the treecode")
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,

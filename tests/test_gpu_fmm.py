@@ -127,3 +127,33 @@ def test_step_with_treecode_tracks_direct_step(sfs):
     assert np.all(np.isfinite(Xb)) and np.all(np.isfinite(Gb))
     assert np.abs(Xb - Xa).max() <= 1e-6
     assert rel_l2(Gb, Ga) <= 1e-4 and rel_l2(Sb, Sa) <= 1e-6
+
+
+@pytest.mark.parametrize("analytic", [True, False])
+def test_sfs_passes_from_treecode_match_direct(analytic):
+    # With uj_method = VPM_UJ_TREE and Gaussian-erf FP32, the analytic SFS
+    # passes (U/J + DJ, ζ + Dζ) run over the tree's near lists; the
+    # finite-difference form keeps its σ and ασ passes on the direct sum.
+    from tests.helpers import scheme
+    X, G, S = helical_wake(20000)
+    flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE
+    if analytic:
+        flags |= L.SFS_ANALYTIC_DSIGMA
+    sd = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags)
+    st = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags)
+    st.uj_method = L.UJ_TREE
+    st.fmm = L.default_fmm()
+    with Ctx(20000) as c:
+        c.set(X, G, S)
+        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sd)))
+        C0, E0 = c.sfs()
+        U0, J0 = np.empty((20000, 3)), np.empty((20000, 3, 3))
+        c.rc(c.lib.vpm_get_UJ(c.p, 0, 20000, L.dptr(U0), 3, L.dptr(J0), 9))
+        c.set(X, G, S)
+        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(st)))
+        C1, E1 = c.sfs()
+        U1, J1 = np.empty((20000, 3)), np.empty((20000, 3, 3))
+        c.rc(c.lib.vpm_get_UJ(c.p, 0, 20000, L.dptr(U1), 3, L.dptr(J1), 9))
+    assert rel_l2(U1, U0) <= 1e-4 and rel_l2(J1, J0) <= 1e-4
+    assert rel_l2(E1, E0) <= 1e-3, rel_l2(E1, E0)
+    assert rel_l2(C1[:, 0], C0[:, 0]) <= (1e-2 if analytic else 1e-12), rel_l2(C1[:, 0], C0[:, 0])
