@@ -358,6 +358,40 @@ def run_fmm(args):
             "direct_rel_l2_U": rel_l2(Ud[idx], U64), "direct_rel_l2_J": rel_l2(Jd[idx], J64)}
 
 
+# -------------------------------------------------------------------- treestep --
+def run_treestep(args):
+    """The same helical wake stepped twice from one state: U/J and analytic
+    dynamic-SFS passes by the treecode (vpm_scheme.uj_method = VPM_UJ_TREE,
+    p=4, ncrit=50, θ=0.4) and by the direct FP32C sum; time per step of both and
+    the distance of the two trajectories after every step."""
+    n = args.n or 1048576
+    nsteps = args.steps or 10
+    dt = args.dt or 1e-4
+    X, G, S = helical_wake(n, turns=12 if n > 500000 else 4)
+    sd = scheme_for(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    st = scheme_for(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    st.uj_method = L.UJ_TREE
+    st.fmm = L.default_fmm()
+    fd, ft = Field(X, G, S), Field(X, G, S)
+    hist, td, tt = [], 0.0, 0.0
+    for k in range(nsteps):
+        _, a = timed(lambda: fd.step(sd, dt, 1))
+        _, b = timed(lambda: ft.step(st, dt, 1))
+        td += a
+        tt += b
+        Xd, Gd, Sd = fd.state()
+        Xt, Gt, St = ft.state()
+        hist.append({"step": k + 1, "max_abs_dx": float(np.abs(Xt - Xd).max()),
+                     "rel_l2_gamma": rel_l2(Gt, Gd), "rel_max_sigma": float(np.abs(St - Sd).max() / np.abs(Sd).max())})
+    dg = ft.diag(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    fd.close()
+    ft.close()
+    return {"workload": f"helical wake N={n}, dynamic SFS (analytic), nu=1e-4", "dt": dt,
+            "steps": nsteps, "seconds_per_step_direct": td / nsteps,
+            "seconds_per_step_tree": tt / nsteps, "speedup": td / tt, "history": hist,
+            "final_sigma_mean": dg["sigma_mean"], "final_nonfinite": dg["nonfinite"]}
+
+
 # ------------------------------------------------------------------------ step --
 def run_step(args):
     """k full RK3 steps (Gaussian-erf, dynamic SFS with analytic ∂/∂σ, ν = 1e-4,
@@ -388,7 +422,7 @@ def run_step(args):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("run", choices=["sweep", "rings", "batch", "large", "step", "fmm"])
+    p.add_argument("run", choices=["sweep", "rings", "batch", "large", "step", "fmm", "treestep"])
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--steps", type=int, default=None)
     p.add_argument("--fields", type=int, default=None)
@@ -400,7 +434,7 @@ def main(argv=None):
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,
-          "step": run_step, "fmm": run_fmm}[args.run]
+          "step": run_step, "fmm": run_fmm, "treestep": run_treestep}[args.run]
     res = fn(args)
     txt = json.dumps(res)
     if args.out:
