@@ -44,10 +44,11 @@ int size_bucket(int64_t n) {
 }  // namespace
 
 // Untuned shapes.  The ζ passes do ~15 instructions of pair work per source
-// against a fixed per-source cost, so they take more targets per thread.
-Shape default_shape(int pass, int precision) {
+// against a fixed per-source cost, so on large fields they take more targets
+// per thread; on small ones the smaller tiles give more target tiles to spread.
+Shape default_shape(int pass, int precision, int64_t n) {
   if (precision == VPM_PREC_FP64) return Shape{128, 1};
-  return (pass & 1) ? Shape{128, 4} : Shape{128, 2};
+  return ((pass & 1) && n >= 32768) ? Shape{128, 4} : Shape{128, 2};
 }
 
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n,
@@ -58,7 +59,7 @@ Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n,
   // the registers and keep their default shapes.
   auto it = g_tune.find(std::make_tuple(device, pass, kernel, precision, size_bucket(n)));
   if (it != g_tune.end()) return it->second;
-  return default_shape(pass, precision);
+  return default_shape(pass, precision, n);
 }
 
 void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s) {
@@ -155,6 +156,11 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   }
   return e;
 }
+
+// Below this size the far-field classification neither pays nor costs
+// measurably, and the coherence count (a memset and atomics per pass) is
+// left out: the classification then stays on.
+bool coherence_counted(int64_t n) { return n >= 65536; }
 
 bool tma_disabled() {
   static const bool off = [] {
@@ -368,10 +374,11 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     a.u = u; a.j = j; a.ldo = c->ld;
     a.part = c->part; a.ldp = c->ld;
     a.far = farfield_enabled() ? 1 : 0;
-    a.coh = c->coh;
+    a.coh = coherence_counted(c->n) ? c->coh : nullptr;
     a.coh_blocks = ceil_div(c->n, 32);
     if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
-      e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec, c->coh, c->st);
+      e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec,
+                              coherence_counted(c->n) ? c->coh : nullptr, c->st);
       if (e != cudaSuccess) return e;
       c->launches += 1;
       a.rec = c->rec;
@@ -396,11 +403,11 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   pc.u = u; pc.j = j; pc.ldo = c->ld;
   pc.ws = ws; pc.dj = dj;
   pc.status = c->status;
-  pc.coh = c->coh;
+  pc.coh = coherence_counted(c->n) ? c->coh : nullptr;
   if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
     if (!c->dry) {
       cudaError_t e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec,
-                                          c->coh, c->st);
+                                          pc.coh ? c->coh : nullptr, c->st);
       if (e != cudaSuccess) return e;
       c->launches += 1;
     }

@@ -45,7 +45,7 @@ struct PairPlan {
   int64_t chunk;
 };
 
-Shape default_shape(int pass, int precision);
+Shape default_shape(int pass, int precision, int64_t n);
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n, const Shape* pinned);
 void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s);
 int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int num_sms);

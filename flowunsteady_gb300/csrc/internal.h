@@ -85,6 +85,8 @@ bool farfield_enabled();
 // Bulk-copy staging of the packed records is on unless VPM_NO_TMA is set (to
 // non-zero); the kernels then read the records with plain loads.
 bool tma_disabled();
+// Whether the pack kernel counts compact source blocks for a field of n particles.
+bool coherence_counted(int64_t n);
 
 struct Shape {
   int block;   // threads per CTA
