@@ -79,7 +79,7 @@ __host__ __device__ constexpr size_t smem_bytes(int block, int tpt) {
 // at 128 (T=4) or 96 (T=2) registers per thread (the D form: 168 for T=2).
 template <int PASS, int PREC, int BLOCK, int T>
 constexpr int min_blocks() {
-  constexpr int regs = PASS == PASS_UJD ? (T >= 4 ? 255 : 168) : (T >= 4 ? 128 : 96);
+  constexpr int regs = PASS == PASS_UJD ? (T >= 4 ? 255 : 168) : (T >= 4 ? 168 : 96);
   return (PairTraits<PASS, PREC>::kUJ && PREC != VPM_PREC_FP64)
              ? (65536 / (BLOCK * regs) > 0 ? 65536 / (BLOCK * regs) : 1)
              : 1;
