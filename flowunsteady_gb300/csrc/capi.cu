@@ -343,6 +343,80 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
 }  // namespace
 
 // Enqueue the pair pass of one context (targets [t0,t1) of its own particles).
+// Large fields are evaluated along a Morton curve: a full-range FP32 pair pass
+// sorts the particles by the Morton code of their position, gathers the state
+// (and the ζ passes' v, w) into that order, runs the same pair pass there and
+// scatters its outputs back.  Warps' targets and staged source blocks are then
+// compact whatever the caller's particle order, so that the far-field forms of
+// the Gaussian-erf kernel apply (uniform 262,144-particle box: 112 → 87 ms).
+// Only the summation order changes; VPM_NO_SORT=1 turns it off.
+static bool sorted_pass(const vpm_ctx* c, int prec, int64_t t0, int64_t t1) {
+  static const bool off = [] {
+    const char* v = std::getenv("VPM_NO_SORT");
+    return v && v[0] && v[0] != '0';
+  }();
+  return !off && !c->bp && prec != VPM_PREC_FP64 && t0 == 0 && t1 == c->n && c->n >= 65536;
+}
+
+static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, double scale,
+                                   const double* vs, double* u, double* j, const double* ws,
+                                   double* dj) {
+  const int64_t n = c->n, ld = c->ld;
+  const bool uj = pass == PASS_UJ || pass == PASS_UJD;
+  cudaError_t e = cudaSuccess;
+  const int* perm = nullptr;
+  if (c->dry) {   // allocations happen while planning, before any capture
+    e = sort_reserve(c->sortw, c->cap);
+    if (e == cudaSuccess && !c->srt) e = cudaMalloc(&c->srt, 13 * size_t(ld) * sizeof(double));
+    if (e == cudaSuccess && !c->sout) e = cudaMalloc(&c->sout, 21 * size_t(ld) * sizeof(double));
+    if (e != cudaSuccess) return e;
+  } else {
+    if (!c->sortw || !c->srt || !c->sout) return cudaErrorInvalidValue;
+    e = sort_order(c->sortw, n, c->X, ld, c->st, &perm);
+    if (e == cudaSuccess) e = launch_gather_rows(n, 3, perm, c->X, ld, c->srt, ld, c->st);
+    if (e == cudaSuccess) e = launch_gather_rows(n, 3, perm, c->G, ld, c->srt + 3 * ld, ld, c->st);
+    if (e == cudaSuccess) e = launch_gather_rows(n, 1, perm, c->S, ld, c->srt + 6 * ld, ld, c->st);
+    if (e == cudaSuccess && vs) e = launch_gather_rows(n, 3, perm, vs, ld, c->srt + 7 * ld, ld, c->st);
+    if (e == cudaSuccess && ws) e = launch_gather_rows(n, 3, perm, ws, ld, c->srt + 10 * ld, ld, c->st);
+    if (e == cudaSuccess && uj)
+      e = launch_pack_sources(kernel, n, c->srt, c->srt + 3 * ld, c->srt + 6 * ld, ld, scale,
+                              c->rec, nullptr, c->st);
+    if (e != cudaSuccess) return e;
+    c->launches += 6 + 3 + (vs ? 1 : 0) + (ws ? 1 : 0) + (uj ? 1 : 0);
+  }
+  PairCall pc;
+  pc.pass = pass; pc.kernel = kernel; pc.prec = prec;
+  pc.t0 = 0; pc.t1 = n; pc.ns = n;
+  pc.xs = c->srt; pc.gs = c->srt + 3 * ld; pc.ss = c->srt + 6 * ld; pc.lds = ld;
+  pc.vs = vs ? c->srt + 7 * ld : nullptr;
+  pc.ws = ws ? c->srt + 10 * ld : nullptr;
+  pc.xt = c->srt; pc.ldt = ld;
+  pc.sigma_scale = scale;
+  pc.u = c->sout; pc.j = uj ? c->sout + 3 * ld : nullptr; pc.dj = dj ? c->sout + 12 * ld : nullptr;
+  pc.ldo = ld;
+  pc.status = c->status;
+  pc.coh = nullptr;
+  if (uj) pc.rec = c->rec;
+  const Shape* pinned = &c->pinned[pass & 1][kernel][prec];
+  PairPlan plan;
+  plan.n_chunk = 1;
+  e = run_pair(pc, c->device, c->num_sms, pinned, c->part, ld, c->part_elems, &c->part_need,
+               c->dry, c->st, &plan);
+  if (c->dry || e != cudaSuccess) return e;
+  c->launches += plan.n_chunk > 1 ? 2 : 1;
+  if (uj) {
+    e = launch_scatter_rows(n, 3, perm, c->sout, ld, u, ld, c->st);
+    if (e == cudaSuccess) e = launch_scatter_rows(n, 9, perm, c->sout + 3 * ld, ld, j, ld, c->st);
+    if (e == cudaSuccess && dj)
+      e = launch_scatter_rows(n, 9, perm, c->sout + 12 * ld, ld, dj, ld, c->st);
+    c->launches += dj ? 3 : 2;
+  } else {
+    e = launch_scatter_rows(n, nval_of(pass), perm, c->sout, ld, u, ld, c->st);
+    c->launches += 1;
+  }
+  return e;
+}
+
 cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int64_t t1,
                      double scale, const double* vs, double* u, double* j, const double* ws,
                      double* dj) {
@@ -394,6 +468,8 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     }
     return e;
   }
+  if (sorted_pass(c, prec, t0, t1))
+    return ctx_pair_sorted(c, pass, kernel, prec, scale, vs, u, j, ws, dj);
   PairCall pc;
   pc.pass = pass; pc.kernel = kernel; pc.prec = prec;
   pc.t0 = t0; pc.t1 = t1; pc.ns = c->n;
@@ -705,6 +781,9 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->rec);
   cudaFree(c->coh);
   vpm::fmm_free(c->fmm);
+  vpm::sort_free(c->sortw);
+  cudaFree(c->srt);
+  cudaFree(c->sout);
   cudaFree(c->status);
   cudaFree(c->red);
   if (c->h_stage) cudaFreeHost(c->h_stage);

@@ -93,6 +93,16 @@ struct BatchPlan {
 }  // namespace vpm
 
 namespace vpm {
+// Morton order of the direct pair passes of large fields (csrc/tree.cu).
+struct SortWork;
+void sort_free(SortWork* s);
+cudaError_t sort_reserve(SortWork*& s, int64_t n);
+cudaError_t sort_order(SortWork* s, int64_t n, const double* X, int64_t ld, cudaStream_t st,
+                       const int** perm);
+cudaError_t launch_gather_rows(int64_t n, int rows, const int* perm, const double* src,
+                               int64_t lds, double* dst, int64_t ldd, cudaStream_t st);
+cudaError_t launch_scatter_rows(int64_t n, int rows, const int* perm, const double* src,
+                                int64_t lds, double* dst, int64_t ldd, cudaStream_t st);
 struct FmmWork;
 void fmm_free(FmmWork* w);
 bool fmm_order_supported(int p);
@@ -133,6 +143,9 @@ struct vpm_ctx {
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
   vpm::FmmWork* fmm = nullptr;    // treecode workspace (allocated on first use)
+  vpm::SortWork* sortw = nullptr; // Morton order of the direct pair passes (large fields)
+  double* srt = nullptr;          // Morton-ordered inputs: X3 Γ3 σ1 v3 w3 (13 rows of ld)
+  double* sout = nullptr;         // Morton-ordered outputs: U3 J9 DJ9 or ζ sums (21 rows of ld)
   float4* rec = nullptr;          // packed source records, 3 per particle (FP32 U/J passes)
   unsigned int* coh = nullptr;    // compact 32-particle blocks at the last packing
   double* ffv = nullptr;          // bound particles (X3 Γ3 σ1) and M (6) rows, ffv_cap apart

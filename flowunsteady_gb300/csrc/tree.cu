@@ -1159,3 +1159,77 @@ cudaError_t fmm_zeta(vpm_ctx* c, bool d, const double* vs, const double* ws, dou
 }
 
 }  // namespace vpm
+
+// ------------------------------------------------------ Morton order of a pass --
+namespace vpm {
+
+// Buffers of the Morton order used by the direct pair passes (csrc/capi.cu):
+// codes, the permutation and CUB scratch, apart from the treecode's own.
+struct SortWork {
+  int64_t cap = 0;
+  uint64_t *codes = nullptr, *codes_alt = nullptr;
+  int *idx = nullptr, *perm = nullptr;
+  double *box = nullptr, *box_part = nullptr;
+  void* cub_tmp = nullptr;
+  size_t cub_bytes = 0;
+};
+
+void sort_free(SortWork* s) {
+  if (!s) return;
+  void* ptrs[] = {s->codes, s->codes_alt, s->idx, s->perm, s->box, s->box_part, s->cub_tmp};
+  for (void* p : ptrs) cudaFree(p);
+  delete s;
+}
+
+cudaError_t sort_reserve(SortWork*& s, int64_t n) {
+  if (!s) s = new SortWork();
+  if (n <= s->cap) return cudaSuccess;
+  void* ptrs[] = {s->codes, s->codes_alt, s->idx, s->perm, s->box, s->box_part, s->cub_tmp};
+  for (void* p : ptrs) cudaFree(p);
+  *s = SortWork();
+  cudaError_t e = cudaSuccess;
+  auto al = [&](auto*& p, size_t count) {
+    if (e == cudaSuccess) e = cudaMalloc(&p, count * sizeof(*p));
+  };
+  al(s->codes, n); al(s->codes_alt, n); al(s->idx, n); al(s->perm, n);
+  al(s->box, 4); al(s->box_part, kBoxBlocks * 6);
+  if (e == cudaSuccess)
+    e = cub::DeviceRadixSort::SortPairs(nullptr, s->cub_bytes, s->codes, s->codes_alt, s->idx,
+                                        s->perm, int(n), 0, 63);
+  if (e == cudaSuccess) e = cudaMalloc(&s->cub_tmp, s->cub_bytes);
+  if (e != cudaSuccess) return e;
+  s->cap = n;
+  return cudaSuccess;
+}
+
+// perm = the particles of X (rows of leading dimension ld) along a Morton curve
+// of their bounding cube; 6 launches plus the radix sort's, no host sync.
+cudaError_t sort_order(SortWork* s, int64_t n, const double* X, int64_t ld, cudaStream_t st,
+                       const int** perm) {
+  box_partial_kernel<<<kBoxBlocks, 256, 0, st>>>(n, X, ld, s->box_part);
+  box_final_kernel<<<1, 1, 0, st>>>(s->box_part, kBoxBlocks, s->box);
+  morton_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, X, ld, s->box, s->codes, s->idx);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  size_t bytes = s->cub_bytes;
+  e = cub::DeviceRadixSort::SortPairs(s->cub_tmp, bytes, s->codes, s->codes_alt, s->idx, s->perm,
+                                      int(n), 0, 63, st);
+  *perm = s->perm;
+  return e;
+}
+
+cudaError_t launch_gather_rows(int64_t n, int rows, const int* perm, const double* src,
+                               int64_t lds, double* dst, int64_t ldd, cudaStream_t st) {
+  if (n <= 0 || rows <= 0) return cudaSuccess;
+  gather_rows_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, rows, perm, src, lds, dst, ldd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_rows(int64_t n, int rows, const int* perm, const double* src,
+                                int64_t lds, double* dst, int64_t ldd, cudaStream_t st) {
+  if (n <= 0 || rows <= 0) return cudaSuccess;
+  scatter_rows_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, rows, perm, src, lds, dst, ldd);
+  return cudaGetLastError();
+}
+
+}  // namespace vpm
