@@ -343,19 +343,63 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
 }  // namespace
 
 // Enqueue the pair pass of one context (targets [t0,t1) of its own particles).
-// Large fields are evaluated along a Morton curve: a full-range FP32 pair pass
-// sorts the particles by the Morton code of their position, gathers the state
-// (and the ζ passes' v, w) into that order, runs the same pair pass there and
-// scatters its outputs back.  Warps' targets and staged source blocks are then
-// compact whatever the caller's particle order, so that the far-field forms of
-// the Gaussian-erf kernel apply (uniform 262,144-particle box: 112 → 87 ms).
-// Only the summation order changes; VPM_NO_SORT=1 turns it off.
-static bool sorted_pass(const vpm_ctx* c, int prec, int64_t t0, int64_t t1) {
+// Large fields and batches are evaluated along a Morton curve: a full-range
+// FP32 pair pass sorts the particles by the Morton code of their position
+// (each field of a batch in its own cube and its own index range), gathers the
+// state (and the ζ passes' v, w) into that order, runs the same pair pass there
+// and scatters its outputs back.  Warps' targets and staged source blocks are
+// then compact whatever the caller's particle order, so that the far-field
+// forms of the Gaussian-erf kernel apply (uniform 262,144-particle box: 114 →
+// 88 ms).  Only the summation order changes; VPM_NO_SORT=1 turns it off.
+static bool sort_disabled() {
   static const bool off = [] {
     const char* v = std::getenv("VPM_NO_SORT");
     return v && v[0] && v[0] != '0';
   }();
-  return !off && !c->bp && prec != VPM_PREC_FP64 && t0 == 0 && t1 == c->n && c->n >= 65536;
+  return off;
+}
+
+static bool sorted_pass(const vpm_ctx* c, int prec, int64_t t0, int64_t t1) {
+  return !sort_disabled() && !c->bp && prec != VPM_PREC_FP64 && t0 == 0 && t1 == c->n &&
+         c->n >= 65536;
+}
+
+static bool sorted_batch(int prec) { return !sort_disabled() && prec != VPM_PREC_FP64; }
+
+// Scratch of the sorted passes (allocated while planning, before any capture):
+// c->srt rows 0-2 X, 3-5 Γ, 6 σ, 7-9 v, 10-12 w; c->sout rows 0-2 U (or the ζ
+// sums), 3-11 J, 12-20 DJ.
+static cudaError_t sort_scratch(vpm_ctx* c, int nfields) {
+  cudaError_t e = sort_reserve(c->sortw, c->cap, nfields);
+  if (e == cudaSuccess && !c->srt) e = cudaMalloc(&c->srt, 13 * size_t(c->ld) * sizeof(double));
+  if (e == cudaSuccess && !c->sout) e = cudaMalloc(&c->sout, 21 * size_t(c->ld) * sizeof(double));
+  return e;
+}
+
+static cudaError_t gather_inputs(vpm_ctx* c, const int* perm, const double* vs, const double* ws) {
+  const int64_t n = c->n, ld = c->ld;
+  cudaError_t e = launch_gather_rows(n, 3, perm, c->X, ld, c->srt, ld, c->st);
+  if (e == cudaSuccess) e = launch_gather_rows(n, 3, perm, c->G, ld, c->srt + 3 * ld, ld, c->st);
+  if (e == cudaSuccess) e = launch_gather_rows(n, 1, perm, c->S, ld, c->srt + 6 * ld, ld, c->st);
+  if (e == cudaSuccess && vs) e = launch_gather_rows(n, 3, perm, vs, ld, c->srt + 7 * ld, ld, c->st);
+  if (e == cudaSuccess && ws) e = launch_gather_rows(n, 3, perm, ws, ld, c->srt + 10 * ld, ld, c->st);
+  c->launches += 3 + (vs ? 1 : 0) + (ws ? 1 : 0);
+  return e;
+}
+
+static cudaError_t scatter_outputs(vpm_ctx* c, int pass, const int* perm, double* u, double* j,
+                                   double* dj) {
+  const int64_t n = c->n, ld = c->ld;
+  if (pass == PASS_UJ || pass == PASS_UJD) {
+    cudaError_t e = launch_scatter_rows(n, 3, perm, c->sout, ld, u, ld, c->st);
+    if (e == cudaSuccess) e = launch_scatter_rows(n, 9, perm, c->sout + 3 * ld, ld, j, ld, c->st);
+    if (e == cudaSuccess && dj)
+      e = launch_scatter_rows(n, 9, perm, c->sout + 12 * ld, ld, dj, ld, c->st);
+    c->launches += dj ? 3 : 2;
+    return e;
+  }
+  c->launches += 1;
+  return launch_scatter_rows(n, nval_of(pass), perm, c->sout, ld, u, ld, c->st);
 }
 
 static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, double scale,
@@ -365,24 +409,18 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
   const bool uj = pass == PASS_UJ || pass == PASS_UJD;
   cudaError_t e = cudaSuccess;
   const int* perm = nullptr;
-  if (c->dry) {   // allocations happen while planning, before any capture
-    e = sort_reserve(c->sortw, c->cap);
-    if (e == cudaSuccess && !c->srt) e = cudaMalloc(&c->srt, 13 * size_t(ld) * sizeof(double));
-    if (e == cudaSuccess && !c->sout) e = cudaMalloc(&c->sout, 21 * size_t(ld) * sizeof(double));
+  if (c->dry) {
+    e = sort_scratch(c, 1);
     if (e != cudaSuccess) return e;
   } else {
     if (!c->sortw || !c->srt || !c->sout) return cudaErrorInvalidValue;
     e = sort_order(c->sortw, n, c->X, ld, c->st, &perm);
-    if (e == cudaSuccess) e = launch_gather_rows(n, 3, perm, c->X, ld, c->srt, ld, c->st);
-    if (e == cudaSuccess) e = launch_gather_rows(n, 3, perm, c->G, ld, c->srt + 3 * ld, ld, c->st);
-    if (e == cudaSuccess) e = launch_gather_rows(n, 1, perm, c->S, ld, c->srt + 6 * ld, ld, c->st);
-    if (e == cudaSuccess && vs) e = launch_gather_rows(n, 3, perm, vs, ld, c->srt + 7 * ld, ld, c->st);
-    if (e == cudaSuccess && ws) e = launch_gather_rows(n, 3, perm, ws, ld, c->srt + 10 * ld, ld, c->st);
+    if (e == cudaSuccess) e = gather_inputs(c, perm, vs, ws);
     if (e == cudaSuccess && uj)
       e = launch_pack_sources(kernel, n, c->srt, c->srt + 3 * ld, c->srt + 6 * ld, ld, scale,
                               c->rec, nullptr, c->st);
     if (e != cudaSuccess) return e;
-    c->launches += 6 + 3 + (vs ? 1 : 0) + (ws ? 1 : 0) + (uj ? 1 : 0);
+    c->launches += 3 + (uj ? 1 : 0);
   }
   PairCall pc;
   pc.pass = pass; pc.kernel = kernel; pc.prec = prec;
@@ -404,17 +442,7 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
                c->dry, c->st, &plan);
   if (c->dry || e != cudaSuccess) return e;
   c->launches += plan.n_chunk > 1 ? 2 : 1;
-  if (uj) {
-    e = launch_scatter_rows(n, 3, perm, c->sout, ld, u, ld, c->st);
-    if (e == cudaSuccess) e = launch_scatter_rows(n, 9, perm, c->sout + 3 * ld, ld, j, ld, c->st);
-    if (e == cudaSuccess && dj)
-      e = launch_scatter_rows(n, 9, perm, c->sout + 12 * ld, ld, dj, ld, c->st);
-    c->launches += dj ? 3 : 2;
-  } else {
-    e = launch_scatter_rows(n, nval_of(pass), perm, c->sout, ld, u, ld, c->st);
-    c->launches += 1;
-  }
-  return e;
+  return scatter_outputs(c, pass, perm, u, j, dj);
 }
 
 cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int64_t t1,
@@ -434,25 +462,42 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     const int nv = nval_of(pass);
     const size_t need = bp->max_chunks > 1 ? size_t(bp->max_chunks) * nv * size_t(c->ld) : 0;
     c->part_need = std::max(c->part_need, need);
-    if (c->dry) return cudaSuccess;
+    const bool srt = sorted_batch(prec);
+    if (c->dry) return srt ? sort_scratch(c, bp->nfields) : cudaSuccess;
     if (need > c->part_elems) return cudaErrorMemoryAllocation;
-    cudaError_t e = cudaMemsetAsync(bp->d_counter, 0, sizeof(unsigned int), c->st);
+    const int64_t ld = c->ld;
+    const double *xs = c->X, *gs = c->G, *ss = c->S, *vq = vs, *wq = ws;
+    double *uo = u, *jo = j, *djo = dj;
+    const int* perm = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (srt) {
+      if (!c->sortw || !c->srt || !c->sout) return cudaErrorInvalidValue;
+      e = sort_order_fields(c->sortw, c->n, c->X, ld, bp->d_foff, bp->nfields, c->st, &perm);
+      if (e == cudaSuccess) e = gather_inputs(c, perm, vs, ws);
+      if (e != cudaSuccess) return e;
+      c->launches += 2;
+      xs = c->srt; gs = c->srt + 3 * ld; ss = c->srt + 6 * ld;
+      vq = vs ? c->srt + 7 * ld : nullptr;
+      wq = ws ? c->srt + 10 * ld : nullptr;
+      uo = c->sout; jo = j ? c->sout + 3 * ld : nullptr; djo = dj ? c->sout + 12 * ld : nullptr;
+    }
+    unsigned int* coh = !srt && coherence_counted(c->n) ? c->coh : nullptr;
+    e = cudaMemsetAsync(bp->d_counter, 0, sizeof(unsigned int), c->st);
     if (e != cudaSuccess) return e;
     PairArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.xs = c->X; a.gs = c->G; a.ss = c->S; a.vs = vs; a.ws = ws; a.lds = c->ld;
-    a.xt = c->X; a.ldt = c->ld;
+    a.xs = xs; a.gs = gs; a.ss = ss; a.vs = vq; a.ws = wq; a.lds = ld;
+    a.xt = xs; a.ldt = ld;
     a.sigma_scale = scale;
-    a.dj = dj;
+    a.dj = djo;
     a.items = bp->d_items; a.n_items = bp->n_items; a.counter = bp->d_counter;
-    a.u = u; a.j = j; a.ldo = c->ld;
-    a.part = c->part; a.ldp = c->ld;
+    a.u = uo; a.j = jo; a.ldo = ld;
+    a.part = c->part; a.ldp = ld;
     a.far = farfield_enabled() ? 1 : 0;
-    a.coh = coherence_counted(c->n) ? c->coh : nullptr;
+    a.coh = coh;
     a.coh_blocks = ceil_div(c->n, 32);
     if (prec != VPM_PREC_FP64 && (pass == PASS_UJ || pass == PASS_UJD)) {
-      e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec,
-                              coherence_counted(c->n) ? c->coh : nullptr, c->st);
+      e = launch_pack_sources(kernel, c->n, xs, gs, ss, ld, scale, c->rec, coh, c->st);
       if (e != cudaSuccess) return e;
       c->launches += 1;
       a.rec = c->rec;
@@ -462,11 +507,12 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     if (e != cudaSuccess) return e;
     c->launches += 1;
     if (bp->max_chunks > 1) {
-      e = launch_reduce(pass, kernel, c->part, c->ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
-                        0, c->n, u, j, dj, c->ld, c->st);
+      e = launch_reduce(pass, kernel, c->part, ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
+                        0, c->n, uo, jo, djo, ld, c->st);
       c->launches += 1;
+      if (e != cudaSuccess) return e;
     }
-    return e;
+    return srt ? scatter_outputs(c, pass, perm, u, j, dj) : cudaSuccess;
   }
   if (sorted_pass(c, prec, t0, t1))
     return ctx_pair_sorted(c, pass, kernel, prec, scale, vs, u, j, ws, dj);

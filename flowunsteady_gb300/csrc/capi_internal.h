@@ -96,9 +96,12 @@ namespace vpm {
 // Morton order of the direct pair passes of large fields (csrc/tree.cu).
 struct SortWork;
 void sort_free(SortWork* s);
-cudaError_t sort_reserve(SortWork*& s, int64_t n);
+cudaError_t sort_reserve(SortWork*& s, int64_t n, int nfields = 1);
 cudaError_t sort_order(SortWork* s, int64_t n, const double* X, int64_t ld, cudaStream_t st,
                        const int** perm);
+// Batches: each field (offsets foff) along the Morton curve of its own cube.
+cudaError_t sort_order_fields(SortWork* s, int64_t n, const double* X, int64_t ld,
+                              const int64_t* foff, int nfields, cudaStream_t st, const int** perm);
 cudaError_t launch_gather_rows(int64_t n, int rows, const int* perm, const double* src,
                                int64_t lds, double* dst, int64_t ldd, cudaStream_t st);
 cudaError_t launch_scatter_rows(int64_t n, int rows, const int* perm, const double* src,

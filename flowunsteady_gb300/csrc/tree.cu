@@ -139,18 +139,33 @@ __global__ void box_partial_kernel(int64_t n, const double* __restrict__ X, int6
     for (int d = 0; d < 6; ++d) part[blockIdx.x * 6 + d] = s[d][0];
 }
 
+// One block of kBoxBlocks threads, one per partial box.
 __global__ void box_final_kernel(const double* part, int nblocks, double* box) {
-  double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-  for (int b = 0; b < nblocks; ++b)
-    for (int d = 0; d < 3; ++d) {
-      v[d] = fmin(v[d], part[b * 6 + d]);
-      v[3 + d] = fmax(v[3 + d], part[b * 6 + 3 + d]);
+  __shared__ double s[6][kBoxBlocks];
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    s[d][t] = t < nblocks ? part[t * 6 + d] : INFINITY;
+    s[3 + d][t] = t < nblocks ? part[t * 6 + 3 + d] : -INFINITY;
+  }
+  __syncthreads();
+  for (int o = kBoxBlocks / 2; o > 0; o >>= 1) {
+    if (t < o) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        s[d][t] = fmin(s[d][t], s[d][t + o]);
+        s[3 + d][t] = fmax(s[3 + d][t], s[3 + d][t + o]);
+      }
     }
-  const double size = fmax(fmax(v[3] - v[0], v[4] - v[1]), v[5] - v[2]);
-  box[0] = v[0];
-  box[1] = v[1];
-  box[2] = v[2];
-  box[3] = size > 0 ? size * (1.0 + 1e-9) : 1.0;
+    __syncthreads();
+  }
+  if (t == 0) {
+    const double size = fmax(fmax(s[3][0] - s[0][0], s[4][0] - s[1][0]), s[5][0] - s[2][0]);
+    box[0] = s[0][0];
+    box[1] = s[1][0];
+    box[2] = s[2][0];
+    box[3] = size > 0 ? size * (1.0 + 1e-9) : 1.0;
+  }
 }
 
 // Spread the low 21 bits of v to every third bit (Morton interleaving).
@@ -921,7 +936,7 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
 
   // 1. codes, sort, gather
   box_partial_kernel<<<kBoxBlocks, 256, 0, st>>>(n, c->X, c->ld, w->box_part);
-  box_final_kernel<<<1, 1, 0, st>>>(w->box_part, kBoxBlocks, w->box);
+  box_final_kernel<<<1, kBoxBlocks, 0, st>>>(w->box_part, kBoxBlocks, w->box);
   morton_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, c->X, c->ld, w->box, w->codes, w->idx);
   if ((e = launched(3)) != cudaSuccess) return e;
   size_t bytes = w->cub_bytes;
@@ -1167,24 +1182,28 @@ namespace vpm {
 // codes, the permutation and CUB scratch, apart from the treecode's own.
 struct SortWork {
   int64_t cap = 0;
+  int fcap = 0;                          // fields the per-field boxes hold
   uint64_t *codes = nullptr, *codes_alt = nullptr;
   int *idx = nullptr, *perm = nullptr;
   double *box = nullptr, *box_part = nullptr;
+  double* fbox = nullptr;                // 4 per field: corner, cube edge
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
 };
 
 void sort_free(SortWork* s) {
   if (!s) return;
-  void* ptrs[] = {s->codes, s->codes_alt, s->idx, s->perm, s->box, s->box_part, s->cub_tmp};
+  void* ptrs[] = {s->codes, s->codes_alt, s->idx, s->perm, s->box, s->box_part, s->fbox, s->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   delete s;
 }
 
-cudaError_t sort_reserve(SortWork*& s, int64_t n) {
+cudaError_t sort_reserve(SortWork*& s, int64_t n, int nfields) {
   if (!s) s = new SortWork();
-  if (n <= s->cap) return cudaSuccess;
-  void* ptrs[] = {s->codes, s->codes_alt, s->idx, s->perm, s->box, s->box_part, s->cub_tmp};
+  if (n <= s->cap && nfields <= s->fcap) return cudaSuccess;
+  n = std::max(n, s->cap);
+  nfields = std::max(nfields, std::max(s->fcap, 1));
+  void* ptrs[] = {s->codes, s->codes_alt, s->idx, s->perm, s->box, s->box_part, s->fbox, s->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   *s = SortWork();
   cudaError_t e = cudaSuccess;
@@ -1192,28 +1211,112 @@ cudaError_t sort_reserve(SortWork*& s, int64_t n) {
     if (e == cudaSuccess) e = cudaMalloc(&p, count * sizeof(*p));
   };
   al(s->codes, n); al(s->codes_alt, n); al(s->idx, n); al(s->perm, n);
-  al(s->box, 4); al(s->box_part, kBoxBlocks * 6);
+  al(s->box, 4); al(s->box_part, kBoxBlocks * 6); al(s->fbox, 4 * size_t(nfields));
   if (e == cudaSuccess)
     e = cub::DeviceRadixSort::SortPairs(nullptr, s->cub_bytes, s->codes, s->codes_alt, s->idx,
-                                        s->perm, int(n), 0, 63);
+                                        s->perm, int(n), 0, 64);
   if (e == cudaSuccess) e = cudaMalloc(&s->cub_tmp, s->cub_bytes);
   if (e != cudaSuccess) return e;
   s->cap = n;
+  s->fcap = nfields;
   return cudaSuccess;
 }
 
 // perm = the particles of X (rows of leading dimension ld) along a Morton curve
-// of their bounding cube; 6 launches plus the radix sort's, no host sync.
+// of their bounding cube, to 2^10 cells per axis (the top 30 bits of the code;
+// ties keep their index order); 3 launches plus the radix sort's, no host sync.
 cudaError_t sort_order(SortWork* s, int64_t n, const double* X, int64_t ld, cudaStream_t st,
                        const int** perm) {
   box_partial_kernel<<<kBoxBlocks, 256, 0, st>>>(n, X, ld, s->box_part);
-  box_final_kernel<<<1, 1, 0, st>>>(s->box_part, kBoxBlocks, s->box);
+  box_final_kernel<<<1, kBoxBlocks, 0, st>>>(s->box_part, kBoxBlocks, s->box);
   morton_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, X, ld, s->box, s->codes, s->idx);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   size_t bytes = s->cub_bytes;
   e = cub::DeviceRadixSort::SortPairs(s->cub_tmp, bytes, s->codes, s->codes_alt, s->idx, s->perm,
-                                      int(n), 0, 63, st);
+                                      int(n), 33, 63, st);
+  *perm = s->perm;
+  return e;
+}
+
+// Bounding cube of field f (particles [foff[f], foff[f+1]) or [foff[f], n)),
+// one block per field.
+__global__ void field_box_kernel(int64_t n, const int64_t* __restrict__ foff, int nfields,
+                                 const double* __restrict__ X, int64_t ld, double* fbox) {
+  __shared__ double s[6][256];
+  const int f = blockIdx.x, t = threadIdx.x;
+  const int64_t i0 = foff[f], i1 = f + 1 < nfields ? foff[f + 1] : n;
+  double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = i0 + t; i < i1; i += blockDim.x)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double x = X[d * ld + i];
+      v[d] = fmin(v[d], x);
+      v[3 + d] = fmax(v[3 + d], x);
+    }
+#pragma unroll
+  for (int d = 0; d < 6; ++d) s[d][t] = v[d];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (t < o) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        s[d][t] = fmin(s[d][t], s[d][t + o]);
+        s[3 + d][t] = fmax(s[3 + d][t], s[3 + d][t + o]);
+      }
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const double size = fmax(fmax(s[3][0] - s[0][0], s[4][0] - s[1][0]), s[5][0] - s[2][0]);
+    const bool any = i1 > i0;
+    fbox[4 * f + 0] = any ? s[0][0] : 0.0;
+    fbox[4 * f + 1] = any ? s[1][0] : 0.0;
+    fbox[4 * f + 2] = any ? s[2][0] : 0.0;
+    fbox[4 * f + 3] = any && size > 0 ? size * (1.0 + 1e-9) : 1.0;
+  }
+}
+
+// Key of particle i: its field in the high bits, then the top 30 bits of its
+// Morton code in the field's own cube.
+__global__ void morton_fields_kernel(int64_t n, const double* __restrict__ X, int64_t ld,
+                                     const int64_t* __restrict__ foff, int nfields,
+                                     const double* __restrict__ fbox, uint64_t* codes, int* idx) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int lo = 0, hi = nfields - 1;   // the last field whose offset is <= i
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (foff[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  const double* b = fbox + 4 * lo;
+  const double scale = double(1 << 10) / b[3];
+  uint64_t q[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double t = floor((X[d * ld + i] - b[d]) * scale);
+    q[d] = uint64_t(fmin(fmax(t, 0.0), double((1 << 10) - 1)));
+  }
+  codes[i] = uint64_t(lo) << 30 | spread3(q[0]) << 2 | spread3(q[1]) << 1 | spread3(q[2]);
+  idx[i] = int(i);
+}
+
+// perm for a batch of fields laid out one after another: each field's
+// particles along the Morton curve of its own cube, within its own range.
+cudaError_t sort_order_fields(SortWork* s, int64_t n, const double* X, int64_t ld,
+                              const int64_t* foff, int nfields, cudaStream_t st, const int** perm) {
+  if (nfields > s->fcap || n > s->cap) return cudaErrorInvalidValue;
+  field_box_kernel<<<nfields, 256, 0, st>>>(n, foff, nfields, X, ld, s->fbox);
+  morton_fields_kernel<<<int((n + 255) / 256), 256, 0, st>>>(n, X, ld, foff, nfields, s->fbox,
+                                                            s->codes, s->idx);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int bits = 30;
+  while (bits < 64 && (uint64_t(nfields - 1) >> (bits - 30)) != 0) ++bits;
+  size_t bytes = s->cub_bytes;
+  e = cub::DeviceRadixSort::SortPairs(s->cub_tmp, bytes, s->codes, s->codes_alt, s->idx, s->perm,
+                                      int(n), 0, bits, st);
   *perm = s->perm;
   return e;
 }
