@@ -286,6 +286,67 @@ __device__ __forceinline__ void accum_pair(float dx, float dy, float dz, float q
   acc[14] = fmaf(q, gz, acc[14]);
 }
 
+// ---- packed FP32 -------------------------------------------------------------
+// For an even number of targets per thread the routines below work on target
+// pairs (k, k+1) with the packed FP32 instructions of sm_100+ (add/mul/fma
+// .rn.f32x2): each lane rounds exactly as the scalar instruction does, and one
+// issue slot carries two pair updates.  The SFU approximations stay scalar.
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// One staged source as broadcast pairs: -x (for the differences), Γ and -Γ.
+struct Src2 {
+  float2 nx, ny, nz, gx, gy, gz, ngx, ngy, ngz;
+  __device__ __forceinline__ Src2(const float4 sa, const float4 sb)
+      : nx(bc2(-sa.x)), ny(bc2(-sa.y)), nz(bc2(-sa.z)), gx(bc2(sb.x)), gy(bc2(sb.y)),
+        gz(bc2(sb.z)), ngx(bc2(-sb.x)), ngy(bc2(-sb.y)), ngz(bc2(-sb.z)) {}
+};
+
+// acc[k][v] += a.x·b.x, acc[k+1][v] += a.y·b.y.
+template <int T, int NV>
+__device__ __forceinline__ void fma_acc2(float (&acc)[T][NV], int k, int v, float2 a, float2 b) {
+  const float2 r = fma2(a, b, make_float2(acc[k][v], acc[k + 1][v]));
+  acc[k][v] = r.x;
+  acc[k + 1][v] = r.y;
+}
+
+// Differences and r² of targets (k, k+1) to the source.
+template <int T>
+__device__ __forceinline__ void diff2(const float (&tx)[T], const float (&ty)[T],
+                                      const float (&tz)[T], int k, const Src2& s, float2& dx,
+                                      float2& dy, float2& dz, float2& r2) {
+  dx = add2(make_float2(tx[k], tx[k + 1]), s.nx);
+  dy = add2(make_float2(ty[k], ty[k + 1]), s.ny);
+  dz = add2(make_float2(tz[k], tz[k + 1]), s.nz);
+  r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+}
+
+// accum_pair for targets (k, k+1).
+template <int T, int NV>
+__device__ __forceinline__ void accum_pair2(float2 dx, float2 dy, float2 dz, float2 q, float2 p,
+                                            const Src2& s, float (&acc)[T][NV], int k) {
+  const float2 c0 = fma2(dz, s.ngy, mul2(dy, s.gz));
+  const float2 c1 = fma2(dx, s.ngz, mul2(dz, s.gx));
+  const float2 c2 = fma2(dy, s.ngx, mul2(dx, s.gy));
+  fma_acc2(acc, k, 0, q, c0);
+  fma_acc2(acc, k, 1, q, c1);
+  fma_acc2(acc, k, 2, q, c2);
+  const float2 p0 = mul2(p, c0), p1 = mul2(p, c1), p2 = mul2(p, c2);
+  fma_acc2(acc, k, 3, p0, dx);
+  fma_acc2(acc, k, 4, p0, dy);
+  fma_acc2(acc, k, 5, p0, dz);
+  fma_acc2(acc, k, 6, p1, dx);
+  fma_acc2(acc, k, 7, p1, dy);
+  fma_acc2(acc, k, 8, p1, dz);
+  fma_acc2(acc, k, 9, p2, dx);
+  fma_acc2(acc, k, 10, p2, dy);
+  fma_acc2(acc, k, 12, q, s.gx);
+  fma_acc2(acc, k, 13, q, s.gy);
+  fma_acc2(acc, k, 14, q, s.gz);
+}
+
 // Winckelmans: source quads (x, y, z, σ²) and (Γx, Γy, Γz, 3/2 σ²).  MASK drops
 // coincident pairs; the kernel sets it only for source tiles that can hold a
 // target's own particle (the kernel is finite at r = 0, so an unmasked
@@ -295,24 +356,114 @@ __device__ __forceinline__ void uj_source_winck(const float4 sa, const float4 sb
                                                 const float (&tx)[T], const float (&ty)[T],
                                                 const float (&tz)[T], float (&acc)[T][15]) {
   const float s2 = sa.w, k15 = sb.w, k25 = sa.w + sb.w;
+  if constexpr (T % 2 == 0) {
+    const Src2 s(sa, sb);
+    const float2 s2p = bc2(s2), k15p = bc2(k15), k25p = bc2(k25);
 #pragma unroll
-  for (int k = 0; k < T; ++k) {
-    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float rs = rsqrt_ftz(r2 + s2);
-    const float rs2 = rs * rs;
-    const float rs3 = rs2 * rs;
-    const float rs5 = rs3 * rs2;
-    const float rs7 = rs5 * rs2;
-    float q = fmaf(k15, rs5, rs3);
-    if (MASK) q = r2 > 0.f ? q : 0.f;
-    const float p = fmaf(k25, rs7, rs5);
-    accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
+    for (int k = 0; k < T; k += 2) {
+      float2 dx, dy, dz, r2;
+      diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
+      const float2 h = add2(r2, s2p);
+      const float2 rs = make_float2(rsqrt_ftz(h.x), rsqrt_ftz(h.y));
+      const float2 rs2 = mul2(rs, rs);
+      const float2 rs3 = mul2(rs2, rs);
+      const float2 rs5 = mul2(rs3, rs2);
+      const float2 rs7 = mul2(rs5, rs2);
+      float2 q = fma2(k15p, rs5, rs3);
+      if (MASK) {
+        q.x = r2.x > 0.f ? q.x : 0.f;
+        q.y = r2.y > 0.f ? q.y : 0.f;
+      }
+      const float2 p = fma2(k25p, rs7, rs5);
+      accum_pair2(dx, dy, dz, q, p, s, acc, k);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float rs = rsqrt_ftz(r2 + s2);
+      const float rs2 = rs * rs;
+      const float rs3 = rs2 * rs;
+      const float rs5 = rs3 * rs2;
+      const float rs7 = rs5 * rs2;
+      float q = fmaf(k15, rs5, rs3);
+      if (MASK) q = r2 > 0.f ? q : 0.f;
+      const float p = fmaf(k25, rs7, rs5);
+      accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
+    }
   }
 }
 
 constexpr float kArgFar = float(-0.5 * kLog2e * 50.0);
 constexpr float kArgZero = -128.f;
+
+// uj_source_gauss on target pairs (T even; see "packed FP32").  g = 1 - e·h
+// with h = kc·r + f is formed as fma(e, -h, 1), and -h from the negated
+// coefficients, which rounds exactly as the scalar form.
+template <int T, bool VOTE>
+__device__ __forceinline__ void uj_source_gauss_x2(const float4 sa, const float4 sb,
+                                                   const float (&tx)[T], const float (&ty)[T],
+                                                   const float (&tz)[T], float (&acc)[T][15],
+                                                   float kt, float kc, float k3) {
+  constexpr int H = T / 2;
+  const Src2 s(sa, sb);
+  const float2 ea = bc2(sa.w), one = bc2(1.f), m3 = bc2(-3.f);
+  float2 dx[H], dy[H], dz[H], arg[H], ri[H], q[H], p[H];
+  float amax = -INFINITY;
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    float2 r2;
+    diff2(tx, ty, tz, 2 * m, s, dx[m], dy[m], dz[m], r2);
+    arg[m] = mul2(r2, ea);
+    amax = fmaxf(amax, fmaxf(arg[m].x, arg[m].y));
+    ri[m] = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+    q[m] = r2;   // r², until the general form below replaces it by q
+  }
+  if (VOTE && __all_sync(0xffffffffu, amax <= kArgFar)) {
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const float2 ri2 = mul2(ri[m], ri[m]);
+      const float2 qq = mul2(ri2, ri[m]);
+      accum_pair2(dx[m], dy[m], dz[m], qq, mul2(mul2(m3, qq), ri2), s, acc, 2 * m);
+    }
+    return;
+  }
+  const float2 ktp = bc2(kt), nkc = bc2(-kc), k3p = bc2(k3);
+  const float2 nA4 = bc2(-kErfcxA4), nA3 = bc2(-kErfcxA3), nA2 = bc2(-kErfcxA2),
+               nA1 = bc2(-kErfcxA1);
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    const float2 r = mul2(q[m], ri[m]);   // q holds r² here
+    const float2 e = make_float2(ex2_ftz(arg[m].x), ex2_ftz(arg[m].y));
+    const float2 u = fma2(ktp, r, one);
+    const float2 t = make_float2(rcp_ftz(u.x), rcp_ftz(u.y));
+    const float2 nf = mul2(t, fma2(t, fma2(t, fma2(t, nA4, nA3), nA2), nA1));
+    const float2 g = fma2(e, fma2(nkc, r, nf), one);
+    const float2 ri2 = mul2(ri[m], ri[m]);
+    q[m] = mul2(g, mul2(ri2, ri[m]));
+    p[m] = mul2(fma2(m3, q[m], mul2(k3p, e)), ri2);
+  }
+  if (__any_sync(0xffffffffu, amax > kArgSeries)) {
+    const float is1 = sb.w, is2 = is1 * is1, is3 = is2 * is1, is5 = is3 * is2;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float a = h ? arg[m].y : arg[m].x;
+        if (a > kArgSeries) {
+          float h1, h2;
+          GaussSeries<float, 10>::eval(a * kArgToRho2, h1, h2);
+          const bool self = a == 0.f;
+          const float qs = self ? 0.f : h1 * is3, ps = self ? 0.f : h2 * is5;
+          if (h) { q[m].y = qs; p[m].y = ps; } else { q[m].x = qs; p[m].x = ps; }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < H; ++m) accum_pair2(dx[m], dy[m], dz[m], q[m], p[m], s, acc, 2 * m);
+}
 
 // Gaussian-erf: source quads (x, y, z, -log2(e)/(2σ²)) and (Γx, Γy, Γz, 1/σ).
 // All T targets take the erf-free form, and a warp vote sends the rare warps
@@ -329,6 +480,10 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
   const float kt = kErfcxP * is1;                      // t = 1/(1 + kt r)
   const float kc = float(kSqrt2overPi) * is1;          // √(2/π) ρ = kc r
   const float k3 = float(kSqrt2overPi) * is1 * is1 * is1;
+  if constexpr (T % 2 == 0) {
+    uj_source_gauss_x2<T, VOTE>(sa, sb, tx, ty, tz, acc, kt, kc, k3);
+    return;
+  }
   float dx[T], dy[T], dz[T], arg[T], q[T], p[T];
   float amax = -INFINITY;
   if constexpr (VOTE) {
@@ -422,15 +577,29 @@ template <int T, int NV>
 __device__ __forceinline__ void uj_source_gauss_far(const float4 sa, const float4 sb,
                                                     const float (&tx)[T], const float (&ty)[T],
                                                     const float (&tz)[T], float (&acc)[T][NV]) {
+  if constexpr (T % 2 == 0) {
+    const Src2 s(sa, sb);
+    const float2 m3 = bc2(-3.f);
 #pragma unroll
-  for (int k = 0; k < T; ++k) {
-    const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float ri = rsqrt_ftz(r2);
-    const float ri2 = ri * ri;
-    const float q = ri2 * ri;
-    const float p = (-3.f * q) * ri2;
-    accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
+    for (int k = 0; k < T; k += 2) {
+      float2 dx, dy, dz, r2;
+      diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
+      const float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+      const float2 ri2 = mul2(ri, ri);
+      const float2 q = mul2(ri2, ri);
+      accum_pair2(dx, dy, dz, q, mul2(mul2(m3, q), ri2), s, acc, k);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+      const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float ri = rsqrt_ftz(r2);
+      const float ri2 = ri * ri;
+      const float q = ri2 * ri;
+      const float p = (-3.f * q) * ri2;
+      accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
+    }
   }
 }
 
