@@ -749,10 +749,164 @@ __device__ __forceinline__ void accum_pair_d(float dx, float dy, float dz, float
   acc[26] = fmaf(dq, gz, acc[26]);
 }
 
+// accum_pair_d for targets (k, k+1) (see "packed FP32").
+template <int T>
+__device__ __forceinline__ void accum_pair_d2(float2 dx, float2 dy, float2 dz, float2 q, float2 p,
+                                              float2 dq, float2 dp, const Src2& s,
+                                              float (&acc)[T][27], int k) {
+  const float2 c0 = fma2(dz, s.ngy, mul2(dy, s.gz));
+  const float2 c1 = fma2(dx, s.ngz, mul2(dz, s.gx));
+  const float2 c2 = fma2(dy, s.ngx, mul2(dx, s.gy));
+  fma_acc2(acc, k, 0, q, c0);
+  fma_acc2(acc, k, 1, q, c1);
+  fma_acc2(acc, k, 2, q, c2);
+  float2 a0 = mul2(p, c0), a1 = mul2(p, c1), a2 = mul2(p, c2);
+  fma_acc2(acc, k, 3, a0, dx);
+  fma_acc2(acc, k, 4, a0, dy);
+  fma_acc2(acc, k, 5, a0, dz);
+  fma_acc2(acc, k, 6, a1, dx);
+  fma_acc2(acc, k, 7, a1, dy);
+  fma_acc2(acc, k, 8, a1, dz);
+  fma_acc2(acc, k, 9, a2, dx);
+  fma_acc2(acc, k, 10, a2, dy);
+  fma_acc2(acc, k, 12, q, s.gx);
+  fma_acc2(acc, k, 13, q, s.gy);
+  fma_acc2(acc, k, 14, q, s.gz);
+  a0 = mul2(dp, c0); a1 = mul2(dp, c1); a2 = mul2(dp, c2);
+  fma_acc2(acc, k, 15, a0, dx);
+  fma_acc2(acc, k, 16, a0, dy);
+  fma_acc2(acc, k, 17, a0, dz);
+  fma_acc2(acc, k, 18, a1, dx);
+  fma_acc2(acc, k, 19, a1, dy);
+  fma_acc2(acc, k, 20, a1, dz);
+  fma_acc2(acc, k, 21, a2, dx);
+  fma_acc2(acc, k, 22, a2, dy);
+  fma_acc2(acc, k, 24, dq, s.gx);
+  fma_acc2(acc, k, 25, dq, s.gy);
+  fma_acc2(acc, k, 26, dq, s.gz);
+}
+
+template <int T, bool MASK>
+__device__ __forceinline__ void ujd_source_winck_x2(const float4 sa, const float4 sb,
+                                                    const float (&tx)[T], const float (&ty)[T],
+                                                    const float (&tz)[T], float (&acc)[T][27]) {
+  const float s2 = sa.w;
+  const Src2 s(sa, sb);
+  const float2 s2p = bc2(s2), k15 = bc2(sb.w), k25 = bc2(sa.w + sb.w);
+  const float2 c75 = bc2(-7.5f * s2 * s2), c175 = bc2(-17.5f * s2 * s2);
+#pragma unroll
+  for (int k = 0; k < T; k += 2) {
+    float2 dx, dy, dz, r2;
+    diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
+    const float2 h = add2(r2, s2p);
+    const float2 rs = make_float2(rsqrt_ftz(h.x), rsqrt_ftz(h.y));
+    const float2 rs2 = mul2(rs, rs);
+    const float2 rs3 = mul2(rs2, rs);
+    const float2 rs5 = mul2(rs3, rs2);
+    const float2 rs7 = mul2(rs5, rs2);
+    float2 q = fma2(k15, rs5, rs3);
+    float2 dq = mul2(c75, rs7);
+    if (MASK) {
+      q.x = r2.x > 0.f ? q.x : 0.f;
+      q.y = r2.y > 0.f ? q.y : 0.f;
+      dq.x = r2.x > 0.f ? dq.x : 0.f;
+      dq.y = r2.y > 0.f ? dq.y : 0.f;
+    }
+    const float2 p = fma2(k25, rs7, rs5);
+    const float2 dp = mul2(c175, mul2(rs7, rs2));
+    accum_pair_d2(dx, dy, dz, q, p, dq, dp, s, acc, k);
+  }
+}
+
+template <int T, bool VOTE>
+__device__ __forceinline__ void ujd_source_gauss_x2(const float4 sa, const float4 sb,
+                                                    const float (&tx)[T], const float (&ty)[T],
+                                                    const float (&tz)[T], float (&acc)[T][27]) {
+  constexpr int H = T / 2;
+  const float is1 = sb.w, is2 = is1 * is1;
+  const float k3 = float(kSqrt2overPi) * is2 * is1;
+  const Src2 s(sa, sb);
+  const float2 ea = bc2(sa.w), one = bc2(1.f), m3 = bc2(-3.f), k3p = bc2(k3), is2p = bc2(is2);
+  float2 dx[H], dy[H], dz[H], r2[H], ri[H], arg[H], q[H], p[H], dq[H], dp[H];
+  float amax = -INFINITY;
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    diff2(tx, ty, tz, 2 * m, s, dx[m], dy[m], dz[m], r2[m]);
+    arg[m] = mul2(r2[m], ea);
+    amax = fmaxf(amax, fmaxf(arg[m].x, arg[m].y));
+    ri[m] = make_float2(rsqrt_ftz(r2[m].x), rsqrt_ftz(r2[m].y));
+  }
+  if (VOTE && __all_sync(0xffffffffu, amax <= kArgFar)) {
+    const bool zero = __all_sync(0xffffffffu, amax <= kArgZero);
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const float2 ri2 = mul2(ri[m], ri[m]);
+      const float2 qq = mul2(ri2, ri[m]);
+      const float2 pp = mul2(mul2(m3, qq), ri2);
+      if (zero) {
+        accum_pair2(dx[m], dy[m], dz[m], qq, pp, s, acc, 2 * m);
+      } else {
+        const float2 k3e = mul2(k3p, make_float2(ex2_ftz(arg[m].x), ex2_ftz(arg[m].y)));
+        accum_pair_d2(dx[m], dy[m], dz[m], qq, pp, make_float2(-k3e.x, -k3e.y), mul2(k3e, is2p),
+                      s, acc, 2 * m);
+      }
+    }
+    return;
+  }
+  const float2 ktp = bc2(kErfcxP * is1), nkc = bc2(-float(kSqrt2overPi) * is1);
+  const float2 nA4 = bc2(-kErfcxA4), nA3 = bc2(-kErfcxA3), nA2 = bc2(-kErfcxA2),
+               nA1 = bc2(-kErfcxA1);
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    const float2 r = mul2(r2[m], ri[m]);
+    const float2 e = make_float2(ex2_ftz(arg[m].x), ex2_ftz(arg[m].y));
+    const float2 u = fma2(ktp, r, one);
+    const float2 t = make_float2(rcp_ftz(u.x), rcp_ftz(u.y));
+    const float2 nf = mul2(t, fma2(t, fma2(t, fma2(t, nA4, nA3), nA2), nA1));
+    const float2 g = fma2(e, fma2(nkc, r, nf), one);
+    const float2 ri2 = mul2(ri[m], ri[m]);
+    const float2 k3e = mul2(k3p, e);
+    q[m] = mul2(g, mul2(ri2, ri[m]));
+    p[m] = mul2(fma2(m3, q[m], k3e), ri2);
+    dq[m] = make_float2(-k3e.x, -k3e.y);
+    dp[m] = mul2(k3e, is2p);
+  }
+  if (__any_sync(0xffffffffu, amax > kArgSeries)) {
+    const float is3 = is2 * is1, is5 = is3 * is2;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float a = h ? arg[m].y : arg[m].x;
+        if (a > kArgSeries) {
+          float h1, h2;
+          GaussSeries<float, 10>::eval(a * kArgToRho2, h1, h2);
+          const bool self = a == 0.f;
+          const float qs = self ? 0.f : h1 * is3, ps = self ? 0.f : h2 * is5;
+          if (h) {
+            q[m].y = qs; p[m].y = ps;
+            if (self) { dq[m].y = 0.f; dp[m].y = 0.f; }
+          } else {
+            q[m].x = qs; p[m].x = ps;
+            if (self) { dq[m].x = 0.f; dp[m].x = 0.f; }
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < H; ++m)
+    accum_pair_d2(dx[m], dy[m], dz[m], q[m], p[m], dq[m], dp[m], s, acc, 2 * m);
+}
+
 template <int T, bool MASK>
 __device__ __forceinline__ void ujd_source_winck(const float4 sa, const float4 sb,
                                                  const float (&tx)[T], const float (&ty)[T],
                                                  const float (&tz)[T], float (&acc)[T][27]) {
+  if constexpr (T % 2 == 0) {
+    ujd_source_winck_x2<T, MASK>(sa, sb, tx, ty, tz, acc);
+    return;
+  }
   const float s2 = sa.w, k15 = sb.w, k25 = sa.w + sb.w;
   const float c75 = -7.5f * s2 * s2, c175 = -17.5f * s2 * s2;
 #pragma unroll
@@ -782,6 +936,10 @@ template <int T, bool VOTE>
 __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 sb,
                                                  const float (&tx)[T], const float (&ty)[T],
                                                  const float (&tz)[T], float (&acc)[T][27]) {
+  if constexpr (T % 2 == 0) {
+    ujd_source_gauss_x2<T, VOTE>(sa, sb, tx, ty, tz, acc);
+    return;
+  }
   const float ea = sa.w, is1 = sb.w;
   const float is2 = is1 * is1;
   const float k3 = float(kSqrt2overPi) * is2 * is1;
@@ -859,6 +1017,23 @@ __device__ __forceinline__ void ujd_source_gauss_far(const float4 sa, const floa
   const float ea = sa.w, is1 = sb.w;
   const float is2 = is1 * is1;
   const float k3 = float(kSqrt2overPi) * is2 * is1;
+  if constexpr (T % 2 == 0) {
+    const Src2 s(sa, sb);
+    const float2 eap = bc2(ea), m3 = bc2(-3.f), k3p = bc2(k3), is2p = bc2(is2);
+#pragma unroll
+    for (int k = 0; k < T; k += 2) {
+      float2 dx, dy, dz, r2;
+      diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
+      const float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+      const float2 ri2 = mul2(ri, ri);
+      const float2 q = mul2(ri2, ri);
+      const float2 p = mul2(mul2(m3, q), ri2);
+      const float2 a = mul2(r2, eap);
+      const float2 k3e = mul2(k3p, make_float2(ex2_ftz(a.x), ex2_ftz(a.y)));
+      accum_pair_d2(dx, dy, dz, q, p, make_float2(-k3e.x, -k3e.y), mul2(k3e, is2p), s, acc, k);
+    }
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < T; ++k) {
     const float dx = tx[k] - sa.x, dy = ty[k] - sa.y, dz = tz[k] - sa.z;
@@ -1026,6 +1201,67 @@ __device__ __forceinline__ void zeta_source(const float4 sa, const float4 sb, co
                                             const float4 sd, const float (&tx)[T],
                                             const float (&ty)[T], const float (&tz)[T],
                                             float (&acc)[T][D ? 12 : 6]) {
+  if constexpr (T % 2 == 0) {
+    // Target pairs (see "packed FP32").
+    constexpr int H = T / 2;
+    const float2 nx = bc2(-sa.x), ny = bc2(-sa.y), nz = bc2(-sa.z), aw = bc2(sa.w);
+    float2 r2[H];
+    float amax = -INFINITY;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const float2 dx = add2(make_float2(tx[2 * m], tx[2 * m + 1]), nx);
+      const float2 dy = add2(make_float2(ty[2 * m], ty[2 * m + 1]), ny);
+      const float2 dz = add2(make_float2(tz[2 * m], tz[2 * m + 1]), nz);
+      r2[m] = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+      if (VOTE) amax = fmaxf(amax, fmaxf(r2[m].x * sa.w, r2[m].y * sa.w));
+    }
+    if (VOTE && KERNEL != VPM_KERNEL_WINCKELMANS && __all_sync(0xffffffffu, amax <= kArgZero))
+      return;
+    const float2 gx = bc2(sb.x), gy = bc2(sb.y), gz = bc2(sb.z);
+    const float2 vx = bc2(sc.x), vy = bc2(sc.y), vz = bc2(sc.z);
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const int k = 2 * m;
+      float2 z, dzz = bc2(0.f);
+      if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+        const float2 h = fma2(r2[m], aw, bc2(sb.w));
+        const float2 rs = make_float2(rsqrt_ftz(h.x), rsqrt_ftz(h.y));
+        const float2 rs2 = mul2(rs, rs);
+        z = mul2(mul2(rs2, rs2), mul2(rs2, rs));
+        if (D) dzz = mul2(z, fma2(bc2(sc.w), rs2, bc2(4.f)));
+      } else {
+        const float2 x = mul2(r2[m], aw);
+        z = mul2(bc2(sb.w), make_float2(ex2_ftz(x.x), ex2_ftz(x.y)));
+        if (D) dzz = mul2(z, fma2(x, bc2(kArgToRho2), bc2(-3.f)));
+      }
+      if (MASK) {
+        z.x = r2[m].x > 0.f ? z.x : 0.f;
+        z.y = r2[m].y > 0.f ? z.y : 0.f;
+        if (D) {
+          dzz.x = r2[m].x > 0.f ? dzz.x : 0.f;
+          dzz.y = r2[m].y > 0.f ? dzz.y : 0.f;
+        }
+      }
+      fma_acc2(acc, k, 0, z, gx);
+      fma_acc2(acc, k, 1, z, gy);
+      fma_acc2(acc, k, 2, z, gz);
+      fma_acc2(acc, k, 3, z, vx);
+      fma_acc2(acc, k, 4, z, vy);
+      fma_acc2(acc, k, 5, z, vz);
+      if (D) {
+        fma_acc2(acc, k, 6, dzz, gx);
+        fma_acc2(acc, k, 7, dzz, gy);
+        fma_acc2(acc, k, 8, dzz, gz);
+        fma_acc2(acc, k, 9, z, bc2(sd.x));
+        fma_acc2(acc, k, 10, z, bc2(sd.y));
+        fma_acc2(acc, k, 11, z, bc2(sd.z));
+        fma_acc2(acc, k, 9, dzz, vx);
+        fma_acc2(acc, k, 10, dzz, vy);
+        fma_acc2(acc, k, 11, dzz, vz);
+      }
+    }
+    return;
+  }
   float r2[T];
   float amax = -INFINITY;
 #pragma unroll
