@@ -550,6 +550,10 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       }
       // FP32 U/J passes do not accumulate A22 (trace-free pairs): rebuild it.
       if constexpr (Tr::kUJ && F32) {
+        if constexpr (KERNEL == VPM_KERNEL_GAUSSIANERF) {
+#pragma unroll
+          for (int w = 3; w < 11; ++w) v[w] *= kGaussAScale;
+        }
         v[11] = -(v[3] + v[7]);
         if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
       }

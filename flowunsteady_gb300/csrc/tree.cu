@@ -638,6 +638,10 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
     double v[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) v[k] = double(shi[k]) + double(slo[k]);
+    if constexpr (UJ && KERNEL == VPM_KERNEL_GAUSSIANERF) {
+#pragma unroll
+      for (int k = 3; k < 11; ++k) v[k] *= kGaussAScale;   // A holds p/(-3) sums
+    }
     if constexpr (UJ) v[11] = -(v[3] + v[7]);   // A22: the FP32 routines keep J trace-free
     if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
 #pragma unroll

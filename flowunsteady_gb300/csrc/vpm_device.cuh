@@ -361,9 +361,16 @@ __device__ __forceinline__ void uj_source_winck(const float4 sa, const float4 sb
     const float2 s2p = bc2(s2), k15p = bc2(k15), k25p = bc2(k25);
 #pragma unroll
     for (int k = 0; k < T; k += 2) {
-      float2 dx, dy, dz, r2;
-      diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
-      const float2 h = add2(r2, s2p);
+      float2 dx, dy, dz, r2, h;
+      if (MASK) {
+        diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
+        h = add2(r2, s2p);
+      } else {   // r² + σ² in the same chain: r² itself is not needed
+        dx = add2(make_float2(tx[k], tx[k + 1]), s.nx);
+        dy = add2(make_float2(ty[k], ty[k + 1]), s.ny);
+        dz = add2(make_float2(tz[k], tz[k + 1]), s.nz);
+        h = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, s2p)));
+      }
       const float2 rs = make_float2(rsqrt_ftz(h.x), rsqrt_ftz(h.y));
       const float2 rs2 = mul2(rs, rs);
       const float2 rs3 = mul2(rs2, rs);
@@ -408,7 +415,7 @@ __device__ __forceinline__ void uj_source_gauss_x2(const float4 sa, const float4
                                                    float kt, float kc, float k3) {
   constexpr int H = T / 2;
   const Src2 s(sa, sb);
-  const float2 ea = bc2(sa.w), one = bc2(1.f), m3 = bc2(-3.f);
+  const float2 ea = bc2(sa.w), one = bc2(1.f);
   float2 dx[H], dy[H], dz[H], arg[H], ri[H], q[H], p[H];
   float amax = -INFINITY;
 #pragma unroll
@@ -425,11 +432,11 @@ __device__ __forceinline__ void uj_source_gauss_x2(const float4 sa, const float4
     for (int m = 0; m < H; ++m) {
       const float2 ri2 = mul2(ri[m], ri[m]);
       const float2 qq = mul2(ri2, ri[m]);
-      accum_pair2(dx[m], dy[m], dz[m], qq, mul2(mul2(m3, qq), ri2), s, acc, 2 * m);
+      accum_pair2(dx[m], dy[m], dz[m], qq, mul2(qq, ri2), s, acc, 2 * m);
     }
     return;
   }
-  const float2 ktp = bc2(kt), nkc = bc2(-kc), k3p = bc2(k3);
+  const float2 ktp = bc2(kt), nkc = bc2(-kc), k3np = bc2(k3 * (-1.f / 3.f));
   const float2 nA4 = bc2(-kErfcxA4), nA3 = bc2(-kErfcxA3), nA2 = bc2(-kErfcxA2),
                nA1 = bc2(-kErfcxA1);
 #pragma unroll
@@ -442,10 +449,10 @@ __device__ __forceinline__ void uj_source_gauss_x2(const float4 sa, const float4
     const float2 g = fma2(e, fma2(nkc, r, nf), one);
     const float2 ri2 = mul2(ri[m], ri[m]);
     q[m] = mul2(g, mul2(ri2, ri[m]));
-    p[m] = mul2(fma2(m3, q[m], mul2(k3p, e)), ri2);
+    p[m] = mul2(fma2(k3np, e, q[m]), ri2);
   }
   if (__any_sync(0xffffffffu, amax > kArgSeries)) {
-    const float is1 = sb.w, is2 = is1 * is1, is3 = is2 * is1, is5 = is3 * is2;
+    const float is1 = sb.w, is2 = is1 * is1, is3 = is2 * is1, is5n = is3 * is2 * (-1.f / 3.f);
 #pragma unroll
     for (int m = 0; m < H; ++m) {
 #pragma unroll
@@ -455,7 +462,7 @@ __device__ __forceinline__ void uj_source_gauss_x2(const float4 sa, const float4
           float h1, h2;
           GaussSeries<float, 10>::eval(a * kArgToRho2, h1, h2);
           const bool self = a == 0.f;
-          const float qs = self ? 0.f : h1 * is3, ps = self ? 0.f : h2 * is5;
+          const float qs = self ? 0.f : h1 * is3, ps = self ? 0.f : h2 * is5n;
           if (h) { q[m].y = qs; p[m].y = ps; } else { q[m].x = qs; p[m].x = ps; }
         }
       }
@@ -464,6 +471,11 @@ __device__ __forceinline__ void uj_source_gauss_x2(const float4 sa, const float4
 #pragma unroll
   for (int m = 0; m < H; ++m) accum_pair2(dx[m], dy[m], dz[m], q[m], p[m], s, acc, 2 * m);
 }
+
+// Gaussian-erf FP32 routines (U/J and α-derivative passes) accumulate
+// p/(-3) instead of p = q'/r in the A sums, so that the far form's p is the one
+// product q/r²; the kernels' epilogues multiply A by -3 (kGaussAScale).
+constexpr double kGaussAScale = -3.0;
 
 // Gaussian-erf: source quads (x, y, z, -log2(e)/(2σ²)) and (Γx, Γy, Γz, 1/σ).
 // All T targets take the erf-free form, and a warp vote sends the rare warps
@@ -484,6 +496,7 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
     uj_source_gauss_x2<T, VOTE>(sa, sb, tx, ty, tz, acc, kt, kc, k3);
     return;
   }
+  const float k3n = k3 * (-1.f / 3.f);
   float dx[T], dy[T], dz[T], arg[T], q[T], p[T];
   float amax = -INFINITY;
   if constexpr (VOTE) {
@@ -503,7 +516,7 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
       for (int k = 0; k < T; ++k) {
         const float ri2 = ri[k] * ri[k];
         const float qq = ri2 * ri[k];
-        accum_pair(dx[k], dy[k], dz[k], qq, (-3.f * qq) * ri2, sb.x, sb.y, sb.z, acc[k]);
+        accum_pair(dx[k], dy[k], dz[k], qq, qq * ri2, sb.x, sb.y, sb.z, acc[k]);
       }
       return;
     }
@@ -516,7 +529,7 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
       const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
       const float ri2 = ri[k] * ri[k];
       q[k] = g * (ri2 * ri[k]);
-      p[k] = fmaf(-3.f, q[k], k3 * e) * ri2;
+      p[k] = fmaf(k3n, e, q[k]) * ri2;
     }
   } else {
 #pragma unroll
@@ -535,11 +548,11 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
       const float g = fmaf(-e, fmaf(kc, r, f), 1.f);
       const float ri2 = ri * ri;
       q[k] = g * (ri2 * ri);
-      p[k] = fmaf(-3.f, q[k], k3 * e) * ri2;
+      p[k] = fmaf(k3n, e, q[k]) * ri2;
     }
   }
   if (__any_sync(0xffffffffu, amax > kArgSeries)) {
-    const float is2 = is1 * is1, is3 = is2 * is1, is5 = is3 * is2;
+    const float is2 = is1 * is1, is3 = is2 * is1, is5n = is3 * is2 * (-1.f / 3.f);
 #pragma unroll
     for (int k = 0; k < T; ++k) {
       if (arg[k] > kArgSeries) {
@@ -547,7 +560,7 @@ __device__ __forceinline__ void uj_source_gauss(const float4 sa, const float4 sb
         GaussSeries<float, 10>::eval(arg[k] * kArgToRho2, h1, h2);
         const bool self = arg[k] == 0.f;   // r² == 0 (the exponent argument is r²·(<0))
         q[k] = self ? 0.f : h1 * is3;
-        p[k] = self ? 0.f : h2 * is5;
+        p[k] = self ? 0.f : h2 * is5n;
       }
     }
   }
@@ -579,7 +592,6 @@ __device__ __forceinline__ void uj_source_gauss_far(const float4 sa, const float
                                                     const float (&tz)[T], float (&acc)[T][NV]) {
   if constexpr (T % 2 == 0) {
     const Src2 s(sa, sb);
-    const float2 m3 = bc2(-3.f);
 #pragma unroll
     for (int k = 0; k < T; k += 2) {
       float2 dx, dy, dz, r2;
@@ -587,7 +599,7 @@ __device__ __forceinline__ void uj_source_gauss_far(const float4 sa, const float
       const float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
       const float2 ri2 = mul2(ri, ri);
       const float2 q = mul2(ri2, ri);
-      accum_pair2(dx, dy, dz, q, mul2(mul2(m3, q), ri2), s, acc, k);
+      accum_pair2(dx, dy, dz, q, mul2(q, ri2), s, acc, k);
     }
   } else {
 #pragma unroll
@@ -597,7 +609,7 @@ __device__ __forceinline__ void uj_source_gauss_far(const float4 sa, const float
       const float ri = rsqrt_ftz(r2);
       const float ri2 = ri * ri;
       const float q = ri2 * ri;
-      const float p = (-3.f * q) * ri2;
+      const float p = q * ri2;
       accum_pair(dx, dy, dz, q, p, sb.x, sb.y, sb.z, acc[k]);
     }
   }
@@ -796,9 +808,16 @@ __device__ __forceinline__ void ujd_source_winck_x2(const float4 sa, const float
   const float2 c75 = bc2(-7.5f * s2 * s2), c175 = bc2(-17.5f * s2 * s2);
 #pragma unroll
   for (int k = 0; k < T; k += 2) {
-    float2 dx, dy, dz, r2;
-    diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
-    const float2 h = add2(r2, s2p);
+    float2 dx, dy, dz, r2, h;
+    if (MASK) {
+      diff2(tx, ty, tz, k, s, dx, dy, dz, r2);
+      h = add2(r2, s2p);
+    } else {
+      dx = add2(make_float2(tx[k], tx[k + 1]), s.nx);
+      dy = add2(make_float2(ty[k], ty[k + 1]), s.ny);
+      dz = add2(make_float2(tz[k], tz[k + 1]), s.nz);
+      h = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, s2p)));
+    }
     const float2 rs = make_float2(rsqrt_ftz(h.x), rsqrt_ftz(h.y));
     const float2 rs2 = mul2(rs, rs);
     const float2 rs3 = mul2(rs2, rs);
@@ -826,7 +845,7 @@ __device__ __forceinline__ void ujd_source_gauss_x2(const float4 sa, const float
   const float is1 = sb.w, is2 = is1 * is1;
   const float k3 = float(kSqrt2overPi) * is2 * is1;
   const Src2 s(sa, sb);
-  const float2 ea = bc2(sa.w), one = bc2(1.f), m3 = bc2(-3.f), k3p = bc2(k3), is2p = bc2(is2);
+  const float2 ea = bc2(sa.w), one = bc2(1.f), k3p = bc2(k3), is2p = bc2(is2);
   float2 dx[H], dy[H], dz[H], r2[H], ri[H], arg[H], q[H], p[H], dq[H], dp[H];
   float amax = -INFINITY;
 #pragma unroll
@@ -842,7 +861,7 @@ __device__ __forceinline__ void ujd_source_gauss_x2(const float4 sa, const float
     for (int m = 0; m < H; ++m) {
       const float2 ri2 = mul2(ri[m], ri[m]);
       const float2 qq = mul2(ri2, ri[m]);
-      const float2 pp = mul2(mul2(m3, qq), ri2);
+      const float2 pp = mul2(qq, ri2);
       if (zero) {
         accum_pair2(dx[m], dy[m], dz[m], qq, pp, s, acc, 2 * m);
       } else {
@@ -867,12 +886,12 @@ __device__ __forceinline__ void ujd_source_gauss_x2(const float4 sa, const float
     const float2 ri2 = mul2(ri[m], ri[m]);
     const float2 k3e = mul2(k3p, e);
     q[m] = mul2(g, mul2(ri2, ri[m]));
-    p[m] = mul2(fma2(m3, q[m], k3e), ri2);
+    p[m] = mul2(fma2(k3e, bc2(-1.f / 3.f), q[m]), ri2);
     dq[m] = make_float2(-k3e.x, -k3e.y);
     dp[m] = mul2(k3e, is2p);
   }
   if (__any_sync(0xffffffffu, amax > kArgSeries)) {
-    const float is3 = is2 * is1, is5 = is3 * is2;
+    const float is3 = is2 * is1, is5n = is3 * is2 * (-1.f / 3.f);
 #pragma unroll
     for (int m = 0; m < H; ++m) {
 #pragma unroll
@@ -882,7 +901,7 @@ __device__ __forceinline__ void ujd_source_gauss_x2(const float4 sa, const float
           float h1, h2;
           GaussSeries<float, 10>::eval(a * kArgToRho2, h1, h2);
           const bool self = a == 0.f;
-          const float qs = self ? 0.f : h1 * is3, ps = self ? 0.f : h2 * is5;
+          const float qs = self ? 0.f : h1 * is3, ps = self ? 0.f : h2 * is5n;
           if (h) {
             q[m].y = qs; p[m].y = ps;
             if (self) { dq[m].y = 0.f; dp[m].y = 0.f; }
@@ -963,7 +982,7 @@ __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 s
     for (int k = 0; k < T; ++k) {
       const float ri2 = ri[k] * ri[k];
       const float qq = ri2 * ri[k];
-      const float pp = (-3.f * qq) * ri2;
+      const float pp = qq * ri2;
       if (zero) {
         accum_pair(dx[k], dy[k], dz[k], qq, pp, sb.x, sb.y, sb.z, acc[k]);
       } else {
@@ -983,12 +1002,12 @@ __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 s
     const float ri2 = ri[k] * ri[k];
     const float k3e = k3 * e;
     q[k] = g * (ri2 * ri[k]);
-    p[k] = fmaf(-3.f, q[k], k3e) * ri2;
+    p[k] = fmaf(k3e, -1.f / 3.f, q[k]) * ri2;
     dq[k] = -k3e;
     dp[k] = k3e * is2;
   }
   if (__any_sync(0xffffffffu, amax > kArgSeries)) {
-    const float is3 = is2 * is1, is5 = is3 * is2;
+    const float is3 = is2 * is1, is5n = is3 * is2 * (-1.f / 3.f);
 #pragma unroll
     for (int k = 0; k < T; ++k) {
       if (arg[k] > kArgSeries) {
@@ -996,7 +1015,7 @@ __device__ __forceinline__ void ujd_source_gauss(const float4 sa, const float4 s
         GaussSeries<float, 10>::eval(arg[k] * kArgToRho2, h1, h2);
         const bool self = arg[k] == 0.f;
         q[k] = self ? 0.f : h1 * is3;
-        p[k] = self ? 0.f : h2 * is5;
+        p[k] = self ? 0.f : h2 * is5n;
         dq[k] = self ? 0.f : dq[k];
         dp[k] = self ? 0.f : dp[k];
       }
@@ -1019,7 +1038,7 @@ __device__ __forceinline__ void ujd_source_gauss_far(const float4 sa, const floa
   const float k3 = float(kSqrt2overPi) * is2 * is1;
   if constexpr (T % 2 == 0) {
     const Src2 s(sa, sb);
-    const float2 eap = bc2(ea), m3 = bc2(-3.f), k3p = bc2(k3), is2p = bc2(is2);
+    const float2 eap = bc2(ea), k3p = bc2(k3), is2p = bc2(is2);
 #pragma unroll
     for (int k = 0; k < T; k += 2) {
       float2 dx, dy, dz, r2;
@@ -1027,7 +1046,7 @@ __device__ __forceinline__ void ujd_source_gauss_far(const float4 sa, const floa
       const float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
       const float2 ri2 = mul2(ri, ri);
       const float2 q = mul2(ri2, ri);
-      const float2 p = mul2(mul2(m3, q), ri2);
+      const float2 p = mul2(q, ri2);
       const float2 a = mul2(r2, eap);
       const float2 k3e = mul2(k3p, make_float2(ex2_ftz(a.x), ex2_ftz(a.y)));
       accum_pair_d2(dx, dy, dz, q, p, make_float2(-k3e.x, -k3e.y), mul2(k3e, is2p), s, acc, k);
@@ -1041,7 +1060,7 @@ __device__ __forceinline__ void ujd_source_gauss_far(const float4 sa, const floa
     const float ri = rsqrt_ftz(r2);
     const float ri2 = ri * ri;
     const float q = ri2 * ri;
-    const float p = (-3.f * q) * ri2;
+    const float p = q * ri2;
     const float k3e = k3 * ex2_ftz(r2 * ea);
     accum_pair_d(dx, dy, dz, q, p, -k3e, k3e * is2, sb.x, sb.y, sb.z, acc[k]);
   }
