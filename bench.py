@@ -45,10 +45,11 @@ BYTES_D2H = 96          # U (3) and J (9) per particle (FP64)
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one pair-kernel launch of the default workload,
 # from an ncu capture (profiles/launches_bench_helical_n262144.md).
-# DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch at the tuned
-# 256x2 shape, from an ncu capture of the benchmark workload; the writes are
-# mostly the FP64 partial sums of the source chunks, so other shapes differ.
-PAIR_KERNEL_TRAFFIC = {262144: 29289728 + 162531584}
+# DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch of the
+# benchmark workload per (N, tile shape), from ncu captures; the writes are
+# mostly the FP64 partial sums of the source chunks, so they depend on the shape.
+PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 28400640 + 193888768,
+                       (262144, "256x2"): 29289728 + 162531584}
 
 
 def parse():
@@ -391,7 +392,7 @@ def run_ours(args, world, rank, local, dist):
     achieved = PAIR_FLOP * pairs / (ms_per_step / 1e3) / 1e12
     roof = {"bound": "fp32_fma", "achieved": achieved, "peak": f32.value, "unit": "TFLOP/s",
             "frac": achieved / f32.value if f32.value > 0 else None,
-            "traffic": PAIR_KERNEL_TRAFFIC.get(n),
+            "traffic": PAIR_KERNEL_TRAFFIC.get((n, args.tile or tuned)),
             "traffic_unit": "bytes per launch (ncu dram__bytes_read + dram__bytes_write)",
             "peak_source": "in-repo FFMA microbenchmark (vpm_measure_fma_peaks) in this run",
             "fp64_peak_tflops": f64.value, "microbench_sm_mhz": mhz.value,
