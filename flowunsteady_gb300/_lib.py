@@ -40,6 +40,8 @@ SFS_FORCE_POSITIVE = 2
 SFS_ANALYTIC_DSIGMA = 4
 UJ_DIRECT = 0
 UJ_TREE = 1
+ORDER_AUTO = 0      # vpm_set_particle_order: Morton order for large fields and batches
+ORDER_CALLER = 1    # the caller's order
 RELAX_NONE = 0
 RELAX_PEDRIZZETTI = 1
 
@@ -59,7 +61,8 @@ EXPORTS = [
     "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
     "vpm_batch_last_error", "vpm_batch_set_stream", "vpm_batch_set_field",
     "vpm_batch_get_field", "vpm_batch_eval_UJ", "vpm_batch_get_UJ", "vpm_batch_step",
-    "vpm_autotune", "vpm_set_tile", "vpm_measure_fma_peaks", "vpm_debug_fail_after",
+    "vpm_autotune", "vpm_set_tile", "vpm_set_particle_order", "vpm_batch_set_particle_order",
+    "vpm_measure_fma_peaks", "vpm_debug_fail_after",
     "vpm_get_launch_count", "vpm_build_info",
 ]
 
@@ -171,6 +174,8 @@ def _declare(lib):
         "vpm_batch_step": (ctypes.c_int, [_vp, ctypes.c_double, P(Scheme), _i64, ctypes.c_int]),
         "vpm_autotune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Tile), _dp]),
         "vpm_set_tile": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Tile)]),
+        "vpm_set_particle_order": (ctypes.c_int, [_vp, ctypes.c_int]),
+        "vpm_batch_set_particle_order": (ctypes.c_int, [_vp, ctypes.c_int]),
         "vpm_measure_fma_peaks": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
         "vpm_debug_fail_after": (ctypes.c_int, [_vp, _i64]),
         "vpm_get_launch_count": (ctypes.c_int, [_vp, P(_i64)]),

@@ -225,6 +225,11 @@ static int all_set(vpm_batch* b) {
   return VPM_OK;
 }
 
+int vpm_batch_set_particle_order(vpm_batch* b, int mode) {
+  if (!b) return set_error(nullptr, VPM_ERR_INVALID, "null batch");
+  return from_ctx(b, vpm_set_particle_order(b->ctx, mode));
+}
+
 int vpm_batch_eval_UJ(vpm_batch* b, int kernel, int precision) {
   if (!b) return set_error(nullptr, VPM_ERR_INVALID, "null batch");
   int rc = all_set(b);

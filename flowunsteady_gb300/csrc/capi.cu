@@ -364,11 +364,13 @@ static bool sort_disabled() {
 }
 
 static bool sorted_pass(const vpm_ctx* c, int prec, int64_t t0, int64_t t1) {
-  return !sort_disabled() && !c->bp && prec != VPM_PREC_FP64 && t0 == 0 && t1 == c->n &&
-         c->n >= 65536;
+  return !sort_disabled() && c->order == VPM_ORDER_AUTO && !c->bp && prec != VPM_PREC_FP64 &&
+         t0 == 0 && t1 == c->n && c->n >= 65536;
 }
 
-static bool sorted_batch(int prec) { return !sort_disabled() && prec != VPM_PREC_FP64; }
+static bool sorted_batch(const vpm_ctx* c, int prec) {
+  return !sort_disabled() && c->order == VPM_ORDER_AUTO && prec != VPM_PREC_FP64;
+}
 
 // Scratch of the sorted passes (allocated while planning, before any capture):
 // c->srt rows 0-2 X, 3-5 Γ, 6 σ, 7-9 v, 10-12 w; c->sout rows 0-2 U (or the ζ
@@ -466,7 +468,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     const int nv = nval_of(pass);
     const size_t need = bp->max_chunks > 1 ? size_t(bp->max_chunks) * nv * size_t(c->ld) : 0;
     c->part_need = std::max(c->part_need, need);
-    const bool srt = sorted_batch(prec);
+    const bool srt = sorted_batch(c, prec);
     if (c->dry) return srt ? sort_scratch(c, bp->nfields) : cudaSuccess;
     if (need > c->part_elems) return cudaErrorMemoryAllocation;
     const int64_t ld = c->ld;
@@ -1244,6 +1246,20 @@ int vpm_set_tile(vpm_ctx* c, int kernel, int precision, const vpm_tile* t) {
     return ctx_fail(c, VPM_ERR_UNSUPPORTED, "tile shape not compiled for this precision");
   c->pinned[0][kernel][precision] = s;
   c->pinned[1][kernel][precision] = s;
+  return VPM_OK;
+}
+
+int vpm_set_particle_order(vpm_ctx* c, int mode) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (mode != VPM_ORDER_AUTO && mode != VPM_ORDER_CALLER)
+    return ctx_fail(c, VPM_ERR_INVALID, "unknown particle order");
+  if (mode != c->order) {
+    DeviceGuard dg(c->device);
+    cudaStreamSynchronize(c->st);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);   // captured for the old order
+    c->graphs.clear();
+    c->order = mode;
+  }
   return VPM_OK;
 }
 

@@ -145,6 +145,7 @@ struct vpm_ctx {
   int64_t fail_after = 0;
   std::string err;
   vpm::BatchPlan* bp = nullptr;   // set when the context backs a vpm_batch
+  int order = VPM_ORDER_AUTO;     // vpm_set_particle_order
   vpm::FmmWork* fmm = nullptr;    // treecode workspace (allocated on first use)
   vpm::SortWork* sortw = nullptr; // Morton order of the direct pair passes (large fields)
   double* srt = nullptr;          // Morton-ordered inputs: X3 Γ3 σ1 v3 w3 (13 rows of ld)

@@ -48,6 +48,8 @@ def test_bad_calls_are_rejected_without_launch():
     assert lib.vpm_set_particles(None, 1, None, 3, None, 3, None, 1) == L.ERR_INVALID
     assert lib.vpm_eval_UJ(None, 0, 0) == L.ERR_INVALID
     assert lib.vpm_step(None, 0.1, None, 1, 1) == L.ERR_INVALID
+    assert lib.vpm_set_particle_order(None, L.ORDER_CALLER) == L.ERR_INVALID
+    assert lib.vpm_batch_set_particle_order(None, L.ORDER_AUTO) == L.ERR_INVALID
     x = np.zeros(3)
     assert lib.vpm_uj_device_async(7, 0, 1, None, None, None, 1, 1, None, 1, None, None, 1,
                                    None) == L.ERR_INVALID
@@ -65,6 +67,7 @@ def test_header_enums_match_python_constants():
     for name, val in [("VPM_ERR_INVALID", L.ERR_INVALID), ("VPM_ERR_CAPACITY", L.ERR_CAPACITY),
                       ("VPM_ERR_NONFINITE", L.ERR_NONFINITE), ("VPM_ERR_INJECTED", L.ERR_INJECTED),
                       ("VPM_KERNEL_GAUSSIANERF", L.KERNEL_GAUSSIANERF),
-                      ("VPM_PREC_FP32C", L.PREC_FP32C), ("VPM_DIAG_COUNT", L.DIAG_COUNT)]:
+                      ("VPM_PREC_FP32C", L.PREC_FP32C), ("VPM_DIAG_COUNT", L.DIAG_COUNT),
+                      ("VPM_ORDER_AUTO", L.ORDER_AUTO), ("VPM_ORDER_CALLER", L.ORDER_CALLER)]:
         m = re.search(rf"{name}\s*=\s*(-?\d+)", src)
         assert m and int(m.group(1)) == val, name

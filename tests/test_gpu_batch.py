@@ -79,3 +79,21 @@ def test_batch_fp32c_step_in_morton_order():
     b.close()
     for dx, dg, ds in err:
         assert dx <= 1e-7 and dg <= 2e-6 and ds <= 5e-7, err
+
+
+def test_batch_particle_order_changes_only_the_summation_order():
+    fs = fields()
+    res = {}
+    for mode in (L.ORDER_AUTO, L.ORDER_CALLER):
+        b = FieldBatch(SIZES)
+        b.set_particle_order(mode)
+        for f, (X, G, S) in enumerate(fs):
+            b.set_field(f, X, G, S)
+        b.eval_UJ(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+        res[mode] = [b.get_UJ(f) for f in range(len(SIZES))]
+        b.close()
+    for f in range(len(SIZES)):
+        if SIZES[f] == 1:
+            continue
+        (Ua, Ja), (Uc, Jc) = res[L.ORDER_AUTO][f], res[L.ORDER_CALLER][f]
+        assert rel_l2(Ua, Uc) <= 1e-6 and rel_l2(Ja, Jc) <= 1e-6, f

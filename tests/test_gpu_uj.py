@@ -302,68 +302,43 @@ def test_gaussian_far_field_forms_match_general_forms(tmp_path, oracle):
     assert rel_l2(ref["U2"][idx], U0) <= 1e-5 and rel_l2(ref["J2"][idx], J0) <= 1e-5
 
 
-_UNSORTED_SCRIPT = r"""
-import sys, ctypes, numpy as np
-sys.path.insert(0, sys.argv[1])
-from tests.helpers import Ctx, scheme
-from flowunsteady_gb300.workloads import helical_wake
-from flowunsteady_gb300 import _lib as L
-n = int(sys.argv[2])
-X, G, S = helical_wake(n)
-order = np.random.default_rng(5).permutation(n)   # an incoherent particle order
-X, G, S = X[order], G[order], S[order]
-flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
-out = {}
-with Ctx(n) as c:
-    c.set(X, G, S)
-    out["U"], out["J"] = c.uj(1, L.PREC_FP32C)
-    sc = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
-    c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
-    out["C"], out["E"] = c.sfs()
-    c.step(sc, 1e-4, nsteps=2)
-    out["X"], out["G"], out["S"] = c.state()
-np.savez(sys.argv[3], **out)
-"""
-
-
-def test_morton_ordered_passes_match_original_order(tmp_path, oracle):
+def test_morton_ordered_passes_match_original_order(oracle):
     # Fields of 65,536 particles or more are evaluated along a Morton curve
-    # (VPM_NO_SORT=1 turns it off): only the summation order changes.  The
-    # particle order here is random, the case the curve is for.
-    import subprocess
-    import sys
+    # (vpm_set_particle_order(VPM_ORDER_CALLER) turns it off): only the
+    # summation order changes.  The particle order here is random, the case
+    # the curve is for.
     n = 70000
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    out = tmp_path / "unsorted.npz"
-    script = tmp_path / "unsorted.py"
-    script.write_text(_UNSORTED_SCRIPT)
-    subprocess.run([sys.executable, str(script), root, str(n), str(out)], check=True,
-                   env=dict(os.environ, VPM_NO_SORT="1"), timeout=600)
-    ref = np.load(out)
     X, G, S = helical_wake(n)
     order = np.random.default_rng(5).permutation(n)
     X, G, S = X[order], G[order], S[order]
     flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
+    sc = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
+    out = {}
+    for mode in (L.ORDER_CALLER, L.ORDER_AUTO):
+        with Ctx(n) as c:
+            c.rc(c.lib.vpm_set_particle_order(c.p, mode))
+            c.set(X, G, S)
+            if mode == L.ORDER_CALLER:   # FP64 passes keep the caller's order in both modes
+                out["U64"], out["J64"] = c.uj(1, L.PREC_FP64)
+                sc64 = scheme(kernel=1, prec=L.PREC_FP64, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
+                c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc64)))
+                out["C64"], out["E64"] = c.sfs()
+            r = out.setdefault(mode, {})
+            r["U"], r["J"] = c.uj(1, L.PREC_FP32C)
+            c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
+            r["C"], r["E"] = c.sfs()
+            c.step(sc, 1e-4, nsteps=2)
+            r["X"], r["G"], r["S"] = c.state()
+    srt, ref = out[L.ORDER_AUTO], out[L.ORDER_CALLER]
     err = {}
-    with Ctx(n) as c:
-        c.set(X, G, S)
-        U64, J64 = c.uj(1, L.PREC_FP64)          # FP64 passes keep the caller's order
-        sc = scheme(kernel=1, prec=L.PREC_FP64, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
-        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
-        C64, E64 = c.sfs()
-        U, J = c.uj(1, L.PREC_FP32C)
-        sc = scheme(kernel=1, prec=L.PREC_FP32C, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
-        c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc)))
-        C, E = c.sfs()
-        c.step(sc, 1e-4, nsteps=2)
-        Xs, Gs, Ss = c.state()
-    for name, a, b in (("U", U, U64), ("J", J, J64), ("E", E, E64), ("C", C[:, 0], C64[:, 0]),
-                       ("U_unsorted", ref["U"], U64), ("J_unsorted", ref["J"], J64),
-                       ("E_unsorted", ref["E"], E64), ("C_unsorted", ref["C"][:, 0], C64[:, 0]),
-                       ("G_steps", Gs, ref["G"]), ("S_steps", Ss, ref["S"])):
-        err[name] = rel_l2(a, b)
-    err["X_steps"] = float(np.abs(Xs - ref["X"]).max())
-    print(err)
+    for tag, r in (("", srt), ("_unsorted", ref)):
+        err["U" + tag] = rel_l2(r["U"], out["U64"])
+        err["J" + tag] = rel_l2(r["J"], out["J64"])
+        err["E" + tag] = rel_l2(r["E"], out["E64"])
+        err["C" + tag] = rel_l2(r["C"][:, 0], out["C64"][:, 0])
+    err["X_steps"] = float(np.abs(srt["X"] - ref["X"]).max())
+    err["G_steps"] = rel_l2(srt["G"], ref["G"])
+    err["S_steps"] = rel_l2(srt["S"], ref["S"])
     assert err["U"] <= 5e-7 and err["J"] <= 5e-7, err
     assert err["U_unsorted"] <= 1e-5 and err["J_unsorted"] <= 1e-5, err
     # E = S(J_p, Ω_p) - Σ ζ S(J_q, Γ_q) nearly cancels: its FP32 error is a few
@@ -374,4 +349,4 @@ def test_morton_ordered_passes_match_original_order(tmp_path, oracle):
     assert err["X_steps"] <= 1e-7 and err["G_steps"] <= 5e-6 and err["S_steps"] <= 1e-8, err
     idx = np.sort(np.random.default_rng(6).choice(n, 300, replace=False))
     U0, J0 = oracle.uj_direct(1, X, G, S, Xt=X[idx])
-    assert rel_l2(U[idx], U0) <= 1e-5 and rel_l2(J[idx], J0) <= 1e-5
+    assert rel_l2(srt["U"][idx], U0) <= 1e-5 and rel_l2(srt["J"][idx], J0) <= 1e-5
