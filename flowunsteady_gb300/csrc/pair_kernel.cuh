@@ -76,7 +76,9 @@ __host__ __device__ constexpr size_t smem_bytes(int block, int tpt) {
 }
 
 // Minimum resident CTAs requested from the compiler: caps the FP32 U/J kernels
-// at 128 (T=4) or 96 (T=2) registers per thread (the D form: 168 for T=2).
+// at 168 (T=4) or 96 (T=2) registers per thread (the D form: 255 and 168).
+// With T=4 the fold pairs in shared memory (61 KB per 128-thread CTA) allow
+// no more than 3 CTAs per SM either.
 template <int PASS, int PREC, int BLOCK, int T>
 constexpr int min_blocks() {
   constexpr int regs = PASS == PASS_UJD ? (T >= 4 ? 255 : 168) : (T >= 4 ? 168 : 96);
