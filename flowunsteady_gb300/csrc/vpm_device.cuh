@@ -37,6 +37,10 @@ constexpr double kZeta0Gauss = 0.06349363593424096978;  // (2π)^{-3/2}
 
 // ρ² below which the FP64 Gaussian-erf series replaces the direct forms.
 constexpr double kSeriesRho2D = 0.25;
+// FP64 Gaussian-erf far form: for ρ² >= 90, e^{-ρ²/2}(erfcx(ρ/√2) + √(2/π)ρ) <
+// 3e-19 and √(2/π)ρ³e^{-ρ²/2}/3 < 7e-18, both below half an FP64 ulp of 1,
+// so g = 1 and q'/r = -3/r⁵ to FP64 rounding.
+constexpr double kFarRho2D = 90.0;
 
 __host__ __device__ inline double zeta0_of(int kernel) {
   return kernel == VPM_KERNEL_WINCKELMANS ? kZeta0Winck : kZeta0Gauss;
@@ -117,6 +121,13 @@ __device__ inline void pair_qp_f64_winck(double r2, double s2, double k15, doubl
 
 __device__ inline void pair_qp_f64_gauss(double r2, double is2, double is1, double& q, double& p) {
   const double rho2 = r2 * is2;
+  if (rho2 >= kFarRho2D) {   // no erf or exp (see kFarRho2D)
+    const double ri = rsqrt(r2);
+    const double ri2 = ri * ri;
+    q = ri2 * ri;
+    p = -3.0 * q * ri2;
+    return;
+  }
   if (rho2 < kSeriesRho2D) {
     double h1, h2;
     GaussSeries<double, 14>::eval(rho2, h1, h2);
