@@ -562,8 +562,6 @@ __device__ __forceinline__ void near_accum2(float2 dx, float2 dy, float2 dz, flo
   acc[12] = fma2(q, gx, acc[12]);
   acc[13] = fma2(q, gy, acc[13]);
   acc[14] = fma2(q, gz, acc[14]);
-  if constexpr (NV == 27) {   // the α-derivative sums follow in the caller
-  }
 }
 
 // One source pair of a U/J (or U/J + DJ, D) near tile against this thread's
