@@ -353,8 +353,10 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
 // state (and the ζ passes' v, w) into that order, runs the same pair pass there
 // and scatters its outputs back.  Warps' targets and staged source blocks are
 // then compact whatever the caller's particle order, so that the far-field
-// forms of the Gaussian-erf kernel apply (uniform 262,144-particle box: 114 →
-// 88 ms).  Only the summation order changes; VPM_NO_SORT=1 turns it off.
+// forms of the Gaussian-erf kernel apply (uniform 262,144-particle box with the
+// scalar FP32 routines: 114 → 88 ms).  Only the summation order changes;
+// vpm_set_particle_order(VPM_ORDER_CALLER) keeps the caller's order for one
+// context, VPM_NO_SORT=1 everywhere.
 static bool sort_disabled() {
   static const bool off = [] {
     const char* v = std::getenv("VPM_NO_SORT");
