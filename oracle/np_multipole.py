@@ -104,3 +104,62 @@ def direct_singular(Y, G, x):
     eps[0, 2, 1] = eps[2, 1, 0] = eps[1, 0, 2] = -1.0
     J = np.einsum("j,ja,jb->ab", qr, c, d) + np.einsum("abc,j,jc->ab", eps, q, G)
     return U, -J / (4 * np.pi)
+
+
+# ---- local expansions (M2L, L2P) ------------------------------------------------
+# Restated from the same mathematics for a target group centred at z: with
+# R = x - c = (z - c) + y and ∂_{R_i} b_k = -(k_i + 1) b_{k+e_i},
+#     b_k((z - c) + y) = Σ_j (-1)^{|j|} C(k+j, j) b_{k+j}(z - c) y^j,
+# C(k+j, j) = Π_i (k_i + j_i)! / (k_i! j_i!), so the moments of a far cell give
+# the local coefficients of ψ (without 1/(4π)) about z,
+#     L_j^m = Σ_k M_k^m (-1)^{|j|} C(k+j, j) b_{k+j}(z - c),   |j| <= q,
+# and ψ_m(z + y) = Σ_j L_j^m y^j, with ∂ψ and ∂∂ψ from the polynomial.
+
+def _binom_multi(k, j):
+    from math import comb
+    return comb(k[0] + j[0], j[0]) * comb(k[1] + j[1], j[1]) * comb(k[2] + j[2], j[2])
+
+
+def local_from_moments(p, q, M, c, z):
+    """L[m, j] (3, ncoef(q)) about z from the moments M (3, ncoef(p)) of a cell at c."""
+    ks, js = multi_indices(p), multi_indices(q)
+    b = taylor_coefficients(p + q, np.asarray(z, np.float64) - np.asarray(c, np.float64))
+    L = np.zeros((3, len(js)))
+    for jj, j in enumerate(js):
+        sgn = -1.0 if sum(j) % 2 else 1.0
+        for kk, k in enumerate(ks):
+            kj = (k[0] + j[0], k[1] + j[1], k[2] + j[2])
+            L[:, jj] += sgn * _binom_multi(k, j) * b[midx(*kj)] * M[:, kk]
+    return L
+
+
+def local_to_target(q, L, z, x):
+    """U (3,) and J (3, 3) at x from the local coefficients L about z."""
+    js = multi_indices(q)
+    y = np.asarray(x, np.float64) - np.asarray(z, np.float64)
+
+    def mono(e):
+        return 0.0 if min(e) < 0 else float(np.prod(y ** np.array(e)))
+
+    dpsi = np.zeros((3, 3))          # [i, m] = ∂_i ψ_m
+    ddpsi = np.zeros((3, 3, 3))      # [i, l, m]
+    for jj, j in enumerate(js):
+        for i in range(3):
+            if j[i] == 0:
+                continue
+            ji = list(j); ji[i] -= 1
+            dpsi[i] += j[i] * mono(ji) * L[:, jj]
+            for l in range(3):
+                f = j[i] * (ji[l])
+                if f == 0:
+                    continue
+                jil = list(ji); jil[l] -= 1
+                ddpsi[i, l] += f * mono(jil) * L[:, jj]
+    dpsi /= 4 * np.pi
+    ddpsi /= 4 * np.pi
+    eps = np.zeros((3, 3, 3))
+    eps[0, 1, 2] = eps[1, 2, 0] = eps[2, 0, 1] = 1.0
+    eps[0, 2, 1] = eps[2, 1, 0] = eps[1, 0, 2] = -1.0
+    U = np.einsum("abc,bc->a", eps, dpsi)
+    J = np.einsum("acd,bcd->ab", eps, ddpsi)
+    return U, J

@@ -1,7 +1,8 @@
 """CPU checks of the treecode's far-field arithmetic (the NumPy restatement in
 oracle/np_multipole.py of what csrc/tree.cuh computes): the Taylor recurrence
-against finite differences, the graded multi-index layout, and the cell
-expansion against the direct singular Biot-Savart sum."""
+against finite differences, the graded multi-index layout, the cell expansion
+against the direct singular Biot-Savart sum, and local expansions about a
+target-group centre (M2L, L2P) against the cell expansion."""
 import numpy as np
 import pytest
 
@@ -48,3 +49,34 @@ def test_cell_expansion_converges_to_the_direct_sum(dist):
     # J is the gradient of U: trace-free
     U, J = mp.far_field(4, mp.moments(4, Y, G, c), c, x)
     assert abs(np.trace(J)) < 1e-9 * np.abs(J).max()
+
+
+def test_local_expansion_reproduces_the_cell_expansion():
+    # M2L then L2P about a target-group centre equals the cell's own expansion
+    # (M2P) at the group's targets up to the local truncation, which falls with
+    # the local order q.
+    rng = np.random.default_rng(12)
+    Y = rng.uniform(-0.1, 0.1, (200, 3))
+    G = rng.normal(0.0, 1.0, (200, 3))
+    c = np.zeros(3)
+    z = np.array([0.9, 0.35, -0.25])
+    X = z + rng.uniform(-0.1, 0.1, (20, 3))
+    p = 4
+    M = mp.moments(p, Y, G, c)
+    ref = [mp.far_field(p, M, c, x) for x in X]
+    errs = []
+    for q in (2, 4, 6, 8):
+        L = mp.local_from_moments(p, q, M, c, z)
+        got = [mp.local_to_target(q, L, z, x) for x in X]
+        eu = max(np.linalg.norm(g[0] - r[0]) / np.linalg.norm(r[0]) for g, r in zip(got, ref))
+        ej = max(np.linalg.norm(g[1] - r[1]) / np.linalg.norm(r[1]) for g, r in zip(got, ref))
+        errs.append((eu, ej))
+    for (eu0, ej0), (eu1, ej1) in zip(errs, errs[1:]):
+        assert eu1 < 0.3 * eu0 and ej1 < 0.3 * ej0
+    assert errs[2][0] < 1e-4 and errs[2][1] < 1e-3
+    # At the group centre the local expansion holds the cell expansion's
+    # derivatives exactly (no truncation in ψ, ∂ψ and ∂∂ψ there for q >= 2).
+    L = mp.local_from_moments(p, 2, M, c, z)
+    U, J = mp.local_to_target(2, L, z, z)
+    U0, J0 = mp.far_field(p, M, c, z)
+    assert np.allclose(U, U0, rtol=1e-12, atol=0) and np.allclose(J, J0, rtol=1e-10, atol=1e-14)
