@@ -107,6 +107,9 @@ def direct_singular(Y, G, x):
 
 
 # ---- local expansions (M2L, L2P) ------------------------------------------------
+# Not evaluated on the GPU: the treecode evaluates every far cell at every
+# target (M2P).  These are the operators of a far field evaluated once per
+# target group, checked here first.
 # Restated from the same mathematics for a target group centred at z: with
 # R = x - c = (z - c) + y and ∂_{R_i} b_k = -(k_i + 1) b_{k+e_i},
 #     b_k((z - c) + y) = Σ_j (-1)^{|j|} C(k+j, j) b_{k+j}(z - c) y^j,
