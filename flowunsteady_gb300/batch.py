@@ -42,8 +42,8 @@ class FieldBatch:
             pass
 
     def set_particle_order(self, mode):
-        """L.ORDER_AUTO (each field along its own Morton curve in FP32 passes)
-        or L.ORDER_CALLER (vpm_batch_set_particle_order)."""
+        """L.ORDER_AUTO (each field along its own Morton curve) or
+        L.ORDER_CALLER (vpm_batch_set_particle_order)."""
         self._check(L.lib().vpm_batch_set_particle_order(self._b, int(mode)))
 
     def set_field(self, f, X, Gamma, sigma):

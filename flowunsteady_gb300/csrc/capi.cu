@@ -348,7 +348,7 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
 
 // Enqueue the pair pass of one context (targets [t0,t1) of its own particles).
 // Large fields and batches are evaluated along a Morton curve: a full-range
-// FP32 pair pass sorts the particles by the Morton code of their position
+// pair pass sorts the particles by the Morton code of their position
 // (each field of a batch in its own cube and its own index range), gathers the
 // state (and the ζ passes' v, w) into that order, runs the same pair pass there
 // and scatters its outputs back.  Warps' targets and staged source blocks are
@@ -365,13 +365,13 @@ static bool sort_disabled() {
   return off;
 }
 
-static bool sorted_pass(const vpm_ctx* c, int prec, int64_t t0, int64_t t1) {
-  return !sort_disabled() && c->order == VPM_ORDER_AUTO && !c->bp && prec != VPM_PREC_FP64 &&
-         t0 == 0 && t1 == c->n && c->n >= 65536;
+static bool sorted_pass(const vpm_ctx* c, int64_t t0, int64_t t1) {
+  return !sort_disabled() && c->order == VPM_ORDER_AUTO && !c->bp && t0 == 0 && t1 == c->n &&
+         c->n >= 65536;
 }
 
-static bool sorted_batch(const vpm_ctx* c, int prec) {
-  return !sort_disabled() && c->order == VPM_ORDER_AUTO && prec != VPM_PREC_FP64;
+static bool sorted_batch(const vpm_ctx* c) {
+  return !sort_disabled() && c->order == VPM_ORDER_AUTO;
 }
 
 // Scratch of the sorted passes (allocated while planning, before any capture):
@@ -415,6 +415,7 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
                                    double* dj) {
   const int64_t n = c->n, ld = c->ld;
   const bool uj = pass == PASS_UJ || pass == PASS_UJD;
+  const bool recs = uj && prec != VPM_PREC_FP64;   // FP32 U/J passes read packed records
   cudaError_t e = cudaSuccess;
   const int* perm = nullptr;
   if (c->dry) {
@@ -424,11 +425,11 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
     if (!c->sortw || !c->srt || !c->sout) return cudaErrorInvalidValue;
     e = sort_order(c->sortw, n, c->X, ld, c->st, &perm);
     if (e == cudaSuccess) e = gather_inputs(c, perm, vs, ws);
-    if (e == cudaSuccess && uj)
+    if (e == cudaSuccess && recs)
       e = launch_pack_sources(kernel, n, c->srt, c->srt + 3 * ld, c->srt + 6 * ld, ld, scale,
                               c->rec, nullptr, c->st);
     if (e != cudaSuccess) return e;
-    c->launches += 3 + (uj ? 1 : 0);
+    c->launches += 3 + (recs ? 1 : 0);
   }
   PairCall pc;
   pc.pass = pass; pc.kernel = kernel; pc.prec = prec;
@@ -442,7 +443,7 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
   pc.ldo = ld;
   pc.status = c->status;
   pc.coh = nullptr;
-  if (uj) pc.rec = c->rec;
+  if (recs) pc.rec = c->rec;
   const Shape* pinned = &c->pinned[pass & 1][kernel][prec];
   PairPlan plan;
   plan.n_chunk = 1;
@@ -470,7 +471,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     const int nv = nval_of(pass);
     const size_t need = bp->max_chunks > 1 ? size_t(bp->max_chunks) * nv * size_t(c->ld) : 0;
     c->part_need = std::max(c->part_need, need);
-    const bool srt = sorted_batch(c, prec);
+    const bool srt = sorted_batch(c);
     if (c->dry) return srt ? sort_scratch(c, bp->nfields) : cudaSuccess;
     if (need > c->part_elems) return cudaErrorMemoryAllocation;
     const int64_t ld = c->ld;
@@ -522,7 +523,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     }
     return srt ? scatter_outputs(c, pass, perm, u, j, dj) : cudaSuccess;
   }
-  if (sorted_pass(c, prec, t0, t1))
+  if (sorted_pass(c, t0, t1))
     return ctx_pair_sorted(c, pass, kernel, prec, scale, vs, u, j, ws, dj);
   PairCall pc;
   pc.pass = pass; pc.kernel = kernel; pc.prec = prec;

@@ -188,7 +188,7 @@ class ParticleField:
             pass
 
     def set_particle_order(self, mode: int):
-        """L.ORDER_AUTO (default: FP32 passes over fields of 65,536 particles or
+        """L.ORDER_AUTO (default: pair passes over fields of 65,536 particles or
         more run along a Morton curve of the positions) or L.ORDER_CALLER (the
         field's own order, as FLOWVPM sums); vpm_set_particle_order."""
         L.check(L.lib().vpm_set_particle_order(self._ctx, int(mode)), self._ctx)

@@ -374,12 +374,12 @@ int vpm_set_tile(vpm_ctx* ctx, int kernel, int precision, const vpm_tile* t);
 
 /* Order in which the pair passes visit the particles (no counterpart in
  * FLOWVPM, whose sums run in the field's own order).
- *   VPM_ORDER_AUTO (default): FP32 and FP32C passes over all particles of a
- *     field of 65,536 or more, and every FP32/FP32C batch pass, sort the
- *     particles along a Morton curve of their positions (each batch field in
- *     its own cube), run there and scatter the results back to the caller's
- *     order.  Only the summation order changes; the Gaussian-erf far-field
- *     forms then apply whatever the caller's order.
+ *   VPM_ORDER_AUTO (default): pair passes over all particles of a field of
+ *     65,536 or more, and every batch pass, sort the particles along a Morton
+ *     curve of their positions (each batch field in its own cube), run there
+ *     and scatter the results back to the caller's order.  Only the summation
+ *     order changes; the Gaussian-erf far-field forms then apply whatever the
+ *     caller's order.
  *   VPM_ORDER_CALLER: the caller's order.
  * The environment variable VPM_NO_SORT=1 forces VPM_ORDER_CALLER everywhere. */
 enum { VPM_ORDER_AUTO = 0, VPM_ORDER_CALLER = 1 };

@@ -318,7 +318,7 @@ def test_morton_ordered_passes_match_original_order(oracle):
         with Ctx(n) as c:
             c.rc(c.lib.vpm_set_particle_order(c.p, mode))
             c.set(X, G, S)
-            if mode == L.ORDER_CALLER:   # FP64 passes keep the caller's order in both modes
+            if mode == L.ORDER_CALLER:   # the FP64 reference, in the caller's order
                 out["U64"], out["J64"] = c.uj(1, L.PREC_FP64)
                 sc64 = scheme(kernel=1, prec=L.PREC_FP64, sfs=L.SFS_DYNAMIC, flags=flags, nu=1e-4)
                 c.rc(c.lib.vpm_eval_sfs(c.p, ctypes.byref(sc64)))
