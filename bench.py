@@ -11,9 +11,10 @@ the Gaussian-erf kernel, FLOWUnsteady's default.
 Metric: pair interactions per second.  `value` is device time of the
 evaluation with the particle field resident in HBM; `e2e` is the same metric
 through the C ABI with host arrays (upload of X, Γ, σ and download of U, J
-inside the timed region).  The accuracy of the timed run (relative L2 of U, J
-and the stretching term against the GPU FP64 direct sum on sampled targets)
-and the FP64 throughput are reported beside it.
+inside the timed region, every step).  The accuracy of the timed run (relative
+L2 of U, J and the stretching term against the CPU FP64 oracle on the targets
+the CPU baseline sampled) and the GPU FP64 throughput on the same targets are
+reported beside it.
 
 `--impl reference` times the CPU FP64 restatement of the pair sum (the
 checker in oracle/, OpenMP over all host cores) on a bounded target sample of
@@ -43,8 +44,6 @@ PAIR_FLOP = 60          # algorithmic flop per U+∇U pair (FMA = 2)
 BYTES_H2D = 56          # X, Γ, σ per particle (FP64)
 BYTES_D2H = 96          # U (3) and J (9) per particle (FP64)
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one pair-kernel launch of the default workload,
-# from an ncu capture (profiles/launches_bench_helical_n262144.md).
 # DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch of the
 # benchmark workload per (N, tile shape), from ncu captures; the writes are
 # mostly the FP64 partial sums of the source chunks, so they depend on the shape.
@@ -161,9 +160,10 @@ def dist_setup(args):
     return world, rank, local, dist
 
 
-def cpu_pair_rate(X, G, S, kernel, seconds, seed=7):
+def cpu_pair_rate(X, G, S, kernel, seconds, seed=7, keep=None):
     """Pairs/s of the CPU FP64 direct sum (oracle, all host threads) on a
-    target sample sized to about `seconds` of work."""
+    target sample sized to about `seconds` of work.  When `keep` is a dict it
+    receives the sample's indices and the oracle's U and J there."""
     from oracle import oracle as O
     O.build()
     rng = np.random.default_rng(seed)
@@ -180,10 +180,12 @@ def cpu_pair_rate(X, G, S, kernel, seconds, seed=7):
         m = min(n, m * 4)
     rate = m * n / t
     m_final = int(min(n, max(m, rate * seconds / n)))
-    idx = rng.choice(n, m_final, replace=False)
+    idx = np.sort(rng.choice(n, m_final, replace=False))
     t0 = time.perf_counter()
-    O.uj_direct(kernel, X, G, S, Xt=X[idx])
+    U, J = O.uj_direct(kernel, X, G, S, Xt=X[idx])
     t = time.perf_counter() - t0
+    if keep is not None:
+        keep.update(idx=idx, U=U, J=J)
     return m_final * n / t, m_final, t, O.max_threads()
 
 
@@ -338,22 +340,37 @@ def run_ours(args, world, rank, local, dist):
         return None
 
     # ---- end to end through the C ABI with host buffers ------------------------
+    # As many steps as the device-timed region; each uploads X, Γ, σ from host
+    # arrays, evaluates and downloads U, J (host clock around the whole step).
     U = np.empty((n, 3))
     J = np.empty((n, 9))
     e2e_t = []
-    for k in range(max(1, min(args.steps, 3))):
+    for k in range(args.steps):
+        flush.fill_(float(k))
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         L.check(lib.vpm_set_particles(ctx, n, L.dptr(X), 3, L.dptr(G), 3, L.dptr(S), 1), ctx)
         L.check(lib.vpm_eval_UJ(ctx, kernel, prec), ctx)
         L.check(lib.vpm_get_UJ(ctx, 0, n, L.dptr(U), 3, L.dptr(J), 9), ctx)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_value = world * pairs / (sum(e2e_t) / len(e2e_t))
+    e2e_value, _ = aggregate(sum(e2e_t), args.steps, pairs, world, dist, dev)
+
+    # ---- CPU baseline; its target sample doubles as the accuracy reference -----
+    cpu = None
+    ref = {}
+    if rank == 0 and world == 1:
+        rate, mt, tt, cores = cpu_pair_rate(X, G, S, kernel, args.cpu_seconds, keep=ref)
+        cpu = {"value": rate, "unit": "pairs/s", "cores": cores, "kind": "port",
+               "sample": f"{mt} random targets x {n} sources ({tt:.1f} s), FP64 oracle, "
+                         f"OpenMP on {cpu_model()}"}
 
     # ---- accuracy of the timed result and FP64 throughput on sampled targets ---
-    rng = np.random.default_rng(2026)
-    m = min(args.sample_targets, n)
-    idx = np.sort(rng.choice(n, m, replace=False))
+    if ref:
+        idx = ref["idx"]
+    else:
+        rng = np.random.default_rng(2026)
+        idx = np.sort(rng.choice(n, min(args.sample_targets, n), replace=False))
+    m = idx.size
     Xs_d = torch.tensor(X.T.copy(), device=dev)
     Gs_d = torch.tensor(G.T.copy(), device=dev)
     Ss_d = torch.tensor(S, device=dev)
@@ -385,8 +402,16 @@ def run_ours(args, world, rank, local, dist):
     def rl2(a, b):
         return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
-    acc = {"U": rl2(Uf, U64), "J": rl2(Jf, J64), "stretching": rl2(Sf, S64),
-           "reference": f"GPU FP64 direct sum on {m} sampled targets"}
+    if ref:
+        # Against the CPU FP64 oracle; the GPU FP64 sum at the same targets too.
+        Uo, Jo = ref["U"], ref["J"]
+        So = np.einsum("iba,ib->ia", Jo, G[idx])
+        acc = {"U": rl2(Uf, Uo), "J": rl2(Jf, Jo), "stretching": rl2(Sf, So),
+               "fp64_U": rl2(U64, Uo), "fp64_J": rl2(J64, Jo),
+               "reference": f"CPU FP64 oracle (oracle/) on {m} sampled targets"}
+    else:
+        acc = {"U": rl2(Uf, U64), "J": rl2(Jf, J64), "stretching": rl2(Sf, S64),
+               "reference": f"GPU FP64 direct sum on {m} sampled targets"}
 
     # ---- roofline of the dominant kernel (the pair kernel) ------------------------
     achieved = PAIR_FLOP * pairs / (ms_per_step / 1e3) / 1e12
@@ -400,12 +425,6 @@ def run_ours(args, world, rank, local, dist):
 
     line = None
     if rank == 0:
-        cpu = None
-        if world == 1:
-            rate, mt, tt, cores = cpu_pair_rate(X, G, S, kernel, args.cpu_seconds)
-            cpu = {"value": rate, "unit": "pairs/s", "cores": cores, "kind": "port",
-                   "sample": f"{mt} random targets x {n} sources ({tt:.1f} s), FP64 oracle, "
-                             f"OpenMP on {cpu_model()}"}
         line = {
             "metric": "U+∇U pair-interactions/s",
             "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,

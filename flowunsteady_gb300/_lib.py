@@ -47,14 +47,15 @@ RELAX_PEDRIZZETTI = 1
 
 DIAG_NAMES = ["enstrophy", "impulse_x", "impulse_y", "impulse_z", "gamma_x", "gamma_y",
               "gamma_z", "cd_mean", "cd_std", "cd_zero_ratio", "cd_min", "cd_max",
-              "sigma_mean", "nonfinite"]
+              "sigma_mean", "nonfinite", "cd_skew", "cd_kurt"]
 DIAG_COUNT = len(DIAG_NAMES)
 
 # Every symbol include/vpm_gpu.h declares.
 EXPORTS = [
     "vpm_scheme_default", "vpm_ctx_create", "vpm_ctx_destroy", "vpm_last_error",
     "vpm_ctx_set_stream", "vpm_get_time", "vpm_set_time", "vpm_set_particles", "vpm_append",
-    "vpm_truncate", "vpm_get_np", "vpm_get_state", "vpm_get_sfs", "vpm_eval_UJ",
+    "vpm_truncate", "vpm_get_np", "vpm_get_state", "vpm_get_sfs", "vpm_set_attributes",
+    "vpm_get_attributes", "vpm_eval_UJ",
     "vpm_eval_UJ_targets", "vpm_get_UJ", "vpm_eval_sfs", "vpm_step", "vpm_diagnostics",
     "vpm_centroids", "vpm_ffv_direct", "vpm_fmm_default", "vpm_eval_UJ_fmm", "vpm_fmm_stats",
     "vpm_save", "vpm_load",
@@ -62,7 +63,7 @@ EXPORTS = [
     "vpm_batch_last_error", "vpm_batch_set_stream", "vpm_batch_set_field",
     "vpm_batch_get_field", "vpm_batch_eval_UJ", "vpm_batch_get_UJ", "vpm_batch_step",
     "vpm_autotune", "vpm_set_tile", "vpm_set_particle_order", "vpm_batch_set_particle_order",
-    "vpm_measure_fma_peaks", "vpm_debug_fail_after",
+    "vpm_measure_fma_peaks", "vpm_debug_fail_after", "vpm_debug_last_plan",
     "vpm_get_launch_count", "vpm_build_info",
 ]
 
@@ -143,6 +144,9 @@ def _declare(lib):
         "vpm_get_np": (ctypes.c_int, [_vp, P(_i64), P(_i64)]),
         "vpm_get_state": (ctypes.c_int, [_vp, _i64, _dp, _i64, _dp, _i64, _dp, _i64]),
         "vpm_get_sfs": (ctypes.c_int, [_vp, _i64, _dp, _i64, _dp, _i64]),
+        "vpm_set_attributes": (ctypes.c_int, [_vp, _i64, _i64, _dp, _i64, _dp, _i64, _dp, _i64]),
+        "vpm_get_attributes": (ctypes.c_int, [_vp, _i64, _i64, _dp, _i64, _dp, _i64,
+                                              P(ctypes.c_int32)]),
         "vpm_eval_UJ": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
         "vpm_eval_UJ_targets": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _i64, _i64]),
         "vpm_get_UJ": (ctypes.c_int, [_vp, _i64, _i64, _dp, _i64, _dp, _i64]),
@@ -178,6 +182,8 @@ def _declare(lib):
         "vpm_batch_set_particle_order": (ctypes.c_int, [_vp, ctypes.c_int]),
         "vpm_measure_fma_peaks": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
         "vpm_debug_fail_after": (ctypes.c_int, [_vp, _i64]),
+        "vpm_debug_last_plan": (ctypes.c_int, [P(ctypes.c_int32), P(ctypes.c_int32),
+                                               P(ctypes.c_int32)]),
         "vpm_get_launch_count": (ctypes.c_int, [_vp, P(_i64)]),
         "vpm_build_info": (ctypes.c_char_p, []),
     }

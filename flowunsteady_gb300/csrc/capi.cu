@@ -79,8 +79,10 @@ int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int 
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
   int per = pair_ctas_per_sm(pass, kernel, precision, s);
-  int r = std::max(1, per) * num_sms;
-  cache[key] = r;
+  // A failed occupancy query or SM count leaves at least one resident CTA;
+  // only a successful answer is cached.
+  int r = std::max(1, per) * std::max(1, num_sms);
+  if (per > 0 && num_sms > 0) cache[key] = r;
   return r;
 }
 
@@ -92,6 +94,7 @@ int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chun
   int best_c = 1;
   int64_t best_chunk = std::max<int64_t>(ns, 1);
   double best = -1.0;
+  resident = std::max(resident, 1);
   const int cmax = max_chunks > 0 ? std::min(max_chunks, 128) : 128;
   for (int c = 1; c <= cmax; ++c) {
     int64_t chunk = round_up(std::max<int64_t>(ceil_div(ns, c), 1), block);
@@ -252,11 +255,13 @@ int ensure_test_filter(vpm_ctx* c) {
   return VPM_OK;
 }
 
-// Host strided AoS -> pinned SoA staging -> device rows [i0, i0+n).
+// Host strided AoS -> pinned SoA staging -> device rows [i0, i0+n).  New
+// particles get volume 0, circulation 1, empty SFS memory and the static flag
+// is_static.
 int upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const double* G,
-           int64_t sg, const double* S, int64_t ss) {
+           int64_t sg, const double* S, int64_t ss, int is_static) {
   if (n == 0) return VPM_OK;
-  int rc = ensure_stage(c, size_t(7) * n);
+  int rc = ensure_stage(c, size_t(9) * n);
   if (rc) return rc;
   double* h = c->h_stage;
   for (int64_t i = 0; i < n; ++i) {
@@ -265,15 +270,41 @@ int upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const
       h[(3 + k) * n + i] = G[i * sg + k];
     }
     h[6 * n + i] = S[i * ss];
+    h[7 * n + i] = 0.0;
+    h[8 * n + i] = 1.0;
   }
   const size_t w = size_t(n) * sizeof(double), dp = size_t(c->ld) * sizeof(double);
   CTX_CK(c, cudaMemcpy2DAsync(c->X + i0, dp, h, w, w, 3, cudaMemcpyHostToDevice, c->st));
   CTX_CK(c, cudaMemcpy2DAsync(c->G + i0, dp, h + 3 * n, w, w, 3, cudaMemcpyHostToDevice, c->st));
   CTX_CK(c, cudaMemcpyAsync(c->S + i0, h + 6 * n, w, cudaMemcpyHostToDevice, c->st));
+  CTX_CK(c, cudaMemcpyAsync(c->vol + i0, h + 7 * n, w, cudaMemcpyHostToDevice, c->st));
+  CTX_CK(c, cudaMemcpyAsync(c->circ + i0, h + 8 * n, w, cudaMemcpyHostToDevice, c->st));
+  CTX_CK(c, cudaMemsetAsync(c->stat + i0, is_static ? 1 : 0, size_t(n), c->st));
   // Fresh particles start with empty SFS memory.
   CTX_CK(c, cudaMemset2DAsync(c->C + i0, dp, 0, w, 3, c->st));
   CTX_CK(c, cudaStreamSynchronize(c->st));
   return VPM_OK;
+}
+
+// The particles the O(N) update kernels visit, and the flags they test: the
+// free prefix [0, n - n_static) without flags when the static particles form
+// the tail, else every particle with its flag.
+void update_range(const vpm_ctx* c, int64_t* nv, const uint8_t** stat) {
+  if (static_tail(c)) {
+    *nv = c->n - c->n_static;
+    *stat = nullptr;
+  } else {
+    *nv = c->n;
+    *stat = c->stat;
+  }
+}
+
+// Host bookkeeping of the static flags after particles [n0, n1) were added.
+void note_added(vpm_ctx* c, int64_t n0, int64_t n1, bool is_static) {
+  c->hstat.resize(size_t(n1), 0);
+  for (int64_t i = n0; i < n1; ++i) c->hstat[size_t(i)] = is_static ? 1 : 0;
+  if (is_static) c->n_static += n1 - n0;
+  else if (n1 > n0) c->last_free = n1;
 }
 
 int validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double* G, int64_t sg,
@@ -622,7 +653,10 @@ static cudaError_t zeta_pass(vpm_ctx* c, const vpm_scheme* s, bool d, const doub
 // computes C_d).  In the analytic form the first stage runs the α-derivative
 // passes (U/J + DJ, then ζ + Dζ) instead of separate passes at σ and ασ.
 static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
-  const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
+  const int64_t n = c->n, ld = c->ld;
+  int64_t nf = 0;
+  const uint8_t* stat = nullptr;
+  update_range(c, &nf, &stat);
   const int K = s->kernel, P = s->precision;
   const bool sfs = s->sfs != VPM_SFS_NONE;
   const bool dyn0 = s->sfs == VPM_SFS_DYNAMIC && stage == 0;
@@ -646,7 +680,7 @@ static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
     }
   }
   if (s->sfs == VPM_SFS_CONSTANT) {
-    ENQ(c, launch_sfs_constant(nf, s->sfs_Cd, c->C, c->st));
+    ENQ(c, launch_sfs_constant(nf, stat, s->sfs_Cd, c->C, c->st));
   } else if (dyn0) {
     const double al = s->sfs_alpha;
     if (!analytic) {
@@ -660,7 +694,8 @@ static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
     sp.zeta0 = zeta0_of(K); sp.inv_zeta0 = 1.0 / sp.zeta0; sp.transposed = s->transposed;
     sp.force_positive = (s->sfs_flags & VPM_SFS_FORCE_POSITIVE) ? 1 : 0;
     sp.analytic = analytic ? 1 : 0;
-    ENQ(c, launch_sfs_dynamic(nf, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp, c->st));
+    ENQ(c, launch_sfs_dynamic(nf, stat, ld, c->G, c->S, c->J, c->Jt, c->E, c->Et, c->C, sp,
+                              c->st));
   }
   return cudaSuccess;
 }
@@ -668,10 +703,12 @@ static cudaError_t enqueue_uj_sfs(vpm_ctx* c, const vpm_scheme* s, int stage) {
 // One stage of a step: U/J, SFS, fused update.
 static cudaError_t enqueue_stage(vpm_ctx* c, const vpm_scheme* s, double dt, double a, double b,
                                  int stage) {
-  const int64_t n = c->n, nf = n - c->n_static, ld = c->ld;
+  const int64_t ld = c->ld;
+  int64_t nf = 0;
+  const uint8_t* stat = nullptr;
+  update_range(c, &nf, &stat);
   const int K = s->kernel;
   const bool sfs = s->sfs != VPM_SFS_NONE;
-  (void)n;
   ENQP(c, enqueue_uj_sfs(c, s, stage));
   UpdateParams up;
   up.a = a; up.b = b; up.dt = dt;
@@ -684,8 +721,8 @@ static cudaError_t enqueue_stage(vpm_ctx* c, const vpm_scheme* s, double dt, dou
   up.transposed = s->transposed;
   up.sfs = sfs ? 1 : 0;
   up.clip_backscatter = (sfs && (s->sfs_flags & VPM_SFS_CLIP_BACKSCATTER)) ? 1 : 0;
-  ENQ(c, launch_rk_update(nf, ld, c->X, c->G, c->S, c->U, c->J, c->E, c->C, c->Q, up, c->status,
-                          c->st));
+  ENQ(c, launch_rk_update(nf, stat, ld, c->X, c->G, c->S, c->U, c->J, c->E, c->C, c->Q, up,
+                          c->status, c->st));
   return cudaSuccess;
 }
 
@@ -700,7 +737,10 @@ static cudaError_t enqueue_step(vpm_ctx* c, const vpm_scheme* s, double dt, bool
   if (relax) {
     // Relaxation after the step on a fresh U/J (vpm.pedrizzetti).
     ENQP(c, uj_pass(c, s));
-    ENQ(c, launch_relax(c->n - c->n_static, c->ld, c->J, c->G, s->relax_factor, c->st));
+    int64_t nf = 0;
+    const uint8_t* stat = nullptr;
+    update_range(c, &nf, &stat);
+    ENQ(c, launch_relax(nf, stat, c->ld, c->J, c->G, s->relax_factor, c->st));
   }
   return cudaSuccess;
 }
@@ -728,7 +768,24 @@ int ctx_validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const 
 int ctx_upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const double* G,
                int64_t sg, const double* S, int64_t ss) {
   DeviceGuard dg(c->device);
-  return upload(c, i0, n, X, sx, G, sg, S, ss);
+  return upload(c, i0, n, X, sx, G, sg, S, ss, 0);
+}
+int ctx_set_static_flags(vpm_ctx* c, const uint8_t* flags, int64_t n) {
+  if (n != c->n) return ctx_fail(c, VPM_ERR_INVALID, "static flags must cover every particle");
+  DeviceGuard dg(c->device);
+  c->hstat.assign(flags, flags + n);
+  c->n_static = 0;
+  c->last_free = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    c->hstat[size_t(i)] = c->hstat[size_t(i)] ? 1 : 0;
+    if (c->hstat[size_t(i)]) ++c->n_static;
+    else c->last_free = i + 1;
+  }
+  if (n > 0) {
+    CTX_CK(c, cudaMemcpyAsync(c->stat, c->hstat.data(), size_t(n), cudaMemcpyHostToDevice, c->st));
+    CTX_CK(c, cudaStreamSynchronize(c->st));
+  }
+  return VPM_OK;
 }
 int ctx_download_rows(vpm_ctx* c, const double* dev, int rows, int64_t i0, int64_t n, double* out,
                       int64_t stride) {
@@ -788,8 +845,8 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   std::memset(c->pinned, 0, sizeof(c->pinned));
   const size_t ld = size_t(c->ld);
-  // State + evaluation rows: X3 G3 S1 C3 Q8 U3 J9 E3 V6 raw12 = 51 rows.
-  const size_t rows = 51;
+  // State + evaluation rows: X3 G3 S1 C3 Q8 U3 J9 E3 V6 raw12 vol1 circ1 = 53 rows.
+  const size_t rows = 53;
   if (cudaMalloc(&c->base, rows * ld * sizeof(double)) != cudaSuccess) {
     delete c;
     return set_error(nullptr, VPM_ERR_NOMEM, "cannot allocate the particle field");
@@ -805,7 +862,11 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   c->E = p; p += 3 * ld;
   c->V = p; p += 6 * ld;      // v rows 0..2, w rows 3..5
   c->raw = p; p += 12 * ld;   // raw ζ sums (12 rows for the α-derivative pass)
+  c->vol = p; p += ld;
+  c->circ = p; p += ld;
   cudaError_t e = cudaMemset(c->base, 0, rows * ld * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c->stat, size_t(c->ld));
+  if (e == cudaSuccess) e = cudaMemset(c->stat, 0, size_t(c->ld));
   if (e == cudaSuccess) e = cudaMalloc(&c->rec, 3 * ld * sizeof(float4));
   // Until the first packing the particle order counts as coherent.
   if (e == cudaSuccess) e = cudaMalloc(&c->coh, sizeof(unsigned int));
@@ -841,6 +902,7 @@ int vpm_ctx_destroy(vpm_ctx* c) {
   cudaFree(c->sout);
   cudaFree(c->status);
   cudaFree(c->red);
+  cudaFree(c->stat);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   delete c;
   return VPM_OK;
@@ -884,10 +946,13 @@ int vpm_set_particles(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const 
   int rc = validate_host(c, n, X, sx, G, sg, S, ss);
   if (rc) return rc;
   DeviceGuard dg(c->device);
-  rc = upload(c, 0, n, X, sx, G, sg, S, ss);
+  rc = upload(c, 0, n, X, sx, G, sg, S, ss, 0);
   if (rc) return rc;
   c->n = n;
   c->n_static = 0;
+  c->last_free = 0;
+  c->hstat.clear();
+  note_added(c, 0, n, false);
   c->uj_lo = c->uj_hi = 0;
   return VPM_OK;
 }
@@ -897,23 +962,26 @@ int vpm_append(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const double*
   if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
   if (n < 0) return ctx_fail(c, VPM_ERR_INVALID, "negative particle count");
   if (c->n + n > c->cap) return ctx_fail(c, VPM_ERR_CAPACITY, "particle count above capacity");
-  if (!is_static && c->n_static > 0 && n > 0)
-    return ctx_fail(c, VPM_ERR_STATE, "free particles cannot follow static particles");
   int rc = validate_host(c, n, X, sx, G, sg, S, ss);
   if (rc) return rc;
   DeviceGuard dg(c->device);
-  rc = upload(c, c->n, n, X, sx, G, sg, S, ss);
+  rc = upload(c, c->n, n, X, sx, G, sg, S, ss, is_static);
   if (rc) return rc;
+  note_added(c, c->n, c->n + n, is_static != 0);
   c->n += n;
-  if (is_static) c->n_static += n;
   return VPM_OK;
 }
 
 int vpm_truncate(vpm_ctx* c, int64_t n) {
   if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
   if (n < 0 || n > c->n) return ctx_fail(c, VPM_ERR_INVALID, "truncate beyond particle count");
-  const int64_t removed = c->n - n;
-  c->n_static = std::max<int64_t>(0, c->n_static - removed);
+  for (int64_t i = n; i < c->n; ++i) c->n_static -= c->hstat[size_t(i)];
+  c->hstat.resize(size_t(n));
+  if (c->last_free > n) {
+    int64_t lf = n;
+    while (lf > 0 && c->hstat[size_t(lf - 1)]) --lf;
+    c->last_free = lf;
+  }
   c->n = n;
   c->uj_hi = std::min(c->uj_hi, n);
   c->uj_lo = std::min(c->uj_lo, c->uj_hi);
@@ -944,6 +1012,54 @@ int vpm_get_sfs(vpm_ctx* c, int64_t n, double* C, int64_t sc, double* E, int64_t
   DeviceGuard dg(c->device);
   int rc = download_rows(c, c->C, 3, 0, n, C, sc);
   if (!rc) rc = download_rows(c, c->E, 3, 0, n, E, se);
+  return rc;
+}
+
+int vpm_set_attributes(vpm_ctx* c, int64_t i0, int64_t n, const double* vol, int64_t svol,
+                       const double* circulation, int64_t scirc, const double* C, int64_t sc) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0 || i0 < 0 || i0 + n > c->n) return ctx_fail(c, VPM_ERR_INVALID, "range beyond particle count");
+  if ((vol && svol < 1) || (circulation && scirc < 1) || (C && sc < 3))
+    return ctx_fail(c, VPM_ERR_INVALID, "stride too small");
+  for (int64_t i = 0; i < n; ++i) {
+    if ((vol && !std::isfinite(vol[i * svol])) ||
+        (circulation && !std::isfinite(circulation[i * scirc])))
+      return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite particle attribute");
+    for (int k = 0; C && k < 3; ++k)
+      if (!std::isfinite(C[i * sc + k])) return ctx_fail(c, VPM_ERR_NONFINITE, "non-finite SFS memory");
+  }
+  if (n == 0) return VPM_OK;
+  DeviceGuard dg(c->device);
+  int rc = ensure_stage(c, size_t(5) * n);
+  if (rc) return rc;
+  double* h = c->h_stage;
+  const size_t w = size_t(n) * sizeof(double), dp = size_t(c->ld) * sizeof(double);
+  if (vol) {
+    for (int64_t i = 0; i < n; ++i) h[i] = vol[i * svol];
+    CTX_CK(c, cudaMemcpyAsync(c->vol + i0, h, w, cudaMemcpyHostToDevice, c->st));
+  }
+  if (circulation) {
+    for (int64_t i = 0; i < n; ++i) h[n + i] = circulation[i * scirc];
+    CTX_CK(c, cudaMemcpyAsync(c->circ + i0, h + n, w, cudaMemcpyHostToDevice, c->st));
+  }
+  if (C) {
+    for (int64_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) h[(2 + k) * n + i] = C[i * sc + k];
+    CTX_CK(c, cudaMemcpy2DAsync(c->C + i0, dp, h + 2 * n, w, w, 3, cudaMemcpyHostToDevice, c->st));
+  }
+  CTX_CK(c, cudaStreamSynchronize(c->st));
+  return VPM_OK;
+}
+
+int vpm_get_attributes(vpm_ctx* c, int64_t i0, int64_t n, double* vol, int64_t svol,
+                       double* circulation, int64_t scirc, int32_t* is_static) {
+  if (!c) return set_error(nullptr, VPM_ERR_INVALID, "null context");
+  if (n < 0 || i0 < 0 || i0 + n > c->n) return ctx_fail(c, VPM_ERR_INVALID, "range beyond particle count");
+  DeviceGuard dg(c->device);
+  int rc = download_rows(c, c->vol, 1, i0, n, vol, svol);
+  if (!rc) rc = download_rows(c, c->circ, 1, i0, n, circulation, scirc);
+  if (!rc && is_static)
+    for (int64_t i = 0; i < n; ++i) is_static[i] = c->hstat[size_t(i0 + i)];
   return rc;
 }
 
@@ -1071,6 +1187,7 @@ int vpm_step(vpm_ctx* c, double dt, const vpm_scheme* s, int64_t nsteps, int use
     if (use_graph) {
       GraphKey key;
       key.n = c->n; key.n_static = c->n_static; key.dt = dt; key.relax = relax;
+      key.mixed = static_tail(c) ? 0 : 1;
       key.scheme = *s;
       cudaGraphExec_t exec = nullptr;
       for (auto& g : c->graphs)
@@ -1126,7 +1243,10 @@ int vpm_diagnostics(vpm_ctx* c, int kernel, int precision, double* out) {
   int rc = check_inject(c);
   if (rc) return rc;
   DeviceGuard dg(c->device);
-  const int64_t n = c->n, nf = n - c->n_static;
+  const int64_t n = c->n, nfree = n - c->n_static;
+  int64_t nf = 0;
+  const uint8_t* stat = nullptr;
+  update_range(c, &nf, &stat);
   for (int k = 0; k < VPM_DIAG_COUNT; ++k) out[k] = 0.0;
   if (n == 0) return VPM_OK;
   c->dry = true;
@@ -1137,7 +1257,7 @@ int vpm_diagnostics(vpm_ctx* c, int kernel, int precision, double* out) {
   CTX_CK(c, ctx_pair(c, PASS_ZETA, kernel, precision, 0, n, 1.0, nullptr, c->raw, nullptr));
   double* partial = c->red;
   double* dout = c->red + size_t(kRedBlocks) * kDiagSlots;
-  CTX_CK(c, launch_diagnostics(n, nf, c->ld, c->X, c->G, c->S, c->C, c->raw, zeta0_of(kernel),
+  CTX_CK(c, launch_diagnostics(n, nf, stat, c->ld, c->X, c->G, c->S, c->C, c->raw, zeta0_of(kernel),
                                partial, dout, c->st));
   c->launches += 2;
   double v[kDiagSlots];
@@ -1151,13 +1271,23 @@ int vpm_diagnostics(vpm_ctx* c, int kernel, int precision, double* out) {
   out[VPM_DIAG_GAMMA_Y] = v[DS_GY];
   out[VPM_DIAG_GAMMA_Z] = v[DS_GZ];
   if (v[DS_CCNT] > 0) {
-    const double mean = v[DS_CSUM] / v[DS_CCNT];
+    // Population moments of the nonzero C_d from the raw power sums.
+    const double cnt = v[DS_CCNT];
+    const double mean = v[DS_CSUM] / cnt;
+    const double p2 = v[DS_CSUM2] / cnt, p3 = v[DS_CSUM3] / cnt, p4 = v[DS_CSUM4] / cnt;
+    const double m2 = std::max(0.0, p2 - mean * mean);
+    const double m3 = p3 - 3.0 * mean * p2 + 2.0 * mean * mean * mean;
+    const double m4 = p4 - 4.0 * mean * p3 + 6.0 * mean * mean * p2 - 3.0 * mean * mean * mean * mean;
     out[VPM_DIAG_CD_MEAN] = mean;
-    out[VPM_DIAG_CD_STD] = std::sqrt(std::max(0.0, v[DS_CSUM2] / v[DS_CCNT] - mean * mean));
+    out[VPM_DIAG_CD_STD] = std::sqrt(m2);
     out[VPM_DIAG_CD_MIN] = v[DS_CMIN];
     out[VPM_DIAG_CD_MAX] = v[DS_CMAX];
+    if (m2 > 0.0) {
+      out[VPM_DIAG_CD_SKEW] = m3 / (m2 * std::sqrt(m2));
+      out[VPM_DIAG_CD_KURT] = m4 / (m2 * m2) - 3.0;
+    }
   }
-  out[VPM_DIAG_CD_ZERO_RATIO] = nf > 0 ? v[DS_CZERO] / double(nf) : 0.0;
+  out[VPM_DIAG_CD_ZERO_RATIO] = nfree > 0 ? v[DS_CZERO] / double(nfree) : 0.0;
   out[VPM_DIAG_SIGMA_MEAN] = v[DS_SIG] / double(n);
   out[VPM_DIAG_NONFINITE] = v[DS_NONFIN];
   return VPM_OK;

@@ -45,6 +45,10 @@ struct PairPlan {
   int64_t chunk;
 };
 
+// Plan of the last stateless U/J call (vpm_uj_device_async/_noalloc) on this
+// host thread, for vpm_debug_last_plan.
+extern thread_local PairPlan g_last_stateless_plan;
+
 Shape default_shape(int pass, int precision, int64_t n);
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n, const Shape* pinned);
 void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s);
@@ -66,6 +70,7 @@ struct GraphKey {
   int64_t n, n_static;
   double dt;
   int64_t relax;
+  int64_t mixed;   // static particles not (only) at the tail: flag-tested updates
   vpm_scheme scheme;
 };
 
@@ -156,7 +161,20 @@ struct vpm_ctx {
   int64_t ffv_cap = 0;
   int64_t launches = 0;           // kernels enqueued (graph replays add their kernel count)
   int64_t step_launches = 0;      // kernels of one captured step (counted while enqueuing)
+  // Per-particle values the method carries but does not use: volume and
+  // circulation rows (FLOWVPM's get_vol / get_circulation).
+  double *vol = nullptr, *circ = nullptr;
+  // Static (source-only) particles: a device flag per particle, its host copy
+  // for particles [0, n), and one past the last free particle.  When the
+  // static particles are exactly the tail [n - n_static, n) the update
+  // kernels run over [0, n - n_static) without reading the flags.
+  uint8_t* stat = nullptr;
+  std::vector<uint8_t> hstat;
+  int64_t last_free = 0;
 };
+
+// True when the static particles are exactly the tail of the field.
+inline bool static_tail(const vpm_ctx* c) { return c->last_free == c->n - c->n_static; }
 
 // Pair pass of a context over targets [t0, t1) of its own particles (queue form
 // when the context backs a batch).
@@ -170,6 +188,9 @@ int ctx_validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const 
                       int64_t sg, const double* S, int64_t ss);
 int ctx_upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const double* G,
                int64_t sg, const double* S, int64_t ss);
+// Static flags of particles [0, n) from a host array (nonzero = static); the
+// particles must already be on the device.
+int ctx_set_static_flags(vpm_ctx* c, const uint8_t* flags, int64_t n);
 int ctx_download_rows(vpm_ctx* c, const double* dev, int rows, int64_t i0, int64_t n, double* out,
                       int64_t stride);
 int ctx_prepare_scratch(vpm_ctx* c, int kernel, int precision);

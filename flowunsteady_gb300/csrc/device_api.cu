@@ -10,6 +10,10 @@
 
 using namespace vpm;
 
+namespace vpm {
+thread_local PairPlan g_last_stateless_plan = {Shape{0, 0}, 0, 0, 0};
+}  // namespace vpm
+
 extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const double* Xs,
                                    const double* Gs, const double* Ss, int64_t ld_s, int64_t nt,
                                    const double* Xt, int64_t ld_t, double* U, double* J,
@@ -32,8 +36,11 @@ extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const 
   }
   cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
   int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t qe = cudaGetDevice(&dev);
+  if (qe == cudaSuccess) qe = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (qe != cudaSuccess || sms <= 0)
+    return set_error(nullptr, VPM_ERR_CUDA,
+                     std::string("querying the current device: ") + cudaGetErrorString(qe));
   PairCall pc;
   pc.pass = PASS_UJ; pc.kernel = kernel; pc.prec = precision;
   pc.t0 = 0; pc.t1 = nt; pc.ns = ns;
@@ -42,7 +49,8 @@ extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const 
   pc.sigma_scale = 1.0;
   pc.u = U; pc.j = J; pc.ldo = ld_o;
   size_t need = 0;
-  run_pair(pc, dev, sms, nullptr, nullptr, nt, 0, &need, true, st, nullptr);
+  PairPlan plan;
+  run_pair(pc, dev, sms, nullptr, nullptr, nt, 0, &need, true, st, &plan);
   double* part = nullptr;
   if (need > 0) {
     cudaError_t e = cudaMallocAsync(&part, need * sizeof(double), st);
@@ -66,5 +74,14 @@ extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const 
   if (part) cudaFreeAsync(part, st);
   if (e != cudaSuccess)
     return set_error(nullptr, VPM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  g_last_stateless_plan = plan;
+  return VPM_OK;
+}
+
+extern "C" int vpm_debug_last_plan(int32_t* block, int32_t* tpt, int32_t* n_chunk) {
+  const PairPlan& p = g_last_stateless_plan;
+  if (block) *block = p.shape.block;
+  if (tpt) *tpt = p.shape.tpt;
+  if (n_chunk) *n_chunk = p.n_chunk;
   return VPM_OK;
 }

@@ -274,10 +274,13 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           const bool ok = mbar_wait(bar, phase);
           phase ^= 1u;
           if (__syncthreads_or(!ok)) {
-            // A copy did not complete in time: record it, give the copies in
-            // flight a second bounded wait, and leave together.
+            // A copy did not complete in time: record it, drain it with a
+            // second, longer bounded wait, and leave together.  At most one
+            // copy is ever in flight (the next tile's copy is issued only
+            // after this wait succeeded and the records were consumed), so the
+            // copy just waited on is the only one that could land late.
             if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
-            mbar_wait(bar, phase ^ 1u);
+            mbar_wait(bar, phase ^ 1u, 1 << 26);
             return;
           }
           const int64_t jj = tile0 + tid;

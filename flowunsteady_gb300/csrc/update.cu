@@ -91,15 +91,23 @@ __global__ void estr_finish_d_kernel(int64_t n, int64_t ld, const double* __rest
   DE[2 * ld + i] = s2 + t2 - raw[11 * ld + i];
 }
 
+// Non-finite test on the exponent bits (integer pipe; FP64 compares issue on
+// the FP64 pipe, 1/64 of the FP32 rate on GB300).
+__device__ inline bool finite_bits(double x) {
+  return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000;
+}
+
 // Pseudo-three-level dynamic coefficient (once per step, first RK stage):
 //   nume = (3α-2) Γ·[S(J(ασ)) - S(J(σ))],  deno = σ³/ζ(0) Γ·[E(ασ) - E(σ)],
 //   Lagrangian average with rlxf, C_d = nume/deno, |C_d| forced/limited.
-__global__ void sfs_dynamic_kernel(int64_t nf, int64_t ld, const double* __restrict__ G,
-                                   const double* __restrict__ S, const double* __restrict__ J,
-                                   const double* __restrict__ Jt, const double* __restrict__ E,
-                                   const double* __restrict__ Et, double* C, SfsParams p) {
+// Particles [0, nv); those with a nonzero static flag (stat may be null) are skipped.
+__global__ void __launch_bounds__(256) sfs_dynamic_kernel(
+    int64_t nv, const uint8_t* __restrict__ stat, int64_t ld, const double* __restrict__ G,
+    const double* __restrict__ S, const double* __restrict__ J, const double* __restrict__ Jt,
+    const double* __restrict__ E, const double* __restrict__ Et, double* __restrict__ C,
+    SfsParams p) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= nf) return;
+  if (i >= nv || (stat && stat[i])) return;
   const double g0 = G[i], g1 = G[ld + i], g2 = G[2 * ld + i];
   double a0, a1, a2, b0, b1, b2;
   double nume, deno;
@@ -130,20 +138,25 @@ __global__ void sfs_dynamic_kernel(int64_t nf, int64_t ld, const double* __restr
   C[2 * ld + i] = deno;
 }
 
-__global__ void sfs_constant_kernel(int64_t nf, double cd, double* C) {
+__global__ void sfs_constant_kernel(int64_t nv, const uint8_t* __restrict__ stat, double cd,
+                                    double* C) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < nf) C[i] = cd;
+  if (i < nv && !(stat && stat[i])) C[i] = cd;
 }
 
 // One RK stage (or an Euler step: a = 0, b = 1) of the free particles, fused:
 // backscatter clipping, rVPM right-hand side, low-storage register update,
-// state update, core spreading, non-finite detection.
-__global__ void rk_update_kernel(int64_t nf, int64_t ld, double* X, double* G, double* S,
-                                 const double* __restrict__ U, const double* __restrict__ J,
-                                 const double* __restrict__ E, double* C, double* Q,
-                                 UpdateParams p, int* status) {
+// state update, core spreading, non-finite detection.  FP64 throughout; the
+// FP64 pipe (not HBM) bounds it, so each particle forms the right-hand side
+// once, one reciprocal of |Γ|² and (with core spreading) one square root.
+// Particles [0, nv); those with a nonzero static flag (stat may be null) are skipped.
+__global__ void __launch_bounds__(256) rk_update_kernel(
+    int64_t nv, const uint8_t* __restrict__ stat, int64_t ld, double* __restrict__ X,
+    double* __restrict__ G, double* __restrict__ S, const double* __restrict__ U,
+    const double* __restrict__ J, const double* __restrict__ E, double* __restrict__ C,
+    double* __restrict__ Q, UpdateParams p, int* status) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= nf) return;
+  if (i >= nv || (stat && stat[i])) return;
   const double g0 = G[i], g1 = G[ld + i], g2 = G[2 * ld + i];
   const double sg = S[i];
   double s0, s1, s2;
@@ -159,44 +172,46 @@ __global__ void rk_update_kernel(int64_t nf, int64_t ld, double* X, double* G, d
       cd = 0.0;
       C[i] = 0.0;
     }
-    cz = cd * sg * sg * sg * p.inv_zeta0;   // C_d/ζ_σ(0)
+    cz = cd * (sg * sg) * (sg * p.inv_zeta0);   // C_d/ζ_σ(0)
     Z -= p.ze * cz * ge;
   }
-  Z = gg > 0.0 ? Z / gg : 0.0;
+  Z = gg > 0.0 ? Z * (1.0 / gg) : 0.0;
   const double a = p.a, b = p.b, dt = p.dt;
-  double q;
   // position
-  q = a * Q[0 * ld + i] + dt * (U[i] + p.uinf0);           Q[0 * ld + i] = q; X[i] += b * q;
-  q = a * Q[1 * ld + i] + dt * (U[ld + i] + p.uinf1);      Q[1 * ld + i] = q; X[ld + i] += b * q;
-  q = a * Q[2 * ld + i] + dt * (U[2 * ld + i] + p.uinf2);  Q[2 * ld + i] = q; X[2 * ld + i] += b * q;
+  const double q0 = a * Q[0 * ld + i] + dt * (U[i] + p.uinf0);
+  const double q1 = a * Q[1 * ld + i] + dt * (U[ld + i] + p.uinf1);
+  const double q2 = a * Q[2 * ld + i] + dt * (U[2 * ld + i] + p.uinf2);
+  Q[0 * ld + i] = q0; Q[1 * ld + i] = q1; Q[2 * ld + i] = q2;
+  const double x0 = X[i] + b * q0, x1 = X[ld + i] + b * q1, x2 = X[2 * ld + i] + b * q2;
+  X[i] = x0; X[ld + i] = x1; X[2 * ld + i] = x2;
   // strength
-  const double n0 = g0 + b * (a * Q[3 * ld + i] + dt * (s0 - 3.0 * Z * g0 - cz * e0));
-  const double n1 = g1 + b * (a * Q[4 * ld + i] + dt * (s1 - 3.0 * Z * g1 - cz * e1));
-  const double n2 = g2 + b * (a * Q[5 * ld + i] + dt * (s2 - 3.0 * Z * g2 - cz * e2));
-  Q[3 * ld + i] = a * Q[3 * ld + i] + dt * (s0 - 3.0 * Z * g0 - cz * e0);
-  Q[4 * ld + i] = a * Q[4 * ld + i] + dt * (s1 - 3.0 * Z * g1 - cz * e1);
-  Q[5 * ld + i] = a * Q[5 * ld + i] + dt * (s2 - 3.0 * Z * g2 - cz * e2);
+  const double z3 = 3.0 * Z;
+  const double r0 = a * Q[3 * ld + i] + dt * (s0 - z3 * g0 - cz * e0);
+  const double r1 = a * Q[4 * ld + i] + dt * (s1 - z3 * g1 - cz * e1);
+  const double r2 = a * Q[5 * ld + i] + dt * (s2 - z3 * g2 - cz * e2);
+  Q[3 * ld + i] = r0; Q[4 * ld + i] = r1; Q[5 * ld + i] = r2;
+  const double n0 = g0 + b * r0, n1 = g1 + b * r1, n2 = g2 + b * r2;
   G[i] = n0; G[ld + i] = n1; G[2 * ld + i] = n2;
   // core size: stretching, then core spreading
-  q = a * Q[6 * ld + i] - dt * sg * Z;
-  Q[6 * ld + i] = q;
-  double ns = sg + b * q;
+  const double qs = a * Q[6 * ld + i] - dt * sg * Z;
+  Q[6 * ld + i] = qs;
+  double ns = sg + b * qs;
   if (p.nu > 0.0) {
-    const double q2 = a * Q[7 * ld + i] + dt * 2.0 * p.nu;
-    Q[7 * ld + i] = q2;
-    ns = sqrt(ns * ns + b * q2);
+    const double qn = a * Q[7 * ld + i] + dt * 2.0 * p.nu;
+    Q[7 * ld + i] = qn;
+    ns = sqrt(ns * ns + b * qn);
   }
   S[i] = ns;
-  if (!(isfinite(n0) && isfinite(n1) && isfinite(n2) && isfinite(ns) && isfinite(X[i]) &&
-        isfinite(X[ld + i]) && isfinite(X[2 * ld + i])))
+  if (!(finite_bits(n0) && finite_bits(n1) && finite_bits(n2) && finite_bits(ns) &&
+        finite_bits(x0) && finite_bits(x1) && finite_bits(x2)))
     atomicOr(status, STATUS_NONFINITE);
 }
 
 // Pedrizzetti relaxation: Γ <- (1-r)Γ + r|Γ| ω/|ω|, ω = ∇×u from J.
-__global__ void relax_kernel(int64_t nf, int64_t ld, const double* __restrict__ J, double* G,
-                             double r) {
+__global__ void relax_kernel(int64_t nv, const uint8_t* __restrict__ stat, int64_t ld,
+                             const double* __restrict__ J, double* G, double r) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= nf) return;
+  if (i >= nv || (stat && stat[i])) return;
   const double w0 = J[7 * ld + i] - J[5 * ld + i];
   const double w1 = J[2 * ld + i] - J[6 * ld + i];
   const double w2 = J[3 * ld + i] - J[1 * ld + i];
@@ -255,10 +270,13 @@ __device__ inline void block_reduce(DiagAcc& acc, DiagAcc* sh) {
 }
 
 // raw: ζ sums (rows 0..2 Ω without self) or null (no enstrophy).
+// C_d statistics cover the free particles: [0, nf) without flags, or every
+// particle whose static flag is zero (stat non-null).
 __global__ void __launch_bounds__(kRedThreads) diag_partial_kernel(
-    int64_t n, int64_t nf, int64_t ld, const double* __restrict__ X, const double* __restrict__ G,
-    const double* __restrict__ S, const double* __restrict__ C, const double* __restrict__ raw,
-    double zeta0, double* partial) {
+    int64_t n, int64_t nf, const uint8_t* __restrict__ stat, int64_t ld,
+    const double* __restrict__ X, const double* __restrict__ G, const double* __restrict__ S,
+    const double* __restrict__ C, const double* __restrict__ raw, double zeta0,
+    double* partial) {
   __shared__ DiagAcc sh[kRedThreads];
   DiagAcc acc;
   diag_identity(acc);
@@ -282,14 +300,17 @@ __global__ void __launch_bounds__(kRedThreads) diag_partial_kernel(
     const bool fin = isfinite(x0) && isfinite(x1) && isfinite(x2) && isfinite(g0) &&
                      isfinite(g1) && isfinite(g2) && isfinite(sg);
     acc.v[DS_NONFIN] += fin ? 0.0 : 1.0;
-    if (C && i < nf) {
+    if (C && (stat ? !stat[i] : i < nf)) {
       const double c = C[i];
       if (c == 0.0) {
         acc.v[DS_CZERO] += 1.0;
       } else {
+        const double c2 = c * c;
         acc.v[DS_CCNT] += 1.0;
         acc.v[DS_CSUM] += c;
-        acc.v[DS_CSUM2] += c * c;
+        acc.v[DS_CSUM2] += c2;
+        acc.v[DS_CSUM3] += c2 * c;
+        acc.v[DS_CSUM4] += c2 * c2;
         acc.v[DS_CMIN] = fmin(acc.v[DS_CMIN], c);
         acc.v[DS_CMAX] = fmax(acc.v[DS_CMAX], c);
       }
@@ -372,32 +393,36 @@ cudaError_t launch_estr_finish_d(int64_t n, int64_t ld, const double* raw, const
   return cudaGetLastError();
 }
 
-cudaError_t launch_sfs_dynamic(int64_t nf, int64_t ld, const double* G, const double* S,
-                               const double* J, const double* Jt, const double* E,
-                               const double* Et, double* C, const SfsParams& p, cudaStream_t st) {
-  if (nf <= 0) return cudaSuccess;
-  sfs_dynamic_kernel<<<grid_for(nf, 256), 256, 0, st>>>(nf, ld, G, S, J, Jt, E, Et, C, p);
+cudaError_t launch_sfs_dynamic(int64_t nv, const uint8_t* stat, int64_t ld, const double* G,
+                               const double* S, const double* J, const double* Jt,
+                               const double* E, const double* Et, double* C, const SfsParams& p,
+                               cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  sfs_dynamic_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, stat, ld, G, S, J, Jt, E, Et, C, p);
   return cudaGetLastError();
 }
 
-cudaError_t launch_sfs_constant(int64_t nf, double cd, double* C, cudaStream_t st) {
-  if (nf <= 0) return cudaSuccess;
-  sfs_constant_kernel<<<grid_for(nf, 256), 256, 0, st>>>(nf, cd, C);
+cudaError_t launch_sfs_constant(int64_t nv, const uint8_t* stat, double cd, double* C,
+                                cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  sfs_constant_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, stat, cd, C);
   return cudaGetLastError();
 }
 
-cudaError_t launch_rk_update(int64_t nf, int64_t ld, double* X, double* G, double* S,
-                             const double* U, const double* J, const double* E, double* C,
-                             double* Q, const UpdateParams& p, int* status, cudaStream_t st) {
-  if (nf <= 0) return cudaSuccess;
-  rk_update_kernel<<<grid_for(nf, 256), 256, 0, st>>>(nf, ld, X, G, S, U, J, E, C, Q, p, status);
+cudaError_t launch_rk_update(int64_t nv, const uint8_t* stat, int64_t ld, double* X, double* G,
+                             double* S, const double* U, const double* J, const double* E,
+                             double* C, double* Q, const UpdateParams& p, int* status,
+                             cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  rk_update_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, stat, ld, X, G, S, U, J, E, C, Q, p,
+                                                      status);
   return cudaGetLastError();
 }
 
-cudaError_t launch_relax(int64_t nf, int64_t ld, const double* J, double* G, double r,
-                         cudaStream_t st) {
-  if (nf <= 0) return cudaSuccess;
-  relax_kernel<<<grid_for(nf, 256), 256, 0, st>>>(nf, ld, J, G, r);
+cudaError_t launch_relax(int64_t nv, const uint8_t* stat, int64_t ld, const double* J, double* G,
+                         double r, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  relax_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, stat, ld, J, G, r);
   return cudaGetLastError();
 }
 
@@ -407,11 +432,11 @@ cudaError_t launch_zero(double* p, int64_t n, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_diagnostics(int64_t n, int64_t nf, int64_t ld, const double* X,
-                               const double* G, const double* S, const double* C,
+cudaError_t launch_diagnostics(int64_t n, int64_t nf, const uint8_t* stat, int64_t ld,
+                               const double* X, const double* G, const double* S, const double* C,
                                const double* raw, double zeta0, double* partial, double* out,
                                cudaStream_t st) {
-  diag_partial_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(n, nf, ld, X, G, S, C, raw, zeta0,
+  diag_partial_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(n, nf, stat, ld, X, G, S, C, raw, zeta0,
                                                           partial);
   diag_final_kernel<<<1, kRedThreads, 0, st>>>(kRedBlocks, partial, out);
   return cudaGetLastError();

@@ -33,7 +33,7 @@ struct UpdateParams {
 // Diagnostic reduction slots.
 enum {
   DS_ENS = 0, DS_IX, DS_IY, DS_IZ, DS_GX, DS_GY, DS_GZ, DS_SIG, DS_NONFIN,
-  DS_CCNT, DS_CSUM, DS_CSUM2, DS_CZERO, DS_CMIN, DS_CMAX, kDiagSlots
+  DS_CCNT, DS_CSUM, DS_CSUM2, DS_CZERO, DS_CMIN, DS_CMAX, DS_CSUM3, DS_CSUM4, kDiagSlots
 };
 constexpr int kRedBlocks = 304;   // 2 x 152 SMs
 
@@ -47,19 +47,24 @@ cudaError_t launch_stretch_vw(int64_t n, int64_t ld, const double* J, const doub
 cudaError_t launch_estr_finish_d(int64_t n, int64_t ld, const double* raw, const double* J,
                                  const double* DJ, int transposed, double* E, double* DE,
                                  cudaStream_t st);
-cudaError_t launch_sfs_dynamic(int64_t nf, int64_t ld, const double* G, const double* S,
-                               const double* J, const double* Jt, const double* E,
-                               const double* Et, double* C, const SfsParams& p, cudaStream_t st);
-cudaError_t launch_sfs_constant(int64_t nf, double cd, double* C, cudaStream_t st);
-cudaError_t launch_rk_update(int64_t nf, int64_t ld, double* X, double* G, double* S,
-                             const double* U, const double* J, const double* E, double* C,
-                             double* Q, const UpdateParams& p, int* status, cudaStream_t st);
-cudaError_t launch_relax(int64_t nf, int64_t ld, const double* J, double* G, double r,
-                         cudaStream_t st);
+// The per-particle kernels below visit particles [0, nv) and skip those whose
+// static flag stat[i] is nonzero (stat may be null: no static particles in range).
+cudaError_t launch_sfs_dynamic(int64_t nv, const uint8_t* stat, int64_t ld, const double* G,
+                               const double* S, const double* J, const double* Jt,
+                               const double* E, const double* Et, double* C, const SfsParams& p,
+                               cudaStream_t st);
+cudaError_t launch_sfs_constant(int64_t nv, const uint8_t* stat, double cd, double* C,
+                                cudaStream_t st);
+cudaError_t launch_rk_update(int64_t nv, const uint8_t* stat, int64_t ld, double* X, double* G,
+                             double* S, const double* U, const double* J, const double* E,
+                             double* C, double* Q, const UpdateParams& p, int* status,
+                             cudaStream_t st);
+cudaError_t launch_relax(int64_t nv, const uint8_t* stat, int64_t ld, const double* J, double* G,
+                         double r, cudaStream_t st);
 cudaError_t launch_zero(double* p, int64_t n, cudaStream_t st);
 // partial: kRedBlocks*kDiagSlots doubles; out: kDiagSlots doubles (device).
-cudaError_t launch_diagnostics(int64_t n, int64_t nf, int64_t ld, const double* X,
-                               const double* G, const double* S, const double* C,
+cudaError_t launch_diagnostics(int64_t n, int64_t nf, const uint8_t* stat, int64_t ld,
+                               const double* X, const double* G, const double* S, const double* C,
                                const double* raw, double zeta0, double* partial, double* out,
                                cudaStream_t st);
 cudaError_t launch_centroid(int64_t i0, int64_t i1, int64_t ld, const double* X, const double* G,

@@ -1180,9 +1180,9 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 
 // Wait for the phase of the given parity to complete, giving up after a bounded
 // number of polls (returns false then).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int polls = 1 << 22) {
   const uint32_t addr = smem_u32(bar);
-  for (int it = 0; it < (1 << 22); ++it) {
+  for (int it = 0; it < polls; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"

@@ -7,7 +7,10 @@ The names follow the FLOWVPM symbols that FLOWUnsteady passes around
                            kernel=gaussianerf, UJ=UJ_gpu, SFS=noSFS,
                            integration=rungekutta3, transposed=True,
                            relaxation=norelaxation, Uinf=...)
-    add_particle(pfield, X, Gamma, sigma; static=False)     (:455-489, :572)
+    add_particle(pfield, X, Gamma, sigma; vol=0, circulation=1, C=None, static=False)
+    add_probe(pfield, X)                  (Γ = 0, σ = 1e-6, vol = 0; :572)
+    add_shed_particles(pfield, X, gamma, dt, V, infD, sigma, vol, l, p_per_step)
+                                          (FLOWUnsteady's shedding add_particle, :455-489)
     remove_particle(pfield, i)            (tail removal,     :360-365, :550-552)
     get_np(pfield)
     pfield.UJ(pfield)                     (probe / force evaluation, :544)
@@ -228,20 +231,39 @@ class ParticleField:
     def _flush(self):
         if not self._pend:
             return
+        # Consecutive appends with the same static flag go up in one call.
         groups = []
-        for X, G, S, static in self._pend:
+        for X, G, S, static, attrs in self._pend:
             if groups and groups[-1][3] == static:
-                groups[-1][0].append(X); groups[-1][1].append(G); groups[-1][2].append(S)
+                g = groups[-1]
+                g[0].append(X); g[1].append(G); g[2].append(S); g[4].append(attrs)
             else:
-                groups.append(([X], [G], [S], static))
+                groups.append(([X], [G], [S], static, [attrs]))
         self._pend = []
-        for Xs, Gs, Ss, static in groups:
+        for Xs, Gs, Ss, static, attrs in groups:
             X = np.ascontiguousarray(np.concatenate(Xs), dtype=np.float64)
             G = np.ascontiguousarray(np.concatenate(Gs), dtype=np.float64)
             S = np.ascontiguousarray(np.concatenate(Ss), dtype=np.float64)
+            n0 = self._np_device()
             L.check(L.lib().vpm_append(self._ctx, X.shape[0], L.dptr(X), 3, L.dptr(G), 3,
                                        L.dptr(S), 1, 1 if static else 0), self._ctx)
+            # vol / circulation / C other than the defaults (0, 1, 0).
+            if any(a is not None for a in attrs):
+                vol = np.concatenate([a[0] if a else np.zeros(x.shape[0])
+                                      for a, x in zip(attrs, Xs)])
+                circ = np.concatenate([a[1] if a else np.ones(x.shape[0])
+                                       for a, x in zip(attrs, Xs)])
+                C = np.concatenate([a[2] if a else np.zeros((x.shape[0], 3))
+                                    for a, x in zip(attrs, Xs)])
+                vol, circ, C = (np.ascontiguousarray(v, dtype=np.float64) for v in (vol, circ, C))
+                L.check(L.lib().vpm_set_attributes(self._ctx, n0, X.shape[0], L.dptr(vol), 1,
+                                                   L.dptr(circ), 1, L.dptr(C), 3), self._ctx)
         self._uj_valid = False
+
+    def _np_device(self) -> int:
+        n = ctypes.c_int64()
+        L.check(L.lib().vpm_get_np(self._ctx, ctypes.byref(n), None), self._ctx)
+        return int(n.value)
 
     def set_particles(self, X, Gamma, sigma):
         self._pend = []
@@ -296,6 +318,24 @@ class ParticleField:
 
     def get_J(self):
         return self.get_UJ()[1]
+
+    def attributes(self):
+        """(vol, circulation, static) of every particle as host arrays."""
+        n = self.get_np()
+        vol, circ = np.empty(n), np.empty(n)
+        st = (ctypes.c_int32 * max(n, 1))()
+        L.check(L.lib().vpm_get_attributes(self._ctx, 0, n, L.dptr(vol), 1, L.dptr(circ), 1, st),
+                self._ctx)
+        return vol, circ, np.array(st[:n], dtype=bool)
+
+    def get_vol(self):
+        return self.attributes()[0]
+
+    def get_circulation(self):
+        return self.attributes()[1]
+
+    def get_static(self):
+        return self.attributes()[2]
 
     def get_C(self):
         n = self.get_np()
@@ -385,18 +425,50 @@ def read(pfield: ParticleField, file: str, *, load_time: bool = False):
     pfield._uj_valid = False
 
 
-def add_particle(pfield: ParticleField, X, Gamma, sigma, *, static: bool = False):
-    """Append one particle or an (n,3)/(n,3)/(n,) batch (vpm.add_particle)."""
+def add_particle(pfield: ParticleField, X, Gamma, sigma, *, vol=0.0, circulation=1.0, C=None,
+                 static: bool = False):
+    """Append one particle or an (n,3)/(n,3)/(n,) batch (vpm.add_particle with
+    its vol, circulation, C and static keywords)."""
     X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    n = X.shape[0]
     G = np.asarray(Gamma, dtype=np.float64).reshape(-1, 3)
-    S = np.broadcast_to(np.asarray(sigma, dtype=np.float64).reshape(-1), (X.shape[0],))
-    pfield._pend.append((X, G, np.array(S), bool(static)))
+    S = np.broadcast_to(np.asarray(sigma, dtype=np.float64).reshape(-1), (n,))
+    vol = np.broadcast_to(np.asarray(vol, dtype=np.float64).reshape(-1), (n,))
+    circ = np.broadcast_to(np.asarray(circulation, dtype=np.float64).reshape(-1), (n,))
+    Cm = (np.zeros((n, 3)) if C is None
+          else np.broadcast_to(np.asarray(C, dtype=np.float64).reshape(-1, 3), (n, 3)))
+    default = C is None and not np.any(vol != 0.0) and not np.any(circ != 1.0)
+    attrs = None if default else (np.array(vol), np.array(circ), np.array(Cm))
+    pfield._pend.append((X, G, np.array(S), bool(static), attrs))
 
 
 def add_probe(pfield: ParticleField, X):
-    """Probe particle: Γ = 0, σ = 1e-6, static (add_probe, src/FLOWUnsteady_simulation.jl:572)."""
+    """Probe particle: a plain particle with Γ = 0, σ = 1e-6 and vol = 0
+    (add_probe, src/FLOWUnsteady_simulation.jl:572)."""
     X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
-    add_particle(pfield, X, np.zeros_like(X), 1e-6, static=True)
+    add_particle(pfield, X, np.zeros_like(X), 1e-6, vol=0.0)
+
+
+def add_shed_particles(pfield: ParticleField, X, gamma, dt, V, infD, sigma, vol, l,
+                       p_per_step: int, *, overwrite_sigma=None, eps: float = 2.0**-52):
+    """Shed p_per_step particles along the segment l from X, as FLOWUnsteady's
+    add_particle does (src/FLOWUnsteady_simulation.jl:455-489): Γ = γ·(V·dt)·infD,
+    raised to 5·eps per component when |Γ| <= 5·eps; circulation max(|γ|, 5·eps);
+    each particle carries Γ/p, σ/p (or overwrite_sigma) and vol/p, at
+    X + (i - 1/2)·l/p."""
+    X = np.asarray(X, dtype=np.float64).reshape(3)
+    infD = np.asarray(infD, dtype=np.float64).reshape(3)
+    l = np.asarray(l, dtype=np.float64).reshape(3)
+    Gamma = gamma * (V * dt) * infD
+    if np.sqrt(Gamma @ Gamma) <= 5 * eps:
+        Gamma = 5 * eps * np.ones(3)
+    circulation = max(abs(gamma), 5 * eps)
+    pps = int(p_per_step)
+    sigmap = sigma / pps if overwrite_sigma is None else overwrite_sigma
+    dX = l / pps
+    i = np.arange(1, pps + 1, dtype=np.float64)[:, None]
+    add_particle(pfield, X + i * dX - dX / 2, np.tile(Gamma / pps, (pps, 1)), sigmap,
+                 vol=vol / pps, circulation=circulation)
 
 
 def remove_particle(pfield: ParticleField, i: int):
@@ -442,8 +514,14 @@ def monitor_enstrophy(pfield: ParticleField) -> float:
 
 
 def monitor_Cd(pfield: ParticleField) -> dict:
+    """Statistics of the SFS coefficient over the free particles, in the order of
+    vpm.monitor_Cd's record (src/FLOWUnsteady_monitors.jl:697-703): t, ratio of
+    zeros, then mean, standard deviation, skewness, excess kurtosis, minimum and
+    maximum of the nonzero C_d."""
     d = pfield.diagnostics()
-    return {k: d[k] for k in ("cd_mean", "cd_std", "cd_zero_ratio", "cd_min", "cd_max")}
+    return {"t": pfield.t, "cd_zero_ratio": d["cd_zero_ratio"], "cd_mean": d["cd_mean"],
+            "cd_std": d["cd_std"], "cd_skew": d["cd_skew"], "cd_kurt": d["cd_kurt"],
+            "cd_min": d["cd_min"], "cd_max": d["cd_max"]}
 
 
 def measure_fma_peaks(device: int = 0):

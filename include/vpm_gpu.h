@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define VPM_ABI_VERSION 1
+#define VPM_ABI_VERSION 2
 
 /* ---------------------------------------------------------------- status -- */
 enum {
@@ -157,14 +157,16 @@ enum {
   VPM_DIAG_GAMMA_X = 4,     /* Σ_p Γ_p                                                       */
   VPM_DIAG_GAMMA_Y = 5,
   VPM_DIAG_GAMMA_Z = 6,
-  VPM_DIAG_CD_MEAN = 7,     /* C_d statistics over particles with C_d != 0 (vpm.monitor_Cd) */
-  VPM_DIAG_CD_STD = 8,
-  VPM_DIAG_CD_ZERO_RATIO = 9,
-  VPM_DIAG_CD_MIN = 10,
+  VPM_DIAG_CD_MEAN = 7,     /* C_d statistics over the free particles with C_d != 0        */
+  VPM_DIAG_CD_STD = 8,      /* (vpm.monitor_Cd's t, rationzero, mean, stddev, skew, kurt,   */
+  VPM_DIAG_CD_ZERO_RATIO = 9, /* minC, maxC; src/FLOWUnsteady_monitors.jl:697-703):         */
+  VPM_DIAG_CD_MIN = 10,     /* population moments; the zero ratio is over all free ones    */
   VPM_DIAG_CD_MAX = 11,
   VPM_DIAG_SIGMA_MEAN = 12,
   VPM_DIAG_NONFINITE = 13,  /* number of particles whose state holds a NaN/Inf            */
-  VPM_DIAG_COUNT = 14
+  VPM_DIAG_CD_SKEW = 14,    /* m3/m2^(3/2) of the nonzero C_d                              */
+  VPM_DIAG_CD_KURT = 15,    /* excess kurtosis m4/m2² - 3 of the nonzero C_d               */
+  VPM_DIAG_COUNT = 16
 };
 
 /* --------------------------------------------------------------- context -- */
@@ -201,17 +203,32 @@ int vpm_set_particles(vpm_ctx* ctx, int64_t n, const double* X, int64_t stride_x
                       int64_t stride_s);
 
 /* Append n particles at the tail (vpm.add_particle, src/FLOWUnsteady_simulation.jl:455-489,
- * and add_probe, :572).  The appended particles are counted as static (sources
- * only, not advanced by vpm_step) when is_static != 0.  Static particles must
- * stay at the tail: appending a free particle after a static one is VPM_ERR_STATE. */
+ * and add_probe, :572).  The appended particles are static (sources only, not
+ * advanced by vpm_step) when is_static != 0.  Free and static particles may
+ * be appended in any order, as FLOWUnsteady appends probes (plain particles,
+ * Γ = 0) after the static ones (:516-541).  New particles start with vol 0,
+ * circulation 1 and empty SFS memory (see vpm_set_attributes). */
 int vpm_append(vpm_ctx* ctx, int64_t n, const double* X, int64_t stride_x, const double* Gamma,
                int64_t stride_g, const double* sigma, int64_t stride_s, int is_static);
+
+/* Per-particle values FLOWVPM carries beside X, Γ, σ (vpm.add_particle's vol,
+ * circulation and C keywords; get_vol, get_circulation, get_C), for particles
+ * [i0, i0+n): the volume, the circulation magnitude, and the SFS memory C
+ * (C_d, ⟨Γ·L⟩, ⟨Γ·m⟩) with stride sc >= 3.  A NULL pointer leaves that value.
+ * vol and circulation are carried (saved, restored, read back) but do not
+ * enter the method.  FLOWUnsteady's mirror images copy C this way (:527-532). */
+int vpm_set_attributes(vpm_ctx* ctx, int64_t i0, int64_t n, const double* vol, int64_t stride_vol,
+                       const double* circulation, int64_t stride_circ, const double* C,
+                       int64_t stride_c);
+/* Read them back, and the static flag (1 or 0) of each particle; any pointer may be NULL. */
+int vpm_get_attributes(vpm_ctx* ctx, int64_t i0, int64_t n, double* vol, int64_t stride_vol,
+                       double* circulation, int64_t stride_circ, int32_t* is_static);
 
 /* Keep the first n particles (vpm.remove_particle from the tail,
  * src/FLOWUnsteady_simulation.jl:360-365, :550-552). */
 int vpm_truncate(vpm_ctx* ctx, int64_t n);
 
-/* Number of particles (vpm.get_np) and of static particles at the tail. */
+/* Number of particles (vpm.get_np) and of static particles among them. */
 int vpm_get_np(const vpm_ctx* ctx, int64_t* n, int64_t* n_static);
 
 /* Download the state of the first n particles (any pointer may be NULL). */
@@ -288,15 +305,18 @@ int vpm_fmm_stats(const vpm_ctx* ctx, int64_t* out);
 /* Write the particle field (the role of vpm.save, src/FLOWUnsteady_simulation.jl:436-440)
  * to <path>.pfield.<num>.bin and <path>.pfield.<num>.xmf (".<num>" left out
  * when num < 0).  The .bin file is a 64-byte header (magic "VPMFIELD", version
- * 1, n, n_static, t, nt) followed by X (n×3), Gamma (n×3), sigma (n), the SFS
- * memory C (n×3) and a static flag (n), all little-endian FP64, particle-major;
- * the .xmf file describes it for ParaView (XDMF 3, binary data items). */
+ * 2, n, n_static, t, nt) followed by X (n×3), Gamma (n×3), sigma (n), the SFS
+ * memory C (n×3), a static flag (n), vol (n) and circulation (n), all
+ * little-endian FP64, particle-major (version 1 files end after the static
+ * flag); the .xmf file describes it for ParaView (XDMF 3, binary data items). */
 int vpm_save(vpm_ctx* ctx, const char* path, int64_t num);
 
 /* Restore a field written by vpm_save (the role of
  * vpm.read!(pfield, file; overwrite=true, load_time), :264): replaces the
- * particles (free, then static), their SFS memory and, when load_time != 0,
- * the time and step counter. */
+ * particles with their static flags, SFS memory, vol and circulation (1 and 0
+ * for version 1 files) and, when load_time != 0, the time and step counter.
+ * A file whose static flags are not 0/1 or disagree with its static count is
+ * VPM_ERR_INVALID. */
 int vpm_load(vpm_ctx* ctx, const char* bin_file, int load_time);
 
 /* Σ|Γ|-weighted centroids of index ranges: for r in [0, nranges) particles
@@ -317,21 +337,26 @@ int vpm_uj_device_async(int kernel, int precision, int64_t ns, const double* Xs,
                         void* cuda_stream);
 
 /* The same evaluation as vpm_uj_device_async, for callers that cannot let the
- * library allocate device memory: a loop that must not allocate once it runs,
- * a host whose device memory is entirely held by its own pool allocator, or
- * work being captured into a CUDA graph.  It has no counterpart in the
- * reference.  It calls no cudaMalloc, cudaFree or other allocating routine:
- * the scratch for split source ranges is a fixed 4 MiB array that every GPU
- * loading the library holds until the process exits.
+ * library allocate device memory: a loop that must not allocate once it runs
+ * (fixed-memory or real-time co-simulation), or a host whose device memory is
+ * entirely held by its own pool allocator (a Julia or Python caching
+ * allocator).  It has no counterpart in the reference.  It calls no
+ * cudaMalloc, cudaFree or other allocating routine: the scratch for split
+ * source ranges is a fixed 4 MiB array that every GPU loading the library
+ * holds until the process exits.
  *   - nt may be at most 16384 targets; larger calls return VPM_ERR_CAPACITY
  *     without launching (use vpm_uj_device_async for them).
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     outside any stream capture.
+ *   - The first call on a device (and the first after the device's context
+ *     was replaced, e.g. by cudaDeviceReset) looks up the array's device
+ *     address (cudaGetSymbolAddress) with that device current; make that
+ *     first call before any stream capture.
  *   - All calls share the one array and leave their partial sums in it; every
  *     slot a call uses is written before it is read.  Calls whose work
  *     overlaps on the GPU (different streams, or host threads) race on the
- *     array: serialise them. */
+ *     array: serialise them.
+ *   - The FP32/FP32C passes convert the FP64 sources in the kernel instead of
+ *     reading packed source records (which would need scratch per source), so
+ *     they run a few percent slower than through vpm_uj_device_async. */
 int vpm_uj_device_noalloc(int kernel, int precision, int64_t ns, const double* Xs,
                           const double* Gs, const double* Ss, int64_t ld_s, int64_t nt,
                           const double* Xt, int64_t ld_t, double* U, double* J, int64_t ld_o,
@@ -393,6 +418,12 @@ int vpm_measure_fma_peaks(int device, double* fp32_tflops, double* fp64_tflops, 
 /* Host fault-injection hook for tests: the next k-th launch-issuing call on the
  * context fails with VPM_ERR_INJECTED before it launches anything (0 disables). */
 int vpm_debug_fail_after(vpm_ctx* ctx, int64_t k);
+
+/* Work plan of the last successful vpm_uj_device_async / vpm_uj_device_noalloc
+ * call on this host thread: tile shape (threads per CTA, targets per thread)
+ * and the number of source chunks (> 1: partial sums went through scratch).
+ * Zeros before the first call.  Any pointer may be NULL. */
+int vpm_debug_last_plan(int32_t* block, int32_t* tpt, int32_t* n_chunk);
 
 /* Number of kernels the context has enqueued since creation (pair passes,
  * reductions and updates; a graph replay counts its kernels). */

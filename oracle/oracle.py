@@ -24,6 +24,8 @@ _lib = None
 
 WINCKELMANS = 0
 GAUSSIANERF = 1
+# Length of the diagnostics vector (the VPM_DIAG_* layout of include/vpm_gpu.h).
+DIAG_COUNT = 16
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _i64 = ctypes.c_int64
@@ -124,6 +126,25 @@ def estr_direct(kernel, X, G, S, J, transposed=True, sigma_scale=1.0, nthreads=0
     return (E if J is not None else None), om
 
 
+def estr_at(kernel, X, G, S, J, idx, transposed=True, sigma_scale=1.0, nthreads=0):
+    """E_str (m,3) at the particles `idx` of the field (X, G, S), from J (n,3,3)
+    at every particle (the targets' J is J[idx]); ζ uses the source core σ·scale."""
+    X, G, S = _c(X, (3,)), _c(G, (3,)), _c(S, ())
+    J = _c(J, (3, 3))
+    idx = np.asarray(idx, dtype=np.int64)
+    Xt = np.ascontiguousarray(X[idx])
+    Jt = np.ascontiguousarray(J[idx])
+    E = np.empty((idx.size, 3))
+    lib().orc_estr_direct(kernel, sigma_scale, int(transposed), idx.size, _p(Xt), _p(Jt), None,
+                          X.shape[0], _p(X), _p(G), _p(S), _p(J), _p(E), None, nthreads)
+    return E
+
+
+def zeta0(kernel) -> float:
+    """ζ(0) of the kernel (the normalisation of the dynamic SFS denominator)."""
+    return float(kernel_eval(kernel, np.zeros(1))[2][0])
+
+
 def uj_dsigma(kernel, X, G, S, Xt=None, nthreads=0):
     """dJ/dα (nt,3,3) for core sizes ασ at α = 1."""
     X, G, S = _c(X, (3,)), _c(G, (3,)), _c(S, ())
@@ -179,7 +200,7 @@ def relax_pedrizzetti(G, J, rlx, nfree=None):
 def diagnostics(kernel, X, G, S, C=None, n_static=0, nthreads=0):
     X, G, S = _c(X, (3,)), _c(G, (3,)), _c(S, ())
     C = None if C is None else _c(C, (3,))
-    out = np.zeros(14)
+    out = np.zeros(DIAG_COUNT)
     lib().orc_diagnostics(kernel, X.shape[0], n_static, _p(X), _p(G), _p(S), _p(C), _p(out),
                           nthreads)
     return out

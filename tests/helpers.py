@@ -95,7 +95,7 @@ class Ctx:
 
 
 def scheme(kernel=1, prec=0, integration=1, transposed=1, sfs=0, nu=0.0, f=0.0, g=0.2,
-           flags=1, alpha=0.999, rlxf=1.0, minC=0.0, maxC=1.0, uinf=(0, 0, 0)):
+           flags=1, alpha=0.999, rlxf=1.0, minC=0.0, maxC=1.0, uinf=(0, 0, 0), Cd=0.0):
     s = L.Scheme()
     s.kernel, s.precision, s.integration, s.transposed = kernel, prec, integration, transposed
     s.f, s.g = f, g
@@ -104,6 +104,6 @@ def scheme(kernel=1, prec=0, integration=1, transposed=1, sfs=0, nu=0.0, f=0.0, 
     s.nu = nu
     s.sfs, s.sfs_flags = sfs, flags
     s.sfs_alpha, s.sfs_rlxf, s.sfs_minC, s.sfs_maxC = alpha, rlxf, minC, maxC
-    s.sfs_Cd = 0.0
+    s.sfs_Cd = Cd
     s.relaxation, s.relax_nsteps, s.relax_factor = 0, 1, 0.3
     return s

@@ -350,3 +350,33 @@ def test_morton_ordered_passes_match_original_order(oracle):
     idx = np.sort(np.random.default_rng(6).choice(n, 300, replace=False))
     U0, J0 = oracle.uj_direct(1, X, G, S, Xt=X[idx])
     assert rel_l2(srt["U"][idx], U0) <= 1e-5 and rel_l2(srt["J"][idx], J0) <= 1e-5
+
+
+def test_jacobian_row_order_is_dU_a_dx_b():
+    # The C ABI's J is row-major per particle: J[3a+b] = dU_a/dx_b.  Pin it
+    # through the ABI against central differences of U at zero-strength probes
+    # (probes carry Γ = 0, so they change nothing): the orientation that
+    # FLOWVPM's classic stretching S = J·Γ and its transposed form rely on.
+    X, G, S = uniform_box(600, seed_index=61)
+    S = S * 3.0
+    rng = np.random.default_rng(62)
+    pts = rng.uniform(-0.6, 0.6, (5, 3))
+    h = 1e-5
+    probes = [pts]
+    for b in range(3):
+        e = np.zeros(3)
+        e[b] = h
+        probes += [pts + e, pts - e]
+    P = np.vstack(probes)
+    m = P.shape[0]
+    with Ctx(600 + m) as c:
+        c.set(X, G, S)
+        c.append(P, np.zeros_like(P), np.full(m, 1e-6))
+        U, J = c.uj(L.KERNEL_GAUSSIANERF, L.PREC_FP64, 600, 600 + m)
+    Jc = J[:5]
+    fd = np.empty((5, 3, 3))
+    for b in range(3):
+        up, um = U[5 + 10 * b:10 + 10 * b], U[10 + 10 * b:15 + 10 * b]
+        fd[:, :, b] = (up - um) / (2 * h)       # column b: dU_a/dx_b for a = 0..2
+    assert rel_l2(Jc, fd) <= 1e-7
+    assert rel_l2(np.transpose(Jc, (0, 2, 1)), fd) > 1e-2

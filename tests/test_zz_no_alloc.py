@@ -1,8 +1,10 @@
 """vpm_uj_device_noalloc: the U/∇U evaluation for callers that cannot let the
-library allocate device memory (fixed-memory loops, hosts whose pool
-allocator owns the GPU's memory, work inside a graph capture).  It must give
-what vpm_uj_device_async gives on the same device arrays, on every call, with
-its scratch in a fixed array instead of an allocation.
+library allocate device memory (loops that must not allocate once running,
+hosts whose own pool allocator holds the GPU's memory).  On every call it
+must give what the CPU FP64 oracle gives (FP64 within 1e-12, FP32C within
+1e-5 relative L2) and what vpm_uj_device_async gives on the same device
+arrays, with its split-source scratch in a fixed array instead of an
+allocation.
 
 This file is named to run last: a failure here leaves every other test run."""
 import ctypes
@@ -28,7 +30,13 @@ def _call(fn, torch, kernel, prec, n, Xd, Gd, Sd, m, Xt):
             None if Xt is None else Xt.data_ptr(), m, U.data_ptr(), J.data_ptr(), m, st)
     assert rc == 0, L.last_error()
     torch.cuda.synchronize()
-    return U.cpu().numpy(), J.cpu().numpy()
+    return U.cpu().numpy().T, J.cpu().numpy().T.reshape(m, 3, 3)
+
+
+def _chunks():
+    n_chunk = ctypes.c_int32()
+    L.lib().vpm_debug_last_plan(None, None, ctypes.byref(n_chunk))
+    return n_chunk.value
 
 
 def _rel_l2(a, b):
@@ -40,20 +48,28 @@ def _rel_l2(a, b):
     (L.KERNEL_WINCKELMANS, L.PREC_FP32C, 1e-5),
     (L.KERNEL_GAUSSIANERF, L.PREC_FP32C, 1e-5),
 ])
-def test_noalloc_matches_allocating_entry_point(kernel, prec, tol):
+def test_noalloc_matches_oracle_and_allocating_entry_point(oracle, kernel, prec, tol):
     torch = pytest.importorskip("torch")
     lib = L.lib()
     n = 6000
     X, G, S = uniform_box(n, seed_index=90)
-    Xd, Gd, Sd = _dev(torch, X.T), _dev(torch, G.T), _dev(torch, S * 2.0)
+    S = S * 2.0
+    Xd, Gd, Sd = _dev(torch, X.T), _dev(torch, G.T), _dev(torch, S)
     # Targets: all particles (self pairs skipped) and a separate probe set.
     rng = np.random.default_rng(3)
-    Xp = _dev(torch, rng.uniform(-1, 1, (1000, 3)).T)
-    for m, Xt in ((n, None), (1000, Xp)):
-        U0, J0 = _call(lib.vpm_uj_device_async, torch, kernel, prec, n, Xd, Gd, Sd, m, Xt)
+    P = rng.uniform(-1, 1, (1000, 3))
+    Xp = _dev(torch, P.T)
+    split = []
+    for m, Xt, pts in ((n, None, X), (1000, Xp, P)):
+        U0, J0 = oracle.uj_direct(kernel, X, G, S, Xt=pts)
+        Ua, Ja = _call(lib.vpm_uj_device_async, torch, kernel, prec, n, Xd, Gd, Sd, m, Xt)
         for _ in range(2):   # two calls in a row share the static scratch
             U1, J1 = _call(lib.vpm_uj_device_noalloc, torch, kernel, prec, n, Xd, Gd, Sd, m, Xt)
+            split.append(_chunks())
             assert _rel_l2(U1, U0) <= tol and _rel_l2(J1, J0) <= tol
+            assert _rel_l2(U1, Ua) <= tol and _rel_l2(J1, Ja) <= tol
+    # The source range was split, so the partial sums went through the scratch.
+    assert max(split) > 1
 
 
 def test_noalloc_rejects_more_targets_than_its_scratch_holds():
