@@ -1153,6 +1153,15 @@ int vpm_eval_sfs(vpm_ctx* c, const vpm_scheme* s) {
   c->dry = false;
   if ((rc = ensure_part(c, c->part_need))) return rc;
   CTX_CK(c, enqueue_uj_sfs(c, s, 0));
+  if (s->sfs_flags & VPM_SFS_CLIP_BACKSCATTER) {
+    // A step applies the backscatter clipping inside its update kernel; here
+    // it is applied on its own, so C_d comes back as the SFS model leaves it.
+    int64_t nf = 0;
+    const uint8_t* stat = nullptr;
+    update_range(c, &nf, &stat);
+    CTX_CK(c, launch_sfs_clip(nf, stat, c->ld, c->G, c->E, c->C, c->st));
+    c->launches += 1;
+  }
   CTX_CK(c, cudaStreamSynchronize(c->st));
   c->uj_lo = 0;
   c->uj_hi = c->n;

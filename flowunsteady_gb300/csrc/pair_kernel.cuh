@@ -157,7 +157,6 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 
   const int tid = threadIdx.x;
   const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
-  const bool same_arrays = a.xt == a.xs && a.ldt == a.lds;
   // Packed records replace the FP64 source reads (and their conversion) when
   // the host provides them; bulk copies need them.
   const bool use_rec = Tr::kRec && a.rec != nullptr;
@@ -245,9 +244,9 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       }
     }
 
-    if constexpr (kFarKernel) {
-      if (use_far) warp_target_box<T>(tx, ty, tz, tbox + 2 * warp);
-    }
+    // FP32: the warp's target box, against which every staged 32-source block
+    // is tested for overlap (coincident pairs) and, for Gaussian-erf, distance.
+    if constexpr (F32) warp_target_box<T>(tx, ty, tz, tbox + 2 * warp);
 
     R acc[T][NV];
 #pragma unroll
@@ -300,9 +299,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           }
           tileA[tid] = qa;
           tileB[tid] = qb;
-          if constexpr (kFarKernel) {
-            if (use_far) warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
-          }
+          warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
           __syncthreads();  // quads ready, staging records consumed
           if (tid == 0 && tile0 + BLOCK < s1) issue(tile0 + BLOCK, s1);
         }
@@ -349,28 +346,40 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         tileB[tid] = qb;
         if (!Tr::kUJ) tileC[tid] = qc;
         if (PASS == PASS_ZETAD) tileD[tid] = qd;
-        if constexpr (kFarKernel) {
-          if (use_far) warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
-        }
+        if constexpr (F32) warp_source_box(qa.x, qa.y, qa.z, qa.w, jj < s1, sbox + 2 * warp);
         __syncthreads();
       }
 
       // ---- all pairs of the tile ------------------------------------------
       const int cnt = int(min(int64_t(BLOCK), s1 - tile0));
-      // Coincident pairs can only occur in tiles that overlap the CTA's own
-      // targets (or anywhere when the targets are a separate array).
-      const bool own = !same_arrays || (tile0 < t1 && tile0 + BLOCK > t0);
+      // FP32: coincident pairs (r² = 0, skipped as the reference's direct sums
+      // skip them) can only occur in 32-source blocks whose box intersects the
+      // warp's target box; only those blocks run the masked pair forms.  The
+      // test is exact in the kernel's own coordinates (comparisons only), so
+      // a target's own particle and any other particle at the same position
+      // are masked wherever they sit.  (FP64 masks every pair.)
+      uint32_t ovl = 0;
+      if constexpr (F32) ovl = overlap_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt);
       if constexpr (Tr::kUJ && F32) {
         const float4* ta = reinterpret_cast<const float4*>(tileA);
         const float4* tb = reinterpret_cast<const float4*>(tileB);
         if constexpr (PASS == PASS_UJ) {
-          if (KERNEL == VPM_KERNEL_WINCKELMANS && !own) {
+          if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+            // Runs of blocks: masked where the boxes intersect.
+            const uint32_t cls = overlap_codes<BLOCK / 32>(ovl, 1u);
+            for (int js = 0; js < cnt;) {
+              const int je = block_run_end(cls, js, cnt, [](uint32_t c) { return c; });
+              if ((ovl >> (js >> 5)) & 1u) {
 #pragma unroll 2
-            for (int js = 0; js < cnt; ++js) uj_source_winck<T, false>(ta[js], tb[js], tx, ty, tz, acc);
-          } else if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+                for (; js < je; ++js) uj_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
+              } else {
 #pragma unroll 2
-            for (int js = 0; js < cnt; ++js) uj_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
+                for (; js < je; ++js) uj_source_winck<T, false>(ta[js], tb[js], tx, ty, tz, acc);
+              }
+            }
           } else {
+            // Gaussian-erf masks coincident pairs in its series branch, which
+            // every warp holding a pair with ρ² < 3/2 takes.
             // Gaussian-erf by runs of 32-source blocks of one class: far blocks
             // skip erfcx/exp, vote blocks decide per source.
             const uint32_t cls = classify_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt,
@@ -392,10 +401,16 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
             }
           }
         } else {
-          if (KERNEL == VPM_KERNEL_WINCKELMANS && !own) {
-            for (int js = 0; js < cnt; ++js) ujd_source_winck<T, false>(ta[js], tb[js], tx, ty, tz, acc);
-          } else if (KERNEL == VPM_KERNEL_WINCKELMANS) {
-            for (int js = 0; js < cnt; ++js) ujd_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
+          if (KERNEL == VPM_KERNEL_WINCKELMANS) {
+            const uint32_t cls = overlap_codes<BLOCK / 32>(ovl, 1u);
+            for (int js = 0; js < cnt;) {
+              const int je = block_run_end(cls, js, cnt, [](uint32_t c) { return c; });
+              if ((ovl >> (js >> 5)) & 1u) {
+                for (; js < je; ++js) ujd_source_winck<T, true>(ta[js], tb[js], tx, ty, tz, acc);
+              } else {
+                for (; js < je; ++js) ujd_source_winck<T, false>(ta[js], tb[js], tx, ty, tz, acc);
+              }
+            }
           } else {
             // Gaussian-erf: where Dq and Dp vanish only the plain sums take the
             // pair; far blocks skip erfcx.
@@ -456,41 +471,38 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         const float4* tc = reinterpret_cast<const float4*>(tileC);
         const float4* td = reinterpret_cast<const float4*>(PASS == PASS_ZETAD ? tileD : tileC);
         constexpr bool DD = PASS == PASS_ZETAD;
+        // Block codes: 3 skip (Gaussian-erf ζ is exactly zero at every target
+        // of the warp), 2 masked (boxes intersect), 1 per-source votes, 0 the
+        // general form.
+        uint32_t cls = overlap_codes<BLOCK / 32>(ovl, 2u);
         if (kFarKernel && use_far) {
-          // Gaussian-erf: blocks of 32 sources whose ζ is exactly zero at every
-          // target of the warp are skipped.
-          // Runs of 32-source blocks: zero blocks are skipped, far and vote
-          // blocks decide per source (outside the CTA's own tiles).
-          const uint32_t cls = classify_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt,
+          const uint32_t far = classify_blocks<BLOCK / 32>(tbox + 2 * warp, sbox, cnt,
                                                            kVoteSpan * kArgZero, true);
-          auto key = [](uint32_t c) { return c == 3u ? 3u : (c >= 1u ? 1u : 0u); };
-          for (int js = 0; js < cnt;) {
-            const int je = block_run_end(cls, js, cnt, key);
-            const uint32_t c = key((cls >> (2 * (js >> 5))) & 3u);
-            if (c == 3u) {
-              js = je;
-            } else if (!own && c == 1u) {
-#pragma unroll 2
-              for (; js < je; ++js)
-                zeta_source<KERNEL, T, false, DD, true>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
-            } else if (!own) {
-#pragma unroll 2
-              for (; js < je; ++js)
-                zeta_source<KERNEL, T, false, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
-            } else {
-#pragma unroll 2
-              for (; js < je; ++js)
-                zeta_source<KERNEL, T, true, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
-            }
+#pragma unroll
+          for (int b = 0; b < BLOCK / 32; ++b) {
+            const uint32_t f = (far >> (2 * b)) & 3u;
+            if (f == 3u) cls |= 3u << (2 * b);            // zero blocks cannot coincide
+            else if (f >= 1u && !((ovl >> b) & 1u)) cls |= 1u << (2 * b);
           }
-        } else if (!own) {
+        }
+        for (int js = 0; js < cnt;) {
+          const int je = block_run_end(cls, js, cnt, [](uint32_t c) { return c; });
+          const uint32_t c = (cls >> (2 * (js >> 5))) & 3u;
+          if (c == 3u) {
+            js = je;
+          } else if (c == 2u) {
 #pragma unroll 2
-          for (int js = 0; js < cnt; ++js)
-            zeta_source<KERNEL, T, false, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
-        } else {
+            for (; js < je; ++js)
+              zeta_source<KERNEL, T, true, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+          } else if (c == 1u) {
 #pragma unroll 2
-          for (int js = 0; js < cnt; ++js)
-            zeta_source<KERNEL, T, true, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+            for (; js < je; ++js)
+              zeta_source<KERNEL, T, false, DD, true>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+          } else {
+#pragma unroll 2
+            for (; js < je; ++js)
+              zeta_source<KERNEL, T, false, DD, false>(ta[js], tb[js], tc[js], td[js], tx, ty, tz, acc);
+          }
         }
       } else {
         // ζ passes, FP64.

@@ -138,6 +138,17 @@ __global__ void __launch_bounds__(256) sfs_dynamic_kernel(
   C[2 * ld + i] = deno;
 }
 
+// Backscatter clipping on its own (vpm.clipping_backscatter): C_d = 0 where
+// C_d Γ·E_str < 0.
+__global__ void sfs_clip_kernel(int64_t nv, const uint8_t* __restrict__ stat, int64_t ld,
+                                const double* __restrict__ G, const double* __restrict__ E,
+                                double* __restrict__ C) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= nv || (stat && stat[i])) return;
+  const double ge = G[i] * E[i] + G[ld + i] * E[ld + i] + G[2 * ld + i] * E[2 * ld + i];
+  if (C[i] * ge < 0.0) C[i] = 0.0;
+}
+
 __global__ void sfs_constant_kernel(int64_t nv, const uint8_t* __restrict__ stat, double cd,
                                     double* C) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -399,6 +410,13 @@ cudaError_t launch_sfs_dynamic(int64_t nv, const uint8_t* stat, int64_t ld, cons
                                cudaStream_t st) {
   if (nv <= 0) return cudaSuccess;
   sfs_dynamic_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, stat, ld, G, S, J, Jt, E, Et, C, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sfs_clip(int64_t nv, const uint8_t* stat, int64_t ld, const double* G,
+                            const double* E, double* C, cudaStream_t st) {
+  if (nv <= 0) return cudaSuccess;
+  sfs_clip_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, stat, ld, G, E, C);
   return cudaGetLastError();
 }
 

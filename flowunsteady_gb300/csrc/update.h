@@ -55,6 +55,8 @@ cudaError_t launch_sfs_dynamic(int64_t nv, const uint8_t* stat, int64_t ld, cons
                                cudaStream_t st);
 cudaError_t launch_sfs_constant(int64_t nv, const uint8_t* stat, double cd, double* C,
                                 cudaStream_t st);
+cudaError_t launch_sfs_clip(int64_t nv, const uint8_t* stat, int64_t ld, const double* G,
+                            const double* E, double* C, cudaStream_t st);
 cudaError_t launch_rk_update(int64_t nv, const uint8_t* stat, int64_t ld, double* X, double* G,
                              double* S, const double* U, const double* J, const double* E,
                              double* C, double* Q, const UpdateParams& p, int* status,

@@ -715,6 +715,38 @@ __device__ __forceinline__ uint32_t classify_blocks(const float4* tbox, const fl
   return cls;
 }
 
+// Bit b set where the warp's target box (tbox[0..1]) and staged block b's
+// source box (sbox[2b..2b+1]) intersect.  Only there can a target and a source
+// coincide (r² = 0 needs equal coordinates, which lie in both boxes); the
+// test uses comparisons only, so it is exact.  Padding sources are outside
+// every box (their block box is empty when all are padding).
+template <int NB>
+__device__ __forceinline__ uint32_t overlap_blocks(const float4* tbox, const float4* sbox,
+                                                   int cnt) {
+  const float4 tl = tbox[0], th = tbox[1];
+  uint32_t m = 0;
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    if (b * 32 < cnt) {
+      const float4 sl = sbox[2 * b], sh = sbox[2 * b + 1];
+      const bool o = sl.x <= th.x && tl.x <= sh.x && sl.y <= th.y && tl.y <= sh.y &&
+                     sl.z <= th.z && tl.z <= sh.z;
+      m |= uint32_t(o) << b;
+    }
+  }
+  return m;
+}
+
+// 2-bit block codes: `code` at every block whose overlap bit is set, 0 elsewhere.
+template <int NB>
+__device__ __forceinline__ uint32_t overlap_codes(uint32_t ovl, uint32_t code) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int b = 0; b < NB; ++b)
+    if ((ovl >> b) & 1u) c |= code << (2 * b);
+  return c;
+}
+
 // End (exclusive, in sources) of the run of blocks that starts at source js and
 // shares the class `key(block class)` of its first block.
 template <typename Key>

@@ -12,10 +12,10 @@ oracle, through the C ABI:
 
 Each case runs two RK3 steps.  FP64 pair passes: positions and core sizes
 within 1e-12 relative (max), strengths within 1e-9 relative (max), C_d within
-1e-7.  FP32C pair passes: positions within 1e-8 (max absolute; |x| <= 0.5),
-strengths within 1e-5 relative L2 (2e-4 when the finite-difference C_d's
-1/(1-α) = 1000 amplification of FP32 rounding enters), core sizes within 1e-6
-relative."""
+1e-7.  FP32C pair passes, measured on the increments of the two steps
+(x - x0, Γ - Γ0, σ - σ0) in relative L2: positions within 1e-5, strengths and
+core sizes within 1e-4 (1e-2 when the finite-difference C_d's 1/(1-α) = 1000
+amplification of FP32 rounding enters)."""
 import numpy as np
 import pytest
 
@@ -82,10 +82,11 @@ def test_scheme_fp64_matches_oracle(oracle, name, kernel):
 @pytest.mark.parametrize("kernel", [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF])
 def test_scheme_fp32c_tracks_oracle(oracle, name, kernel):
     kw, fd = CASES[name]
+    X0, G0, S0 = field()
     (Xg, Gg, Sg, _, _), (Xo, Go, So, _, _) = run_case(oracle, kernel, L.PREC_FP32C, kw)
-    assert np.abs(Xg - Xo).max() <= 1e-8
-    assert rel_l2(Gg, Go) <= (2e-4 if fd else 1e-5)
-    assert rel_max(Sg, So) <= 1e-6
+    assert rel_l2(Xg - X0, Xo - X0) <= 1e-5
+    assert rel_l2(Gg - G0, Go - G0) <= (1e-2 if fd else 1e-4)
+    assert rel_l2(Sg - S0, So - S0) <= (1e-2 if fd else 1e-4)
 
 
 def test_classic_and_transposed_differ():
