@@ -183,7 +183,7 @@ def _declare(lib):
         "vpm_measure_fma_peaks": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp]),
         "vpm_debug_fail_after": (ctypes.c_int, [_vp, _i64]),
         "vpm_debug_last_plan": (ctypes.c_int, [P(ctypes.c_int32), P(ctypes.c_int32),
-                                               P(ctypes.c_int32)]),
+                                               P(ctypes.c_int32), P(ctypes.c_int32)]),
         "vpm_get_launch_count": (ctypes.c_int, [_vp, P(_i64)]),
         "vpm_build_info": (ctypes.c_char_p, []),
     }

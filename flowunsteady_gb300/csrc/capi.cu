@@ -114,8 +114,61 @@ int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chun
   return best_c;
 }
 
+// Clusters of `cluster` CTAs of a shape resident at once (cached per device).
+int active_clusters(int device, int pass, int kernel, int precision, Shape s, int cluster) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int, int, int>, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_tuple(device, pass, kernel, precision, s.block, s.tpt, cluster);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  const int n = pair_max_active_clusters(pass, kernel, precision, s, cluster);
+  cache[key] = n;
+  return n;
+}
+
+int cluster_mode() {
+  static const int mode = [] {
+    const char* v = std::getenv("VPM_CLUSTER");
+    if (!v || !v[0]) return -1;
+    return v[0] == '0' ? 0 : 1;
+  }();
+  return mode;
+}
+
+// Largest cluster of the split-source form (16 needs the non-portable size).
+constexpr int kMaxCluster = 16;
+
+// Split-source clusters for an FP32C pass of n_tb target tiles over ns
+// sources: the cluster size (1 = none fits) whose clusters fill whole waves
+// best, with its chunk length and wave efficiency score (as plan_chunks').
+static int plan_cluster(int device, const PairCall& pc, Shape sh, int64_t n_tb,
+                        int64_t* chunk_out, double* score_out) {
+  int best_nc = 1;
+  double best = -1.0;
+  for (int nc = 2; nc <= kMaxCluster; ++nc) {
+    const int64_t chunk = round_up(std::max<int64_t>(ceil_div(pc.ns, nc), 1), sh.block);
+    if (chunk < 2 * sh.block) break;
+    if (ceil_div(pc.ns, chunk) != nc) continue;   // exactly nc non-empty chunks
+    const int slots = active_clusters(device, pc.pass, pc.kernel, pc.prec, sh, nc);
+    if (slots <= 0) continue;
+    const int64_t waves = ceil_div(n_tb, slots);
+    const double score = double(n_tb) / double(waves * slots) - 0.003 * nc;
+    if (score > best + 1e-12) {
+      best = score;
+      best_nc = nc;
+      *chunk_out = chunk;
+    }
+  }
+  *score_out = best;
+  return best_nc;
+}
+
 // Plan and enqueue one pair pass.  `need_part` (elements) is raised to what
-// the launch needs; when dry, nothing is launched.
+// the launch needs; when dry, nothing is launched.  A split source range goes
+// either through partial slots summed by a reduction launch, or (FP32C,
+// single field) through clusters that sum on chip: clusters are taken when
+// they fill the waves within 2 % as well as the slot plan.
 cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* pinned,
                      double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
                      cudaStream_t st, PairPlan* plan_out) {
@@ -126,16 +179,33 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   const int64_t n_tb = ceil_div(nt, TB);
   const int resident = resident_ctas(device, pc.pass, pc.kernel, pc.prec, sh, num_sms);
   int64_t chunk = 0;
-  int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
-  const int nv = nval_of(pc.pass);
-  const size_t need = n_chunk > 1 ? size_t(n_chunk) * nv * size_t(ldp) : 0;
-  if (need_part) *need_part = std::max(*need_part, need);
-  if (plan_out) {
-    plan_out->shape = sh;
-    plan_out->n_tb = n_tb;
-    plan_out->n_chunk = n_chunk;
-    plan_out->chunk = chunk;
+  int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, 0);
+  int cluster = 1;
+  if (pc.prec == VPM_PREC_FP32C && n_chunk > 1 && cluster_mode() != 0) {
+    const int64_t items = n_tb * n_chunk;
+    const int64_t waves = ceil_div(items, resident);
+    const double slot_score = double(items) / double(waves * resident) - 0.003 * n_chunk;
+    int64_t cchunk = 0;
+    double cscore = -1.0;
+    const int nc = plan_cluster(device, pc, sh, n_tb, &cchunk, &cscore);
+    if (nc > 1 && (cluster_mode() == 1 || cscore >= slot_score - 0.02)) {
+      cluster = nc;
+      n_chunk = nc;
+      chunk = cchunk;
+    }
   }
+  if (cluster <= 1 && pc.max_chunks > 0 && n_chunk > pc.max_chunks)
+    n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
+  PairPlan plan;
+  plan.shape = sh;
+  plan.n_tb = n_tb;
+  plan.n_chunk = n_chunk;
+  plan.chunk = chunk;
+  plan.cluster = cluster;
+  const int nv = nval_of(pc.pass);
+  const size_t need = plan.slots() > 1 ? size_t(plan.slots()) * nv * size_t(ldp) : 0;
+  if (need_part) *need_part = std::max(*need_part, need);
+  if (plan_out) *plan_out = plan;
   if (dry) return cudaSuccess;
   if (need > part_elems) return cudaErrorMemoryAllocation;
   PairArgs a;
@@ -155,9 +225,10 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.far = farfield_enabled() ? 1 : 0;
   a.coh = pc.coh;
   a.coh_blocks = ceil_div(pc.ns, 32);
+  a.cluster = cluster;
   cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
-  if (n_chunk > 1) {
+  if (plan.slots() > 1) {
     e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
@@ -477,11 +548,10 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
   if (recs) pc.rec = c->rec;
   const Shape* pinned = &c->pinned[pass & 1][kernel][prec];
   PairPlan plan;
-  plan.n_chunk = 1;
   e = run_pair(pc, c->device, c->num_sms, pinned, c->part, ld, c->part_elems, &c->part_need,
                c->dry, c->st, &plan);
   if (c->dry || e != cudaSuccess) return e;
-  c->launches += plan.n_chunk > 1 ? 2 : 1;
+  c->launches += plan.slots() > 1 ? 2 : 1;
   return scatter_outputs(c, pass, perm, u, j, dj);
 }
 
@@ -577,10 +647,9 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   }
   const Shape* pinned = &c->pinned[pass & 1][kernel][prec];  // D passes share their plain pass's pin
   PairPlan plan;
-  plan.n_chunk = 1;
   cudaError_t e = run_pair(pc, c->device, c->num_sms, pinned, c->part, c->ld, c->part_elems,
                            &c->part_need, c->dry, c->st, &plan);
-  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += plan.n_chunk > 1 ? 2 : 1;
+  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += plan.slots() > 1 ? 2 : 1;
   return e;
 }
 

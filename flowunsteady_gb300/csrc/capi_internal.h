@@ -39,15 +39,22 @@ struct PairCall {
 };
 
 struct PairPlan {
-  Shape shape;
-  int64_t n_tb;
-  int n_chunk;
-  int64_t chunk;
+  Shape shape = Shape{0, 0};
+  int64_t n_tb = 0;
+  int n_chunk = 1;      // source chunks per target tile
+  int64_t chunk = 0;    // sources per chunk
+  int cluster = 1;      // > 1: the chunks of a tile are one cluster, summed on chip
+  // Partial slots the plan writes (and a reduction launch sums).
+  int slots() const { return (n_chunk > 1 && cluster <= 1) ? n_chunk : 1; }
 };
 
 // Plan of the last stateless U/J call (vpm_uj_device_async/_noalloc) on this
 // host thread, for vpm_debug_last_plan.
 extern thread_local PairPlan g_last_stateless_plan;
+// Split-source clusters: -1 (VPM_CLUSTER unset) lets the planner choose, 0
+// (VPM_CLUSTER=0) always uses partial slots, 1 (VPM_CLUSTER=1) takes clusters
+// whenever a cluster size fits.
+int cluster_mode();
 
 Shape default_shape(int pass, int precision, int64_t n);
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n, const Shape* pinned);

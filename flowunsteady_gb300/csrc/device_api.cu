@@ -11,7 +11,7 @@
 using namespace vpm;
 
 namespace vpm {
-thread_local PairPlan g_last_stateless_plan = {Shape{0, 0}, 0, 0, 0};
+thread_local PairPlan g_last_stateless_plan = PairPlan();
 }  // namespace vpm
 
 extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const double* Xs,
@@ -78,10 +78,12 @@ extern "C" int vpm_uj_device_async(int kernel, int precision, int64_t ns, const 
   return VPM_OK;
 }
 
-extern "C" int vpm_debug_last_plan(int32_t* block, int32_t* tpt, int32_t* n_chunk) {
+extern "C" int vpm_debug_last_plan(int32_t* block, int32_t* tpt, int32_t* n_chunk,
+                                   int32_t* cluster) {
   const PairPlan& p = g_last_stateless_plan;
   if (block) *block = p.shape.block;
   if (tpt) *tpt = p.shape.tpt;
-  if (n_chunk) *n_chunk = p.n_chunk;
+  if (n_chunk) *n_chunk = p.n_tb > 0 ? p.n_chunk : 0;
+  if (cluster) *cluster = p.n_tb > 0 ? p.cluster : 0;
   return VPM_OK;
 }

@@ -76,6 +76,11 @@ struct PairArgs {
   const unsigned int* coh;
   int64_t coh_blocks;
   int* status;   // STATUS_TIMEOUT is OR-ed here if a copy wait gives up (may be null)
+  // FP32C single-field form only: > 1 when the n_chunk source chunks of a
+  // target tile run as one thread-block cluster of `cluster` CTAs (grid =
+  // n_tb x cluster, cluster rank = chunk) that sum their compensated partial
+  // sums through distributed shared memory in rank order; no partial slots.
+  int32_t cluster;
 };
 
 // Tile shape of a launch.
@@ -98,6 +103,10 @@ cudaError_t launch_pair(int pass, int kernel, int precision, Shape shape, const 
                         int grid, cudaStream_t st);
 // Dynamic shared memory of a shape (bytes).
 size_t pair_smem_bytes(int pass, int precision, Shape shape);
+// Clusters of `cluster` CTAs of a shape that fit on the device at once (0: the
+// shape cannot run as such clusters; only FP32C shapes do).
+int pair_max_active_clusters(int pass, int kernel, int precision, Shape shape, int cluster);
+int pair_max_active_clusters_d(int pass, int kernel, int precision, Shape shape, int cluster);
 // Max resident CTAs per SM of a shape.
 int pair_ctas_per_sm(int pass, int kernel, int precision, Shape shape);
 // Whether a shape is compiled.

@@ -22,6 +22,12 @@ int pair_ctas_per_sm(int pass, int kernel, int precision, Shape s) {
   return pair_ctas_per_sm_d(pass, kernel, precision, s);
 }
 
+int pair_max_active_clusters(int pass, int kernel, int precision, Shape s, int cluster) {
+  if (pass == PASS_UJ) return max_active_clusters<PASS_UJ>(kernel, precision, s, cluster);
+  if (pass == PASS_ZETA) return max_active_clusters<PASS_ZETA>(kernel, precision, s, cluster);
+  return pair_max_active_clusters_d(pass, kernel, precision, s, cluster);
+}
+
 cudaError_t launch_pair(int pass, int kernel, int precision, Shape s, const PairArgs& a, int grid,
                         cudaStream_t st) {
   if (pass == PASS_UJ) return launch<PASS_UJ>(kernel, precision, s, a, grid, st);

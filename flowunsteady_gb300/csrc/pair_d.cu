@@ -13,6 +13,11 @@ int pair_ctas_per_sm_d(int pass, int kernel, int precision, Shape s) {
                           : ctas_per_sm<PASS_ZETAD>(kernel, precision, s);
 }
 
+int pair_max_active_clusters_d(int pass, int kernel, int precision, Shape s, int cluster) {
+  return pass == PASS_UJD ? max_active_clusters<PASS_UJD>(kernel, precision, s, cluster)
+                          : max_active_clusters<PASS_ZETAD>(kernel, precision, s, cluster);
+}
+
 cudaError_t launch_pair_d(int pass, int kernel, int precision, Shape s, const PairArgs& a,
                           int grid, cudaStream_t st) {
   return pass == PASS_UJD ? launch<PASS_UJD>(kernel, precision, s, a, grid, st)

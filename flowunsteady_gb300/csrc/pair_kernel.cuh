@@ -29,6 +29,7 @@
 // a whole number of waves, or a persistent grid pulls items from a queue.
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #include "internal.h"
@@ -123,9 +124,53 @@ __device__ inline void write_final(const double* v, const PairArgs& a, int64_t i
   }
 }
 
+// Cluster form of the epilogue (FP32C): after every rank's (hi, lo) pairs are
+// final, rank r forms the values of the targets [r·per, (r+1)·per) of the
+// tile from every rank's pairs, in rank order: the same FP64 sums, in the same
+// order, as the partial-slot form and its fixed-order reduction.
 template <int PASS, int KERNEL, int PREC, int BLOCK, int T>
+__device__ __forceinline__ void cluster_epilogue(const PairArgs& a, const float* fold_hi,
+                                              const float* fold_lo, int64_t t0, int64_t t1) {
+  using Tr = PairTraits<PASS, PREC>;
+  constexpr int NV = Tr::kNval;
+  constexpr int TB = BLOCK * T;
+  const int tid = threadIdx.x;
+  const uint32_t nc = uint32_t(a.cluster), rank = cluster_ctarank();
+  const int per = (TB + int(nc) - 1) / int(nc);
+  const int tend = min(TB, int(rank + 1) * per);
+  for (int t = int(rank) * per + tid; t < tend; t += BLOCK) {
+    const int64_t i = t0 + t;
+    if (i >= t1) break;
+    const int k = t / BLOCK, j = t % BLOCK;
+    // Rank q's value w, as the partial-slot epilogue forms it.
+    auto rank_value = [&](int w, uint32_t q) {
+      const int o = (w * T + k) * BLOCK + j;
+      double u = double(ld_cluster_f32(fold_hi + o, q)) + double(ld_cluster_f32(fold_lo + o, q));
+      if (Tr::kUJ && KERNEL == VPM_KERNEL_GAUSSIANERF && w >= 3 && w < 11) u *= kGaussAScale;
+      return u;
+    };
+    double v[NV];
+#pragma unroll
+    for (int w = 0; w < NV; ++w) {
+      double sum = 0.0;
+      for (uint32_t q = 0; q < nc; ++q) {
+        // U/J: the trace-free A22 (and DA22) rebuilt per rank.
+        if (Tr::kUJ && w == 11) sum += -(rank_value(3, q) + rank_value(7, q));
+        else if (PASS == PASS_UJD && w == 23) sum += -(rank_value(15, q) + rank_value(19, q));
+        else sum += rank_value(w, q);
+      }
+      v[w] = sum;
+    }
+    write_final<PASS, KERNEL>(v, a, i);
+  }
+}
+
+// CLU: the split-source cluster form (FP32C only; launched with a cluster
+// dimension of a.cluster CTAs, one item per CTA).
+template <int PASS, int KERNEL, int PREC, int BLOCK, int T, bool CLU = false>
 __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     pair_kernel(const PairArgs a) {
+  static_assert(!CLU || PREC == VPM_PREC_FP32C, "the cluster form sums compensated pairs");
   using Tr = PairTraits<PASS, PREC>;
   using R = typename Tr::R;
   constexpr bool COMP = Tr::kComp;
@@ -197,12 +242,15 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       const PairItem it = a.items[item];
       t0 = it.t0; t1 = it.t1; s0 = it.s0; s1 = it.s1; slot = it.slot;
     } else {
-      const int tb = item % a.n_tb, c = item / a.n_tb;
+      // Clusters: consecutive CTAs share a target tile, cluster rank = chunk;
+      // otherwise chunk-major items with a partial slot per chunk.
+      const int tb = CLU ? item / a.cluster : item % a.n_tb;
+      const int c = CLU ? item % a.cluster : item / a.n_tb;
       t0 = a.t_off + int64_t(tb) * TB;
       t1 = min(t0 + TB, a.t_off + a.nt);
       s0 = int64_t(c) * a.chunk;
       s1 = min(s0 + a.chunk, a.ns);
-      slot = a.n_chunk > 1 ? c : -1;
+      slot = (a.n_chunk > 1 && !CLU) ? c : -1;
     }
 
     // Reference point of the CTA: its first target (FP32C only).
@@ -264,6 +312,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     }
 
     int tiles = 0;
+    bool aborted = false;
     if (use_tma && tid == 0 && s0 < s1) issue(s0, s1);
     for (int64_t tile0 = s0; tile0 < s1; tile0 += BLOCK) {
       // ---- stage one tile of sources -------------------------------------
@@ -280,7 +329,9 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
             // copy just waited on is the only one that could land late.
             if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
             mbar_wait(bar, phase ^ 1u, 1 << 26);
-            return;
+            if constexpr (!CLU) return;
+            aborted = true;
+            break;
           }
           const int64_t jj = tile0 + tid;
           Quad<R> qa, qb;
@@ -550,6 +601,19 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       }
     }
 
+    // A CTA whose copy timed out leaves without results (the status word
+    // reports it); in a cluster it still takes part in both cluster barriers
+    // below, so that no CTA leaves while another may read its shared memory.
+
+    // ---- epilogue: cluster form ----------------------------------------------
+    if constexpr (CLU) {
+      // Every rank's (hi, lo) pairs are final after the first barrier.
+      cluster_sync_all();
+      if (!aborted) cluster_epilogue<PASS, KERNEL, PREC, BLOCK, T>(a, fold_hi, fold_lo, t0, t1);
+      cluster_sync_all();   // remote reads done before any CTA leaves
+      return;
+    }
+
     // ---- epilogue ------------------------------------------------------------
 #pragma unroll
     for (int k = 0; k < T; ++k) {
@@ -624,16 +688,20 @@ __global__ void reduce_kernel(const double* __restrict__ part, int64_t ldp,
 // ---------------------------------------------------------------- dispatch --
 typedef void (*PairFn)(const PairArgs);
 
-template <int PASS, int KERNEL, int PREC, int BLOCK, int T>
+template <int PASS, int KERNEL, int PREC, int BLOCK, int T, bool CLU = false>
 PairFn fn_ready() {
   static bool once = [] {
-    cudaFuncSetAttribute(pair_kernel<PASS, KERNEL, PREC, BLOCK, T>,
+    cudaFuncSetAttribute(pair_kernel<PASS, KERNEL, PREC, BLOCK, T, CLU>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(smem_bytes<PASS, PREC>(BLOCK, T)));
+    // Clusters of up to 16 CTAs (beyond the portable 8) for the split-source form.
+    if (CLU)
+      cudaFuncSetAttribute(pair_kernel<PASS, KERNEL, PREC, BLOCK, T, CLU>,
+                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return true;
   }();
   (void)once;
-  return pair_kernel<PASS, KERNEL, PREC, BLOCK, T>;
+  return pair_kernel<PASS, KERNEL, PREC, BLOCK, T, CLU>;
 }
 
 // Compiled shapes: FP64 {128x1}; FP32 and FP32C {128x2, 128x4, 256x2}.
@@ -666,6 +734,23 @@ PairFn pick_kernel(int kernel, int prec, Shape s) {
                                           : pick_prec<PASS, VPM_KERNEL_GAUSSIANERF>(prec, s);
 }
 
+// The cluster form of an FP32C shape (null for other precisions and shapes).
+template <int PASS, int KERNEL>
+PairFn pick_cluster_k(Shape s) {
+  constexpr int P = VPM_PREC_FP32C;
+  if (s.block == 128 && s.tpt == 2) return fn_ready<PASS, KERNEL, P, 128, 2, true>();
+  if (s.block == 128 && s.tpt == 4) return fn_ready<PASS, KERNEL, P, 128, 4, true>();
+  if (s.block == 256 && s.tpt == 2) return fn_ready<PASS, KERNEL, P, 256, 2, true>();
+  return nullptr;
+}
+
+template <int PASS>
+PairFn pick_cluster(int kernel, int prec, Shape s) {
+  if (prec != VPM_PREC_FP32C) return nullptr;
+  return kernel == VPM_KERNEL_WINCKELMANS ? pick_cluster_k<PASS, VPM_KERNEL_WINCKELMANS>(s)
+                                          : pick_cluster_k<PASS, VPM_KERNEL_GAUSSIANERF>(s);
+}
+
 template <int PASS>
 size_t smem_of(int precision, Shape s) {
   switch (precision) {
@@ -686,14 +771,60 @@ int ctas_per_sm(int kernel, int precision, Shape s) {
   return n;
 }
 
+// Launch configuration of a cluster launch (`attr` receives the attribute).
+inline cudaLaunchConfig_t cluster_config(int grid, int block, size_t smem, cudaStream_t st,
+                                         int cluster, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(unsigned(grid), 1, 1);
+  cfg.blockDim = dim3(unsigned(block), 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  attr->id = cudaLaunchAttributeClusterDimension;
+  attr->val.clusterDim.x = unsigned(cluster);
+  attr->val.clusterDim.y = 1;
+  attr->val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
 template <int PASS>
 cudaError_t launch(int kernel, int precision, Shape s, const PairArgs& a, int grid,
                    cudaStream_t st) {
   PairFn f = pick_kernel<PASS>(kernel, precision, s);
   if (!f) return cudaErrorInvalidConfiguration;
   if (grid <= 0) return cudaSuccess;
+  if (a.cluster > 1) {
+    // One item per CTA, every CTA of a cluster on the same target tile.
+    f = pick_cluster<PASS>(kernel, precision, s);
+    if (!f || a.items || a.counter || grid % a.cluster != 0 ||
+        int64_t(grid) != int64_t(a.n_tb) * a.n_chunk || a.n_chunk != a.cluster)
+      return cudaErrorInvalidConfiguration;
+    cudaLaunchAttribute attr;
+    cudaLaunchConfig_t cfg = cluster_config(grid, s.block, smem_of<PASS>(precision, s), st,
+                                            a.cluster, &attr);
+    return cudaLaunchKernelEx(&cfg, f, a);
+  }
   f<<<grid, s.block, smem_of<PASS>(precision, s), st>>>(a);
   return cudaGetLastError();
+}
+
+// Clusters of `cluster` CTAs of a shape that can be resident at once (0: none
+// can be scheduled, or the query failed).
+template <int PASS>
+int max_active_clusters(int kernel, int precision, Shape s, int cluster) {
+  PairFn f = pick_cluster<PASS>(kernel, precision, s);
+  if (!f) return 0;
+  cudaLaunchAttribute attr;
+  cudaLaunchConfig_t cfg = cluster_config(cluster, s.block, smem_of<PASS>(precision, s), nullptr,
+                                          cluster, &attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, f, &cfg) != cudaSuccess) {
+    cudaGetLastError();   // clear the sticky-free error of a refused query
+    return 0;
+  }
+  return n;
 }
 
 template <int PASS>

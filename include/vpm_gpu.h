@@ -420,10 +420,12 @@ int vpm_measure_fma_peaks(int device, double* fp32_tflops, double* fp64_tflops, 
 int vpm_debug_fail_after(vpm_ctx* ctx, int64_t k);
 
 /* Work plan of the last successful vpm_uj_device_async / vpm_uj_device_noalloc
- * call on this host thread: tile shape (threads per CTA, targets per thread)
- * and the number of source chunks (> 1: partial sums went through scratch).
- * Zeros before the first call.  Any pointer may be NULL. */
-int vpm_debug_last_plan(int32_t* block, int32_t* tpt, int32_t* n_chunk);
+ * call on this host thread: tile shape (threads per CTA, targets per thread),
+ * the number of source chunks each target tile is split into, and the cluster
+ * size: 1 when the chunks' partial sums went through scratch (if n_chunk > 1),
+ * n_chunk when the chunks ran as one thread-block cluster summing them in
+ * shared memory.  Zeros before the first call.  Any pointer may be NULL. */
+int vpm_debug_last_plan(int32_t* block, int32_t* tpt, int32_t* n_chunk, int32_t* cluster);
 
 /* Number of kernels the context has enqueued since creation (pair passes,
  * reductions and updates; a graph replay counts its kernels). */

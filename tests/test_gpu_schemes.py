@@ -13,9 +13,11 @@ oracle, through the C ABI:
 Each case runs two RK3 steps.  FP64 pair passes: positions and core sizes
 within 1e-12 relative (max), strengths within 1e-9 relative (max), C_d within
 1e-7.  FP32C pair passes, measured on the increments of the two steps
-(x - x0, Γ - Γ0, σ - σ0) in relative L2: positions within 1e-5, strengths and
-core sizes within 1e-4 (1e-2 when the finite-difference C_d's 1/(1-α) = 1000
-amplification of FP32 rounding enters)."""
+(x - x0, Γ - Γ0, σ - σ0) in relative L2: positions within 2e-6, strengths and
+core sizes within 2e-5 (measured: 2-3e-7 and up to 1.8e-6).  Where the
+finite-difference C_d enters, its 1/(1-α) = 1000 amplification of FP32
+rounding moves C_d by ~1e-3 relative: positions within 1e-3, strengths and
+core sizes within 1e-2 (measured: up to 7e-5 and 8e-4)."""
 import numpy as np
 import pytest
 
@@ -84,9 +86,9 @@ def test_scheme_fp32c_tracks_oracle(oracle, name, kernel):
     kw, fd = CASES[name]
     X0, G0, S0 = field()
     (Xg, Gg, Sg, _, _), (Xo, Go, So, _, _) = run_case(oracle, kernel, L.PREC_FP32C, kw)
-    assert rel_l2(Xg - X0, Xo - X0) <= 1e-5
-    assert rel_l2(Gg - G0, Go - G0) <= (1e-2 if fd else 1e-4)
-    assert rel_l2(Sg - S0, So - S0) <= (1e-2 if fd else 1e-4)
+    assert rel_l2(Xg - X0, Xo - X0) <= (1e-3 if fd else 2e-6)
+    assert rel_l2(Gg - G0, Go - G0) <= (1e-2 if fd else 2e-5)
+    assert rel_l2(Sg - S0, So - S0) <= (1e-2 if fd else 2e-5)
 
 
 def test_classic_and_transposed_differ():
