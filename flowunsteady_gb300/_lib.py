@@ -62,6 +62,7 @@ EXPORTS = [
     "vpm_uj_device_async", "vpm_uj_device_noalloc", "vpm_batch_create", "vpm_batch_destroy",
     "vpm_batch_last_error", "vpm_batch_set_stream", "vpm_batch_set_field",
     "vpm_batch_get_field", "vpm_batch_eval_UJ", "vpm_batch_get_UJ", "vpm_batch_step",
+    "vpm_batch_autotune", "vpm_batch_get_shapes",
     "vpm_autotune", "vpm_set_tile", "vpm_set_particle_order", "vpm_batch_set_particle_order",
     "vpm_measure_fma_peaks", "vpm_debug_fail_after", "vpm_debug_last_plan",
     "vpm_get_launch_count", "vpm_build_info",
@@ -176,6 +177,8 @@ def _declare(lib):
         "vpm_batch_eval_UJ": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
         "vpm_batch_get_UJ": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _i64, _dp, _i64]),
         "vpm_batch_step": (ctypes.c_int, [_vp, ctypes.c_double, P(Scheme), _i64, ctypes.c_int]),
+        "vpm_batch_autotune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+        "vpm_batch_get_shapes": (ctypes.c_int, [_vp, P(ctypes.c_int32), P(ctypes.c_int32)]),
         "vpm_autotune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Tile), _dp]),
         "vpm_set_tile": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, P(Tile)]),
         "vpm_set_particle_order": (ctypes.c_int, [_vp, ctypes.c_int]),

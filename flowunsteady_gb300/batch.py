@@ -73,5 +73,19 @@ class FieldBatch:
         self._check(L.lib().vpm_batch_step(self._b, float(dt), ctypes.byref(scheme), int(nsteps),
                                            1 if use_graph else 0))
 
+    def autotune(self, kernel: int, precision: int) -> float:
+        """Tile shape per size bucket (vpm_batch_autotune); returns the tuned
+        batch's U/J pass time in ms."""
+        ms = ctypes.c_double()
+        self._check(L.lib().vpm_batch_autotune(self._b, kernel, precision, ctypes.byref(ms)))
+        return ms.value
+
+    def shapes(self):
+        """(block, targets per thread) of every field in the current plan."""
+        nf = len(self.sizes)
+        blk, tpt = (ctypes.c_int32 * nf)(), (ctypes.c_int32 * nf)()
+        self._check(L.lib().vpm_batch_get_shapes(self._b, blk, tpt))
+        return list(zip(list(blk), list(tpt)))
+
     def set_stream(self, stream_handle: int):
         self._check(L.lib().vpm_batch_set_stream(self._b, ctypes.c_void_p(stream_handle)))

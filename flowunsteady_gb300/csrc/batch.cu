@@ -40,81 +40,121 @@ int from_ctx(vpm_batch* b, int rc) {
 
 }  // namespace
 
-// Build the work queue for a kernel/precision: the tile shape is the one the
-// autotuner (or the default) gives the size bucket that carries most of the
-// pair work; the source chunk length L is the smallest multiple of the block
-// that keeps the queue near four items per resident CTA.
-int batch_plan(vpm_ctx* c, int kernel, int precision) {
+// Items of the fields in `fields`, each field with its tile shape `shape[f]`,
+// grouped by shape: within a group the source chunk length L is the smallest
+// multiple of the block that keeps the group's queue near four items per
+// resident CTA, and items are sorted by cost (largest first).  Writes the
+// device queue, per-field chunk counts and groups into bp.
+static int build_queue(vpm_ctx* c, int kernel, int precision, const std::vector<int>& fields,
+                       const std::vector<Shape>& shape) {
   BatchPlan* bp = c->bp;
   const int nf = bp->nfields;
-  int64_t dom_n = 1;
-  double dom_w = -1.0;
-  for (int f = 0; f < nf; ++f) {
-    const double w = double(bp->h_n[f]) * double(bp->h_n[f]);
-    if (w > dom_w) {
-      dom_w = w;
-      dom_n = std::max<int64_t>(bp->h_n[f], 1);
-    }
+  std::vector<Shape> shapes;
+  for (int f : fields) {
+    bool seen = false;
+    for (const Shape& s : shapes) seen = seen || (s.block == shape[f].block && s.tpt == shape[f].tpt);
+    if (!seen) shapes.push_back(shape[f]);
   }
-  const Shape sh = lookup_shape(c->device, PASS_UJ, kernel, precision, dom_n,
-                                &c->pinned[PASS_UJ][kernel][precision]);
-  const int r_uj = resident_ctas(c->device, PASS_UJ, kernel, precision, sh, c->num_sms);
-  const int r_z = resident_ctas(c->device, PASS_ZETA, kernel, precision, sh, c->num_sms);
-  const int64_t TB = int64_t(sh.block) * sh.tpt;
-  auto count_items = [&](int64_t L) {
-    int64_t items = 0;
-    for (int f = 0; f < nf; ++f) {
-      const int64_t n = bp->h_n[f];
-      if (n == 0) continue;
-      items += ceil_div(n, TB) * ceil_div(n, L);
-    }
-    return items;
-  };
-  int64_t nmax = 1;
-  for (int f = 0; f < nf; ++f) nmax = std::max(nmax, bp->h_n[f]);
-  int64_t L = round_up(nmax, sh.block);
-  for (int64_t cand = 2 * sh.block; cand < round_up(nmax, sh.block); cand *= 2) {
-    if (count_items(cand) <= 4 * int64_t(r_uj)) {
-      L = cand;
-      break;
-    }
-  }
+  if (int(shapes.size()) > kMaxBatchGroups)
+    return set_error(&c->err, VPM_ERR_UNSUPPORTED, "too many tile shapes in one batch");
   std::vector<PairItem> items;
   std::vector<int32_t> fchunks(nf, 1);
+  std::vector<BatchGroup> groups;
   int max_chunks = 1;
-  for (int f = 0; f < nf; ++f) {
-    const int64_t n = bp->h_n[f], off = bp->h_off[f];
-    if (n == 0) continue;
-    const int64_t cf = ceil_div(n, L);
-    fchunks[f] = int32_t(cf);
-    max_chunks = std::max<int>(max_chunks, int(cf));
-    for (int64_t t = 0; t < n; t += TB)
-      for (int64_t ch = 0; ch < cf; ++ch) {
-        PairItem it;
-        it.t0 = off + t;
-        it.t1 = off + std::min(n, t + TB);
-        it.s0 = off + ch * L;
-        it.s1 = off + std::min(n, (ch + 1) * L);
-        it.slot = cf > 1 ? int32_t(ch) : -1;
-        it.field = f;
-        items.push_back(it);
+  for (const Shape& sh : shapes) {
+    const int r_uj = resident_ctas(c->device, PASS_UJ, kernel, precision, sh, c->num_sms);
+    const int r_z = resident_ctas(c->device, PASS_ZETA, kernel, precision, sh, c->num_sms);
+    const int64_t TB = int64_t(sh.block) * sh.tpt;
+    std::vector<int> mine;
+    int64_t nmax = 1;
+    for (int f : fields)
+      if (shape[f].block == sh.block && shape[f].tpt == sh.tpt && bp->h_n[f] > 0) {
+        mine.push_back(f);
+        nmax = std::max(nmax, bp->h_n[f]);
       }
+    auto count_items = [&](int64_t L) {
+      int64_t cnt = 0;
+      for (int f : mine) cnt += ceil_div(bp->h_n[f], TB) * ceil_div(bp->h_n[f], L);
+      return cnt;
+    };
+    int64_t L = round_up(nmax, sh.block);
+    for (int64_t cand = 2 * sh.block; cand < round_up(nmax, sh.block); cand *= 2) {
+      if (count_items(cand) <= 4 * int64_t(r_uj)) {
+        L = cand;
+        break;
+      }
+    }
+    BatchGroup g;
+    g.shape = sh;
+    g.first = int(items.size());
+    g.resident = std::min(r_uj, r_z);
+    for (int f : mine) {
+      const int64_t n = bp->h_n[f], off = bp->h_off[f];
+      const int64_t cf = ceil_div(n, L);
+      fchunks[f] = int32_t(cf);
+      max_chunks = std::max<int>(max_chunks, int(cf));
+      for (int64_t t = 0; t < n; t += TB)
+        for (int64_t ch = 0; ch < cf; ++ch) {
+          PairItem it;
+          it.t0 = off + t;
+          it.t1 = off + std::min(n, t + TB);
+          it.s0 = off + ch * L;
+          it.s1 = off + std::min(n, (ch + 1) * L);
+          it.slot = cf > 1 ? int32_t(ch) : -1;
+          it.field = f;
+          items.push_back(it);
+        }
+    }
+    std::stable_sort(items.begin() + g.first, items.end(), [](const PairItem& a, const PairItem& b) {
+      return (a.t1 - a.t0) * (a.s1 - a.s0) > (b.t1 - b.t0) * (b.s1 - b.s0);
+    });
+    g.n_items = int(items.size()) - g.first;
+    if (g.n_items > 0) groups.push_back(g);
   }
-  std::stable_sort(items.begin(), items.end(), [](const PairItem& a, const PairItem& b) {
-    return (a.t1 - a.t0) * (a.s1 - a.s0) > (b.t1 - b.t0) * (b.s1 - b.s0);
-  });
+  // The group with the most pair work launches first.
+  auto work = [&](const BatchGroup& g) {
+    double w = 0.0;
+    for (int i = g.first; i < g.first + g.n_items; ++i)
+      w += double(items[i].t1 - items[i].t0) * double(items[i].s1 - items[i].s0);
+    return w;
+  };
+  std::stable_sort(groups.begin(), groups.end(),
+                   [&](const BatchGroup& a, const BatchGroup& b) { return work(a) > work(b); });
   cudaFree(bp->d_items);
   bp->d_items = nullptr;
   if (!items.empty()) {
     if (cudaMalloc(&bp->d_items, items.size() * sizeof(PairItem)) != cudaSuccess)
       return set_error(&c->err, VPM_ERR_NOMEM, "cannot allocate the batch work queue");
-    cudaMemcpy(bp->d_items, items.data(), items.size() * sizeof(PairItem), cudaMemcpyHostToDevice);
+    if (cudaMemcpy(bp->d_items, items.data(), items.size() * sizeof(PairItem),
+                   cudaMemcpyHostToDevice) != cudaSuccess)
+      return set_error(&c->err, VPM_ERR_CUDA, "cannot upload the batch work queue");
   }
-  cudaMemcpy(bp->d_fchunks, fchunks.data(), nf * sizeof(int32_t), cudaMemcpyHostToDevice);
-  bp->shape = sh;
+  if (cudaMemcpy(bp->d_fchunks, fchunks.data(), nf * sizeof(int32_t), cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return set_error(&c->err, VPM_ERR_CUDA, "cannot upload the batch chunk counts");
+  bp->groups = groups;
   bp->n_items = int(items.size());
   bp->max_chunks = max_chunks;
-  bp->resident = std::min(r_uj, r_z);
+  bp->h_shape = shape;
+  return VPM_OK;
+}
+
+// Build the work queue for a kernel/precision: every field takes the tile
+// shape of its size bucket (the autotuner's choice, or the default), so a
+// batch makes one persistent launch per distinct shape.
+int batch_plan(vpm_ctx* c, int kernel, int precision) {
+  BatchPlan* bp = c->bp;
+  const int nf = bp->nfields;
+  std::vector<int> fields(nf);
+  std::vector<Shape> shape(nf);
+  for (int f = 0; f < nf; ++f) {
+    fields[f] = f;
+    shape[f] = lookup_shape(c->device, PASS_UJ, kernel, precision,
+                            std::max<int64_t>(bp->h_n[f], 1),
+                            &c->pinned[PASS_UJ][kernel][precision]);
+  }
+  const int rc = build_queue(c, kernel, precision, fields, shape);
+  if (rc != VPM_OK) return rc;
   bp->kernel = kernel;
   bp->precision = precision;
   return VPM_OK;
@@ -151,7 +191,7 @@ int vpm_batch_create(int device, int nfields, const int64_t* n, vpm_batch** out)
   cudaSetDevice(device);
   cudaError_t e = cudaMalloc(&bp.d_foff, nfields * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&bp.d_fchunks, nfields * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&bp.d_counter, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&bp.d_counter, kMaxBatchGroups * sizeof(unsigned int));
   if (e == cudaSuccess)
     e = cudaMemcpy(bp.d_foff, bp.h_off.data(), nfields * sizeof(int64_t), cudaMemcpyHostToDevice);
   cudaSetDevice(prev);
@@ -257,6 +297,100 @@ int vpm_batch_get_UJ(vpm_batch* b, int f, double* U, int64_t su, double* J, int6
   if (!b) return set_error(nullptr, VPM_ERR_INVALID, "null batch");
   if (f < 0 || f >= b->plan.nfields) return bfail(b, VPM_ERR_INVALID, "no such field");
   return from_ctx(b, vpm_get_UJ(b->ctx, b->plan.h_off[f], b->plan.h_n[f], U, su, J, sj));
+}
+
+int vpm_batch_autotune(vpm_batch* b, int kernel, int precision, double* ms) {
+  if (!b) return set_error(nullptr, VPM_ERR_INVALID, "null batch");
+  int rc = all_set(b);
+  if (rc) return rc;
+  if (kernel != VPM_KERNEL_WINCKELMANS && kernel != VPM_KERNEL_GAUSSIANERF)
+    return bfail(b, VPM_ERR_INVALID, "unknown kernel");
+  if (precision != VPM_PREC_FP64 && precision != VPM_PREC_FP32 && precision != VPM_PREC_FP32C)
+    return bfail(b, VPM_ERR_INVALID, "unknown precision");
+  vpm_ctx* c = b->ctx;
+  BatchPlan& bp = b->plan;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(c->device);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  // The U/J pass of the current queue, timed on the batch's stream (one
+  // untimed pass first).
+  auto time_queue = [&](float* t) -> int {
+    bp.kernel = kernel;
+    bp.precision = precision;
+    int r = ctx_prepare_scratch(c, kernel, precision);
+    if (r) return r;
+    cudaError_t x = ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J);
+    if (x == cudaSuccess) x = cudaEventRecord(e0, c->st);
+    if (x == cudaSuccess) x = ctx_pair(c, PASS_UJ, kernel, precision, 0, c->n, 1.0, nullptr, c->U, c->J);
+    if (x == cudaSuccess) x = cudaEventRecord(e1, c->st);
+    if (x == cudaSuccess) x = cudaEventSynchronize(e1);
+    if (x == cudaSuccess) x = cudaEventElapsedTime(t, e0, e1);
+    return x == cudaSuccess ? VPM_OK
+                            : set_error(&c->err, VPM_ERR_CUDA,
+                                        std::string("batch autotune: ") + cudaGetErrorString(x));
+  };
+  // Fields by size bucket; each bucket's fields alone are timed with every
+  // compiled shape as one persistent queue, and the fastest shape is stored
+  // for that bucket.
+  std::vector<std::pair<int, std::vector<int>>> buckets;
+  for (int f = 0; f < bp.nfields; ++f) {
+    if (bp.h_n[f] == 0) continue;
+    const int bk = shape_bucket(bp.h_n[f]);
+    auto it = std::find_if(buckets.begin(), buckets.end(),
+                           [&](const std::pair<int, std::vector<int>>& p) { return p.first == bk; });
+    if (it == buckets.end()) buckets.push_back({bk, {f}});
+    else it->second.push_back(f);
+  }
+  static const Shape cands[] = {{128, 2}, {128, 4}, {256, 2}, {128, 1}};
+  std::vector<Shape> shape(bp.nfields, Shape{128, 2});
+  for (size_t q = 0; q < buckets.size() && e == cudaSuccess && rc == VPM_OK; ++q) {
+    const std::vector<int>& fs = buckets[q].second;
+    Shape best{0, 0};
+    float best_ms = 1e30f;
+    for (const Shape& s : cands) {
+      if (!pair_shape_supported(precision, s)) continue;
+      for (int f : fs) shape[f] = s;
+      rc = build_queue(c, kernel, precision, fs, shape);
+      float t = 0.f;
+      if (rc == VPM_OK) rc = time_queue(&t);
+      if (rc != VPM_OK) break;
+      if (t < best_ms) {
+        best_ms = t;
+        best = s;
+      }
+    }
+    if (rc == VPM_OK && best.block > 0)
+      store_shape(c->device, PASS_UJ, kernel, precision, bp.h_n[fs.front()], best);
+  }
+  float t = 0.f;
+  if (rc == VPM_OK && e == cudaSuccess) {
+    rc = batch_plan(c, kernel, precision);
+    if (rc == VPM_OK) rc = time_queue(&t);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  c->uj_lo = c->uj_hi = 0;   // U/J hold timing runs
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return bfail(b, VPM_ERR_CUDA, std::string("batch autotune: ") + cudaGetErrorString(e));
+  if (rc != VPM_OK) return from_ctx(b, rc);
+  if (ms) *ms = t;
+  return VPM_OK;
+}
+
+int vpm_batch_get_shapes(vpm_batch* b, int32_t* block, int32_t* tpt) {
+  if (!b) return set_error(nullptr, VPM_ERR_INVALID, "null batch");
+  if (b->plan.h_shape.size() != size_t(b->plan.nfields))
+    return bfail(b, VPM_ERR_STATE, "no work plan yet (evaluate or step first)");
+  for (int f = 0; f < b->plan.nfields; ++f) {
+    if (block) block[f] = b->plan.h_shape[f].block;
+    if (tpt) tpt[f] = b->plan.h_shape[f].tpt;
+  }
+  return VPM_OK;
 }
 
 int vpm_batch_step(vpm_batch* b, double dt, const vpm_scheme* s, int64_t nsteps, int use_graph) {

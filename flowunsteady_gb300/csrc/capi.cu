@@ -66,6 +66,8 @@ Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n,
   return default_shape(pass, precision, n);
 }
 
+int shape_bucket(int64_t n) { return size_bucket(n); }
+
 void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune[std::make_tuple(device, pass, kernel, precision, size_bucket(n))] = s;
@@ -130,8 +132,7 @@ int active_clusters(int device, int pass, int kernel, int precision, Shape s, in
 int cluster_mode() {
   static const int mode = [] {
     const char* v = std::getenv("VPM_CLUSTER");
-    if (!v || !v[0]) return -1;
-    return v[0] == '0' ? 0 : 1;
+    return (v && v[0] && v[0] != '0') ? 1 : 0;
   }();
   return mode;
 }
@@ -142,6 +143,11 @@ constexpr int kMaxCluster = 16;
 // Split-source clusters for an FP32C pass of n_tb target tiles over ns
 // sources: the cluster size (1 = none fits) whose clusters fill whole waves
 // best, with its chunk length and wave efficiency score (as plan_chunks').
+// Measured on GB300 against partial slots (helical wake, Gaussian-erf, CUDA
+// events): 7,600 particles 0.206 against 0.177 ms, 65,536 5.64 against 5.17 ms,
+// 262,144 76.8 against 73.5 ms, although the clusters write no partial sums
+// (DRAM writes of the pass: 0 against 50 MB at 131,072).  So partial slots are
+// the default and clusters are taken only with VPM_CLUSTER=1.
 static int plan_cluster(int device, const PairCall& pc, Shape sh, int64_t n_tb,
                         int64_t* chunk_out, double* score_out) {
   int best_nc = 1;
@@ -166,9 +172,8 @@ static int plan_cluster(int device, const PairCall& pc, Shape sh, int64_t n_tb,
 
 // Plan and enqueue one pair pass.  `need_part` (elements) is raised to what
 // the launch needs; when dry, nothing is launched.  A split source range goes
-// either through partial slots summed by a reduction launch, or (FP32C,
-// single field) through clusters that sum on chip: clusters are taken when
-// they fill the waves within 2 % as well as the slot plan.
+// through partial slots summed by a reduction launch, or (FP32C, single field,
+// VPM_CLUSTER=1) through thread-block clusters that sum on chip.
 cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* pinned,
                      double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
                      cudaStream_t st, PairPlan* plan_out) {
@@ -181,14 +186,11 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   int64_t chunk = 0;
   int n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, 0);
   int cluster = 1;
-  if (pc.prec == VPM_PREC_FP32C && n_chunk > 1 && cluster_mode() != 0) {
-    const int64_t items = n_tb * n_chunk;
-    const int64_t waves = ceil_div(items, resident);
-    const double slot_score = double(items) / double(waves * resident) - 0.003 * n_chunk;
+  if (pc.prec == VPM_PREC_FP32C && n_chunk > 1 && cluster_mode() == 1) {
     int64_t cchunk = 0;
     double cscore = -1.0;
     const int nc = plan_cluster(device, pc, sh, n_tb, &cchunk, &cscore);
-    if (nc > 1 && (cluster_mode() == 1 || cscore >= slot_score - 0.02)) {
+    if (nc > 1) {
       cluster = nc;
       n_chunk = nc;
       chunk = cchunk;
@@ -592,7 +594,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
       uo = c->sout; jo = j ? c->sout + 3 * ld : nullptr; djo = dj ? c->sout + 12 * ld : nullptr;
     }
     unsigned int* coh = !srt && coherence_counted(c->n) ? c->coh : nullptr;
-    e = cudaMemsetAsync(bp->d_counter, 0, sizeof(unsigned int), c->st);
+    e = cudaMemsetAsync(bp->d_counter, 0, kMaxBatchGroups * sizeof(unsigned int), c->st);
     if (e != cudaSuccess) return e;
     PairArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -600,7 +602,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     a.xt = xs; a.ldt = ld;
     a.sigma_scale = scale;
     a.dj = djo;
-    a.items = bp->d_items; a.n_items = bp->n_items; a.counter = bp->d_counter;
+    a.items = bp->d_items; a.n_items = bp->n_items;
     a.u = uo; a.j = jo; a.ldo = ld;
     a.part = c->part; a.ldp = ld;
     a.far = farfield_enabled() ? 1 : 0;
@@ -613,9 +615,18 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
       a.rec = c->rec;
       a.tma = tma_disabled() ? 0 : 1;
     }
-    e = launch_pair(pass, kernel, prec, bp->shape, a, std::min(bp->resident, bp->n_items), c->st);
-    if (e != cudaSuccess) return e;
-    c->launches += 1;
+    // One persistent launch per tile-shape group, each over its own queue.
+    for (size_t g = 0; g < bp->groups.size(); ++g) {
+      const BatchGroup& grp = bp->groups[g];
+      PairArgs ag = a;
+      ag.items = bp->d_items + grp.first;
+      ag.n_items = grp.n_items;
+      ag.counter = bp->d_counter + g;
+      e = launch_pair(pass, kernel, prec, grp.shape, ag, std::min(grp.resident, grp.n_items),
+                      c->st);
+      if (e != cudaSuccess) return e;
+      c->launches += 1;
+    }
     if (bp->max_chunks > 1) {
       e = launch_reduce(pass, kernel, c->part, ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
                         0, c->n, uo, jo, djo, ld, c->st);

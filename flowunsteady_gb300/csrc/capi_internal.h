@@ -51,14 +51,15 @@ struct PairPlan {
 // Plan of the last stateless U/J call (vpm_uj_device_async/_noalloc) on this
 // host thread, for vpm_debug_last_plan.
 extern thread_local PairPlan g_last_stateless_plan;
-// Split-source clusters: -1 (VPM_CLUSTER unset) lets the planner choose, 0
-// (VPM_CLUSTER=0) always uses partial slots, 1 (VPM_CLUSTER=1) takes clusters
-// whenever a cluster size fits.
+// Split-source clusters: 0 (default) sums split source ranges through partial
+// slots; 1 (VPM_CLUSTER=1) takes clusters whenever a cluster size fits.
 int cluster_mode();
 
 Shape default_shape(int pass, int precision, int64_t n);
 Shape lookup_shape(int device, int pass, int kernel, int precision, int64_t n, const Shape* pinned);
 void store_shape(int device, int pass, int kernel, int precision, int64_t n, Shape s);
+// Size bucket (floor log2 n) under which tuned shapes are stored.
+int shape_bucket(int64_t n);
 int resident_ctas(int device, int pass, int kernel, int precision, Shape s, int num_sms);
 int plan_chunks(int64_t n_tb, int64_t ns, int block, int resident, int64_t* chunk_out,
                 int max_chunks = 0);
@@ -87,19 +88,27 @@ struct GraphEntry {
   int64_t kernels;   // kernel nodes of one replay
 };
 
-// Flattened work queue of a batch of independent fields (see batch.cu).
-struct BatchPlan {
+// Flattened work queue of a batch of independent fields (see batch.cu): one
+// group of items per tile shape, each group one persistent launch.
+constexpr int kMaxBatchGroups = 4;
+struct BatchGroup {
   Shape shape;
+  int first = 0;        // items [first, first + n_items) of d_items
+  int n_items = 0;
+  int resident = 1;     // persistent grid of the group's launch
+};
+struct BatchPlan {
+  std::vector<BatchGroup> groups;
   PairItem* d_items = nullptr;
   int n_items = 0;
   int64_t* d_foff = nullptr;
   int32_t* d_fchunks = nullptr;
   int nfields = 0;
   int max_chunks = 1;
-  unsigned int* d_counter = nullptr;
-  int resident = 1;
+  unsigned int* d_counter = nullptr;   // one queue counter per group
   int kernel = -1, precision = -1;   // plan built for this pair
   std::vector<int64_t> h_off, h_n;   // field offsets and sizes
+  std::vector<Shape> h_shape;        // tile shape of each field in the current plan
 };
 
 }  // namespace vpm

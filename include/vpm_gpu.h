@@ -382,6 +382,18 @@ int vpm_batch_get_UJ(vpm_batch* b, int field, double* U, int64_t stride_u, doubl
                      int64_t stride_j);
 int vpm_batch_step(vpm_batch* b, double dt, const vpm_scheme* s, int64_t nsteps, int use_graph);
 
+/* Tile shapes of a batch by size bucket (log2 N): every field takes the shape
+ * stored for its bucket in the per-device table (see vpm_autotune), and the
+ * fields of one shape form one persistent launch per pair pass (the default,
+ * before tuning: every bucket below 196,608 particles takes 128x2).
+ * vpm_batch_autotune times, for each bucket present, that bucket's fields
+ * alone as one persistent U/J launch with every compiled shape, stores the
+ * fastest for the bucket, rebuilds the batch's work queue and returns the time
+ * of one U/J pass of the whole batch (ms).  vpm_batch_get_shapes reads the
+ * shape of each field (arrays of nfields). */
+int vpm_batch_autotune(vpm_batch* b, int kernel, int precision, double* ms);
+int vpm_batch_get_shapes(vpm_batch* b, int32_t* block, int32_t* tpt);
+
 /* ----------------------------------------------------------- utilities -- */
 /* Tile shape of the pair kernels: block size, targets per thread and source
  * chunk length.  vpm_autotune times every compiled shape of the U/J pass and,

@@ -525,22 +525,38 @@ int orc_diagnostics(int kernel, int64_t n, int64_t n_static, const double* X, co
   }
   out[VPM_DIAG_ENSTROPHY] = 0.5 * ens;
   out[VPM_DIAG_SIGMA_MEAN] = n > 0 ? out[VPM_DIAG_SIGMA_MEAN] / n : 0.0;
+  // C_d statistics over the free particles with C_d != 0 (vpm.monitor_Cd's
+  // record, src/FLOWUnsteady_monitors.jl:697-703): mean, standard deviation,
+  // skewness and excess kurtosis as population moments about the mean (two
+  // passes), minimum and maximum; the zero ratio over all free particles.
   const int64_t nf = n - n_static;
-  double s1 = 0, s2 = 0, mn = 0, mx = 0;
+  double s1 = 0, mn = 0, mx = 0;
   int64_t nz = 0, cnt = 0;
   for (int64_t p = 0; p < nf && C; ++p) {
     double c = C[3 * p];
     if (c == 0.0) { ++nz; continue; }
     if (cnt == 0) { mn = mx = c; }
     mn = std::min(mn, c); mx = std::max(mx, c);
-    s1 += c; s2 += c * c; ++cnt;
+    s1 += c; ++cnt;
   }
   if (cnt > 0) {
-    double mean = s1 / cnt;
+    const double mean = s1 / cnt;
+    double m2 = 0, m3 = 0, m4 = 0;
+    for (int64_t p = 0; p < nf; ++p) {
+      const double c = C[3 * p];
+      if (c == 0.0) continue;
+      const double d = c - mean, d2 = d * d;
+      m2 += d2; m3 += d2 * d; m4 += d2 * d2;
+    }
+    m2 /= cnt; m3 /= cnt; m4 /= cnt;
     out[VPM_DIAG_CD_MEAN] = mean;
-    out[VPM_DIAG_CD_STD] = std::sqrt(std::max(0.0, s2 / cnt - mean * mean));
+    out[VPM_DIAG_CD_STD] = std::sqrt(m2);
     out[VPM_DIAG_CD_MIN] = mn;
     out[VPM_DIAG_CD_MAX] = mx;
+    if (m2 > 0.0) {
+      out[VPM_DIAG_CD_SKEW] = m3 / (m2 * std::sqrt(m2));
+      out[VPM_DIAG_CD_KURT] = m4 / (m2 * m2) - 3.0;
+    }
   }
   out[VPM_DIAG_CD_ZERO_RATIO] = nf > 0 && C ? double(nz) / double(nf) : 0.0;
   return 0;

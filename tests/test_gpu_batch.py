@@ -97,3 +97,51 @@ def test_batch_particle_order_changes_only_the_summation_order():
             continue
         (Ua, Ja), (Uc, Jc) = res[L.ORDER_AUTO][f], res[L.ORDER_CALLER][f]
         assert rel_l2(Ua, Uc) <= 1e-6 and rel_l2(Ja, Jc) <= 1e-6, f
+
+
+def test_batch_fields_of_different_shapes_run_as_separate_launches(oracle):
+    # A field of 200,000 particles takes the 128x4 shape (the default from
+    # 196,608 particles on), the small ones 128x2 (or what the per-device table
+    # holds for their size bucket): one persistent launch per shape.  Every
+    # field still matches the oracle.
+    sizes = [3000, 200000, 5000, 700]
+    fs = []
+    for f, n in enumerate(sizes):
+        X, G, S = uniform_box(n, seed_index=110 + f)
+        fs.append((X, G * 100, S * 2))
+    b = FieldBatch(sizes)
+    for f, (X, G, S) in enumerate(fs):
+        b.set_field(f, X, G, S)
+    b.eval_UJ(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    shapes = b.shapes()
+    assert shapes[1] == (128, 4) and len(set(shapes)) >= 2
+    rng = np.random.default_rng(111)
+    for f, (X, G, S) in enumerate(fs):
+        U, J = b.get_UJ(f)
+        idx = rng.choice(X.shape[0], min(400, X.shape[0]), replace=False)
+        U0, J0 = oracle.uj_direct(1, X, G, S, Xt=X[idx])
+        assert rel_l2(U[idx], U0) <= 1e-5 and rel_l2(J[idx], J0) <= 1e-5, f
+    b.close()
+
+
+def test_batch_autotune_per_size_bucket(oracle):
+    sizes = [2048, 2500, 9000, 12000, 40000]
+    fs = []
+    for f, n in enumerate(sizes):
+        X, G, S = uniform_box(n, seed_index=120 + f)
+        fs.append((X, G * 100, S * 2))
+    b = FieldBatch(sizes)
+    for f, (X, G, S) in enumerate(fs):
+        b.set_field(f, X, G, S)
+    ms = b.autotune(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    assert ms > 0
+    shapes = b.shapes()
+    assert all(s in {(128, 2), (128, 4), (256, 2)} for s in shapes)
+    assert shapes[0] == shapes[1] and shapes[2] == shapes[3]   # same size bucket, same shape
+    b.eval_UJ(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+    for f, (X, G, S) in enumerate(fs):
+        U, J = b.get_UJ(f)
+        idx = np.random.default_rng(f).choice(X.shape[0], 300, replace=False)
+        U0, J0 = oracle.uj_direct(1, X, G, S, Xt=X[idx])
+        assert rel_l2(U[idx], U0) <= 1e-5 and rel_l2(J[idx], J0) <= 1e-5, f
+    b.close()

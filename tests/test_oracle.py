@@ -193,3 +193,22 @@ def test_free_vortex_force_matches_numpy(oracle, k):
     M = oracle.ffv_direct(k, Xb, Gb, Sb, Xf, Gf)
     M2 = P.ffv(k, Xb, Gb, Sb, Xf, Gf)
     assert rel_max(M, M2) < 1e-12
+
+
+def test_cd_statistics_follow_monitor_cd(oracle):
+    # vpm.monitor_Cd's record (src/FLOWUnsteady_monitors.jl:697-703): over the
+    # free particles with C_d != 0, mean, std, skewness, excess kurtosis,
+    # min, max; the zero ratio over all free particles.
+    from flowunsteady_gb300.workloads import uniform_box
+    X, G, S = uniform_box(500, seed_index=30)
+    rng = np.random.default_rng(31)
+    C = np.zeros((500, 3))
+    C[:, 0] = np.where(rng.random(500) < 0.3, 0.0, rng.normal(0.1, 0.05, 500))
+    d = oracle.diagnostics(1, X, G, S * 3, C, n_static=20)
+    c = C[:480, 0]
+    nz = c[c != 0]
+    m = nz.mean()
+    m2, m3, m4 = (((nz - m) ** k).mean() for k in (2, 3, 4))
+    assert abs(d[7] - m) <= 1e-14 and abs(d[8] - np.sqrt(m2)) <= 1e-14
+    assert abs(d[14] - m3 / m2**1.5) <= 1e-12 and abs(d[15] - (m4 / m2**2 - 3)) <= 1e-12
+    assert d[9] == (c == 0).mean() and d[10] == nz.min() and d[11] == nz.max()
