@@ -210,7 +210,9 @@ def run_batch(args):
             b.set_field(f, X, G, S)
 
     load()
+    tuned_ms = b.autotune(k, L.PREC_FP32C) if args.autotune else None
     b.eval_UJ(k, L.PREC_FP32C)
+    shapes = sorted({f"{bl}x{tp}" for bl, tp in b.shapes()})
     (_, t_uj) = timed(lambda: b.eval_UJ(k, L.PREC_FP32C))
     uj = [b.get_UJ(f) for f in range(len(sizes))]
     b.step(0.005, sc, 1)                       # capture + warm-up
@@ -221,6 +223,7 @@ def run_batch(args):
     pairs_step = sum(n * n for n in sizes)
     res = {"workload": f"{len(sizes)} fields, N in [{min(sizes)}, {max(sizes)}]",
            "sizes": sizes, "sum_n": sum(sizes), "sum_n2": pairs_step, "steps": nsteps,
+           "tile_shapes": shapes, "autotuned": bool(args.autotune), "autotune_uj_ms": tuned_ms,
            "batch_uj_seconds": t_uj, "batch_uj_pairs_per_s": pairs_step / t_uj,
            "batch_seconds": t_batch, "batch_steps_per_s": nsteps / t_batch,
            # dynamic SFS: stage 1 runs U/J and ζ at σ and ασ, stages 2-3 once: 4 U/J passes
@@ -429,7 +432,8 @@ def main(argv=None):
     p.add_argument("--dt", type=float, default=None)
     p.add_argument("--keep", action="store_true", help="include the final state (rings)")
     p.add_argument("--no-reference", action="store_true", help="batch: skip the FP64 fields")
-    p.add_argument("--autotune", action="store_true", help="step: tune the tile shapes first")
+    p.add_argument("--autotune", action="store_true",
+                   help="step, batch: tune the tile shapes first (per size bucket for a batch)")
     p.add_argument("--tree", action="store_true", help="step: U/J passes by the treecode")
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
