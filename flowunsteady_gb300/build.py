@@ -37,7 +37,10 @@ def elf_matches_host(path: str) -> bool:
     return want is None or int.from_bytes(head[18:20], "little") == want
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# Host loops over particles (validation, AoS <-> SoA staging) use OpenMP.
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-fopenmp"]
+LINK_FLAGS = ["-Xcompiler", "-fopenmp"]
 
 
 def nvcc() -> str:
@@ -85,7 +88,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     newest = max(os.path.getmtime(o) for o in objs)
     if (force or not os.path.exists(LIB) or not elf_matches_host(LIB)
             or os.path.getmtime(LIB) < newest):
-        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + LINK_FLAGS
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

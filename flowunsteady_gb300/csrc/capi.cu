@@ -328,6 +328,10 @@ int ensure_test_filter(vpm_ctx* c) {
   return VPM_OK;
 }
 
+// The host-side loops over particles (validation, AoS <-> SoA staging) run on
+// all host threads from this many particles on.
+constexpr int64_t kHostParallelMin = 16384;
+
 // Host strided AoS -> pinned SoA staging -> device rows [i0, i0+n).  New
 // particles get volume 0, circulation 1, empty SFS memory and the static flag
 // is_static.
@@ -337,6 +341,7 @@ int upload(vpm_ctx* c, int64_t i0, int64_t n, const double* X, int64_t sx, const
   int rc = ensure_stage(c, size_t(9) * n);
   if (rc) return rc;
   double* h = c->h_stage;
+#pragma omp parallel for schedule(static) if (n >= kHostParallelMin)
   for (int64_t i = 0; i < n; ++i) {
     for (int k = 0; k < 3; ++k) {
       h[k * n + i] = X[i * sx + k];
@@ -386,6 +391,17 @@ int validate_host(vpm_ctx* c, int64_t n, const double* X, int64_t sx, const doub
   if (n == 0) return VPM_OK;
   if (!X || !G || !S) return ctx_fail(c, VPM_ERR_INVALID, "null particle array");
   if (sx < 3 || sg < 3 || ss < 1) return ctx_fail(c, VPM_ERR_INVALID, "stride too small");
+  // A parallel scan for any bad value; only then the ordered scan below names
+  // the first one.
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad) if (n >= kHostParallelMin)
+  for (int64_t i = 0; i < n; ++i) {
+    const double s = S[i * ss];
+    bool ok = std::isfinite(s) && s > 0.0;
+    for (int k = 0; k < 3; ++k) ok = ok && std::isfinite(X[i * sx + k]) && std::isfinite(G[i * sg + k]);
+    bad |= ok ? 0 : 1;
+  }
+  if (!bad) return VPM_OK;
   for (int64_t i = 0; i < n; ++i) {
     const double s = S[i * ss];
     for (int k = 0; k < 3; ++k)
@@ -409,6 +425,7 @@ int download_rows(vpm_ctx* c, const double* dev, int rows, int64_t i0, int64_t n
   CTX_CK(c, cudaMemcpy2DAsync(c->h_stage, w, dev + i0, sp, w, rows, cudaMemcpyDeviceToHost, c->st));
   CTX_CK(c, cudaStreamSynchronize(c->st));
   const double* h = c->h_stage;
+#pragma omp parallel for schedule(static) if (n >= kHostParallelMin)
   for (int64_t i = 0; i < n; ++i)
     for (int k = 0; k < rows; ++k) out[i * stride + k] = h[k * n + i];
   return VPM_OK;
