@@ -658,31 +658,59 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   }
 }
 
+// Fixed-order sum of the partial slots.  A block holds 32 targets (x) and
+// kReduceRows value rows (y): thread (x, y) sums rows y, y + kReduceRows, ...
+// of its target over the chunks in chunk order, four loads in flight (the same
+// FP64 additions in the same order as one thread per target walking every
+// row, so the result is bitwise that one), and one warp then forms the final
+// values from shared memory.  A target per thread alone left most SMs idle at
+// small N (30 blocks at N = 7,600) with one dependent chain per thread.
+constexpr int kReduceRows = 8;
+
 template <int PASS, int KERNEL>
-__global__ void reduce_kernel(const double* __restrict__ part, int64_t ldp,
-                              const int64_t* __restrict__ foff, const int32_t* __restrict__ fchunks,
-                              int nfields, int scalar_chunks, int64_t t_begin, int64_t t_end,
-                              PairArgs out) {
+__global__ void __launch_bounds__(32 * kReduceRows) reduce_kernel(
+    const double* __restrict__ part, int64_t ldp, const int64_t* __restrict__ foff,
+    const int32_t* __restrict__ fchunks, int nfields, int scalar_chunks, int64_t t_begin,
+    int64_t t_end, PairArgs out) {
   constexpr int NV = nval_of(PASS);
-  const int64_t i = t_begin + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= t_end) return;
-  int nc = scalar_chunks;
-  if (foff) {
-    int lo = 0, hi = nfields - 1;
-    while (lo < hi) {  // last field with foff[f] <= i
-      const int mid = (lo + hi + 1) >> 1;
-      if (foff[mid] <= i) lo = mid; else hi = mid - 1;
+  __shared__ double sv[NV][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t i = t_begin + int64_t(blockIdx.x) * 32 + tx;
+  int nc = 0;
+  if (i < t_end) {
+    nc = scalar_chunks;
+    if (foff) {
+      int lo = 0, hi = nfields - 1;
+      while (lo < hi) {  // last field with foff[f] <= i
+        const int mid = (lo + hi + 1) >> 1;
+        if (foff[mid] <= i) lo = mid; else hi = mid - 1;
+      }
+      nc = fchunks[lo];
     }
-    nc = fchunks[lo];
   }
-  if (nc <= 1) return;
-  double v[NV];
+  const bool live = nc > 1;
+  if (live) {
+    const int64_t step = int64_t(NV) * ldp;
+    for (int w = ty; w < NV; w += kReduceRows) {
+      const double* p = part + int64_t(w) * ldp + i;
+      double v = 0.0;
+      int c = 0;
+      for (; c + 4 <= nc; c += 4) {
+        const double a0 = p[int64_t(c) * step], a1 = p[int64_t(c + 1) * step];
+        const double a2 = p[int64_t(c + 2) * step], a3 = p[int64_t(c + 3) * step];
+        v += a0; v += a1; v += a2; v += a3;
+      }
+      for (; c < nc; ++c) v += p[int64_t(c) * step];
+      sv[w][tx] = v;
+    }
+  }
+  __syncthreads();
+  if (ty == 0 && live) {
+    double v[NV];
 #pragma unroll
-  for (int w = 0; w < NV; ++w) v[w] = 0.0;
-  for (int c = 0; c < nc; ++c)
-#pragma unroll
-    for (int w = 0; w < NV; ++w) v[w] += part[(int64_t(c) * NV + w) * ldp + i];
-  write_final<PASS, KERNEL>(v, out, i);
+    for (int w = 0; w < NV; ++w) v[w] = sv[w][tx];
+    write_final<PASS, KERNEL>(v, out, i);
+  }
 }
 
 // ---------------------------------------------------------------- dispatch --
@@ -837,8 +865,8 @@ cudaError_t reduce(int kernel, const double* part, int64_t ldp, const int64_t* f
   PairArgs out;
   memset(&out, 0, sizeof(out));
   out.u = u; out.j = j; out.dj = dj; out.ldo = ldo;
-  const int bs = 256;
-  const int grid = int((n + bs - 1) / bs);
+  const dim3 bs(32, kReduceRows);
+  const int grid = int((n + 31) / 32);
   if (kernel == VPM_KERNEL_WINCKELMANS)
     reduce_kernel<PASS, VPM_KERNEL_WINCKELMANS><<<grid, bs, 0, st>>>(
         part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin, t_end, out);
