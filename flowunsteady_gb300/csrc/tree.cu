@@ -498,268 +498,125 @@ __global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restr
 }
 
 // --------------------------------------------------------------- near field --
-// One CTA per target group (one target per thread) against every particle of
-// its near source ranges, staged in shared memory.  FP32: positions relative
-// to the group's first particle from the packed records, sums folded into
-// (hi, lo) pairs every four tiles.  Raw sums go to raw[k·ldr + i] in Morton
-// order:
-//   PASS_UJ    U 3, A 9, W 3 (with the kernel's own pair forms);
+// One CTA of kNearThreads threads per target group against every particle of
+// its near source ranges, with the pair routines of the direct sum
+// (vpm_device.cuh) on T targets per thread:
+//   - the group's 64 targets are held as TQ = 64/T target sets of T targets
+//     (target t = tq + TQ·k), each set by SL = kNearThreads/TQ threads, one per
+//     source slice;
+//   - the concatenated near ranges are staged kNearThreads sources at a time
+//     (positions relative to the group's first particle, from the packed
+//     records); slice s takes the staged sources s, s + SL, s + 2·SL, ..., so
+//     every thread reads each of its sources with broadcast 16-byte loads and
+//     applies it to T targets (packed FP32 pairs for T even);
+//   - a tile is always full: slots past the sources hold a padding source at
+//     1e18 with zero strength, which adds exactly 0 (its q and p underflow),
+//     so the warp votes of the pair routines see the same trip count on every
+//     lane;
+//   - FP32 sums are folded into (hi, lo) pairs (Knuth's TwoSum) every
+//     kNearFoldSources sources of a thread; the epilogue forms every target's raw
+//     sums in FP64 as the slices' (hi + lo) in slice order.
+// Raw sums go to raw[k·ldr + i] in Morton order:
+//   PASS_UJ    U 3, A 9, W 3 (Gaussian-erf A sums hold p/(-3), as the direct
+//              pass's do);
 //   PASS_UJD   those plus DA 9, DW 3 (Gaussian-erf: Dq, Dp vanish beyond the
 //              near field's 7.1σ to FP32 significance);
 //   PASS_ZETA  Ω 3, V 3; PASS_ZETAD also DΩ 3, DV 3 (Gaussian-erf: ζ likewise),
 //              with v_q (and w_q) taken from vw rows of the Morton order.
-//
-// Source pairs: with one target per thread the packed FP32 instructions
-// (add/mul/fma .rn.f32x2) take two SOURCES at once, lane 0 an even staged
-// source and lane 1 the odd one after it; every sum keeps one accumulator per
-// lane, and the folds add both lanes.  The pair forms are those of the direct
-// sum's routines (vpm_device.cuh) with per-lane source constants.  A staged
-// tile is kept as separate float arrays, so that a source pair is one 8-byte
-// load per quantity.
-struct NearTile {
-  float nx[kTreeBlock], ny[kTreeBlock], nz[kTreeBlock];   // -(x - group origin)
-  float gx[kTreeBlock], gy[kTreeBlock], gz[kTreeBlock];   // Γ
-  float ngx[kTreeBlock], ngy[kTreeBlock], ngz[kTreeBlock];   // -Γ (U/J)
-  float c0[kTreeBlock], c1[kTreeBlock], c2[kTreeBlock], c3[kTreeBlock], c4[kTreeBlock];
-  float vx[kTreeBlock], vy[kTreeBlock], vz[kTreeBlock];   // v_q (ζ passes)
-  float wx[kTreeBlock], wy[kTreeBlock], wz[kTreeBlock];   // w_q (PASS_ZETAD)
-};
-// Source constants c0..c4 by pass and kernel:
-//   U/J, U/J + DJ, Gaussian-erf: a = -log2(e)/(2σ²), kErfcxP/σ, -√(2/π)/σ,
-//                                √(2/π)/σ³, 1/σ;
-//   U/J, Winckelmans:            σ², 3/2 σ², 5/2 σ² (c0 + c1);
-//   ζ passes (Gaussian-erf):     a, ζ(0)/σ³.
-// A padding slot (past the sources, read when a tile's count is odd) sits at
-// 1e18 with zero strength and a = -1: every form is finite there and adds 0.
+// Coincident pairs are dropped: the Winckelmans and ζ routines run masked,
+// and the Gaussian-erf U/J routines drop them in their series branch.
+constexpr int kNearThreads = 128;
 constexpr float kNearPadX = 1e18f;
+constexpr int kNearFoldSources = 256;   // sources a thread sums in FP32 between folds
 
-__device__ __forceinline__ float2 ld2(const float* a, int p) {
-  return reinterpret_cast<const float2*>(a)[p];
-}
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
-
-// accum_pair2 with per-lane Γ (sums indexed as in accum_pair; acc lanes are
-// the two sources).
-template <int NV>
-__device__ __forceinline__ void near_accum2(float2 dx, float2 dy, float2 dz, float2 q, float2 p,
-                                            float2 gx, float2 gy, float2 gz, float2 ngx,
-                                            float2 ngy, float2 ngz, float2 (&acc)[NV]) {
-  const float2 c0 = fma2(dz, ngy, mul2(dy, gz));
-  const float2 c1 = fma2(dx, ngz, mul2(dz, gx));
-  const float2 c2 = fma2(dy, ngx, mul2(dx, gy));
-  acc[0] = fma2(q, c0, acc[0]);
-  acc[1] = fma2(q, c1, acc[1]);
-  acc[2] = fma2(q, c2, acc[2]);
-  const float2 p0 = mul2(p, c0), p1 = mul2(p, c1), p2 = mul2(p, c2);
-  acc[3] = fma2(p0, dx, acc[3]);
-  acc[4] = fma2(p0, dy, acc[4]);
-  acc[5] = fma2(p0, dz, acc[5]);
-  acc[6] = fma2(p1, dx, acc[6]);
-  acc[7] = fma2(p1, dy, acc[7]);
-  acc[8] = fma2(p1, dz, acc[8]);
-  acc[9] = fma2(p2, dx, acc[9]);
-  acc[10] = fma2(p2, dy, acc[10]);
-  acc[12] = fma2(q, gx, acc[12]);
-  acc[13] = fma2(q, gy, acc[13]);
-  acc[14] = fma2(q, gz, acc[14]);
-}
-
-// One source pair of a U/J (or U/J + DJ, D) near tile against this thread's
-// target; MASK drops coincident pairs.
-template <int KERNEL, bool D, int NV>
-__device__ __forceinline__ void near_uj_pair(const NearTile& tl, int pp, float2 tx, float2 ty,
-                                             float2 tz, float2 (&acc)[NV]) {
-  const float2 dx = add2(tx, ld2(tl.nx, pp)), dy = add2(ty, ld2(tl.ny, pp)),
-               dz = add2(tz, ld2(tl.nz, pp));
-  const float2 gx = ld2(tl.gx, pp), gy = ld2(tl.gy, pp), gz = ld2(tl.gz, pp);
-  const float2 ngx = ld2(tl.ngx, pp), ngy = ld2(tl.ngy, pp), ngz = ld2(tl.ngz, pp);
-  const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
-  if constexpr (KERNEL == VPM_KERNEL_WINCKELMANS) {
-    const float2 h = add2(r2, ld2(tl.c0, pp));
-    const float2 rs = make_float2(rsqrt_ftz(h.x), rsqrt_ftz(h.y));
-    const float2 rs2 = mul2(rs, rs);
-    const float2 rs3 = mul2(rs2, rs);
-    const float2 rs5 = mul2(rs3, rs2);
-    const float2 rs7 = mul2(rs5, rs2);
-    float2 q = fma2(ld2(tl.c1, pp), rs5, rs3);
-    q.x = r2.x > 0.f ? q.x : 0.f;
-    q.y = r2.y > 0.f ? q.y : 0.f;
-    near_accum2<NV>(dx, dy, dz, q, fma2(ld2(tl.c2, pp), rs7, rs5), gx, gy, gz, ngx, ngy, ngz,
-                    acc);
-  } else {
-    // Gaussian-erf: the forms of uj_source_gauss / ujd_source_gauss (A sums
-    // hold p/(-3)); a warp vote takes the far form where both sources are
-    // beyond ρ² = 50 at all 32 targets.
-    const float2 arg = mul2(r2, ld2(tl.c0, pp));
-    const float amax = fmaxf(arg.x, arg.y);
-    const float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-    const float2 ri2 = mul2(ri, ri);
-    if (__all_sync(0xffffffffu, amax <= kArgFar)) {
-      const float2 q = mul2(ri2, ri);
-      const float2 p = mul2(q, ri2);
-      near_accum2<NV>(dx, dy, dz, q, p, gx, gy, gz, ngx, ngy, ngz, acc);
-      if constexpr (D) {
-        if (!__all_sync(0xffffffffu, amax <= kArgZero)) {
-          const float2 e = make_float2(ex2_ftz(arg.x), ex2_ftz(arg.y));
-          const float2 k3e = mul2(ld2(tl.c3, pp), e);
-          const float2 is1 = ld2(tl.c4, pp);
-          const float2 dp = mul2(k3e, mul2(is1, is1));
-          const float2 c0 = fma2(dz, ngy, mul2(dy, gz));
-          const float2 c1 = fma2(dx, ngz, mul2(dz, gx));
-          const float2 c2 = fma2(dy, ngx, mul2(dx, gy));
-          const float2 a0 = mul2(dp, c0), a1 = mul2(dp, c1), a2 = mul2(dp, c2);
-          acc[15] = fma2(a0, dx, acc[15]); acc[16] = fma2(a0, dy, acc[16]);
-          acc[17] = fma2(a0, dz, acc[17]); acc[18] = fma2(a1, dx, acc[18]);
-          acc[19] = fma2(a1, dy, acc[19]); acc[20] = fma2(a1, dz, acc[20]);
-          acc[21] = fma2(a2, dx, acc[21]); acc[22] = fma2(a2, dy, acc[22]);
-          const float2 dq = neg2(k3e);
-          acc[24] = fma2(dq, gx, acc[24]); acc[25] = fma2(dq, gy, acc[25]);
-          acc[26] = fma2(dq, gz, acc[26]);
-        }
-      }
-      return;
-    }
-    const float2 r = mul2(r2, ri);
-    const float2 e = make_float2(ex2_ftz(arg.x), ex2_ftz(arg.y));
-    const float2 u = fma2(ld2(tl.c1, pp), r, bc2(1.f));
-    const float2 t = make_float2(rcp_ftz(u.x), rcp_ftz(u.y));
-    const float2 nf = mul2(t, fma2(t, fma2(t, fma2(t, bc2(-kErfcxA4), bc2(-kErfcxA3)),
-                                           bc2(-kErfcxA2)), bc2(-kErfcxA1)));
-    const float2 g = fma2(e, fma2(ld2(tl.c2, pp), r, nf), bc2(1.f));
-    const float2 k3e = mul2(ld2(tl.c3, pp), e);
-    float2 q = mul2(g, mul2(ri2, ri));
-    float2 p = mul2(fma2(k3e, bc2(-1.f / 3.f), q), ri2);
-    float2 dq = neg2(k3e), dp = bc2(0.f);
-    if constexpr (D) {
-      const float2 is1 = ld2(tl.c4, pp);
-      dp = mul2(k3e, mul2(is1, is1));
-    }
-    if (__any_sync(0xffffffffu, fmaxf(arg.x, arg.y) > kArgSeries)) {
-      const float2 is1 = ld2(tl.c4, pp);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const float a = h ? arg.y : arg.x;
-        if (a > kArgSeries) {
-          const float i1 = h ? is1.y : is1.x, i3 = i1 * i1 * i1, i5n = i3 * i1 * i1 * (-1.f / 3.f);
-          float h1, h2;
-          GaussSeries<float, 10>::eval(a * kArgToRho2, h1, h2);
-          const bool self = a == 0.f;
-          const float qs = self ? 0.f : h1 * i3, ps = self ? 0.f : h2 * i5n;
-          if (h) {
-            q.y = qs; p.y = ps;
-            if (self) { dq.y = 0.f; dp.y = 0.f; }
-          } else {
-            q.x = qs; p.x = ps;
-            if (self) { dq.x = 0.f; dp.x = 0.f; }
-          }
-        }
-      }
-    }
-    near_accum2<NV>(dx, dy, dz, q, p, gx, gy, gz, ngx, ngy, ngz, acc);
-    if constexpr (D) {
-      const float2 c0 = fma2(dz, ngy, mul2(dy, gz));
-      const float2 c1 = fma2(dx, ngz, mul2(dz, gx));
-      const float2 c2 = fma2(dy, ngx, mul2(dx, gy));
-      const float2 a0 = mul2(dp, c0), a1 = mul2(dp, c1), a2 = mul2(dp, c2);
-      acc[15] = fma2(a0, dx, acc[15]); acc[16] = fma2(a0, dy, acc[16]);
-      acc[17] = fma2(a0, dz, acc[17]); acc[18] = fma2(a1, dx, acc[18]);
-      acc[19] = fma2(a1, dy, acc[19]); acc[20] = fma2(a1, dz, acc[20]);
-      acc[21] = fma2(a2, dx, acc[21]); acc[22] = fma2(a2, dy, acc[22]);
-      acc[24] = fma2(dq, gx, acc[24]); acc[25] = fma2(dq, gy, acc[25]);
-      acc[26] = fma2(dq, gz, acc[26]);
-    }
-  }
-}
-
-// One source pair of a ζ near tile (Gaussian-erf; coincident pairs dropped;
-// a warp vote skips pairs whose ζ underflows to zero at all 32 targets).
-template <bool D, int NV>
-__device__ __forceinline__ void near_zeta_pair(const NearTile& tl, int pp, float2 tx, float2 ty,
-                                               float2 tz, float2 (&acc)[NV]) {
-  const float2 dx = add2(tx, ld2(tl.nx, pp)), dy = add2(ty, ld2(tl.ny, pp)),
-               dz = add2(tz, ld2(tl.nz, pp));
-  const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
-  const float2 x = mul2(r2, ld2(tl.c0, pp));
-  if (__all_sync(0xffffffffu, fmaxf(x.x, x.y) <= kArgZero)) return;
-  float2 z = mul2(ld2(tl.c1, pp), make_float2(ex2_ftz(x.x), ex2_ftz(x.y)));
-  float2 dzz = bc2(0.f);
-  if (D) dzz = mul2(z, fma2(x, bc2(kArgToRho2), bc2(-3.f)));
-  z.x = r2.x > 0.f ? z.x : 0.f;
-  z.y = r2.y > 0.f ? z.y : 0.f;
-  if (D) {
-    dzz.x = r2.x > 0.f ? dzz.x : 0.f;
-    dzz.y = r2.y > 0.f ? dzz.y : 0.f;
-  }
-  const float2 gx = ld2(tl.gx, pp), gy = ld2(tl.gy, pp), gz = ld2(tl.gz, pp);
-  const float2 vx = ld2(tl.vx, pp), vy = ld2(tl.vy, pp), vz = ld2(tl.vz, pp);
-  acc[0] = fma2(z, gx, acc[0]);
-  acc[1] = fma2(z, gy, acc[1]);
-  acc[2] = fma2(z, gz, acc[2]);
-  acc[3] = fma2(z, vx, acc[3]);
-  acc[4] = fma2(z, vy, acc[4]);
-  acc[5] = fma2(z, vz, acc[5]);
-  if constexpr (D) {
-    acc[6] = fma2(dzz, gx, acc[6]);
-    acc[7] = fma2(dzz, gy, acc[7]);
-    acc[8] = fma2(dzz, gz, acc[8]);
-    acc[9] = fma2(dzz, vx, fma2(z, ld2(tl.wx, pp), acc[9]));
-    acc[10] = fma2(dzz, vy, fma2(z, ld2(tl.wy, pp), acc[10]));
-    acc[11] = fma2(dzz, vz, fma2(z, ld2(tl.wz, pp), acc[11]));
-  }
-}
+template <int PASS>
+struct NearShape {
+  // The U/J passes hold 15 (27 with DJ) sums per target: two targets per
+  // thread keep their registers and fold pairs within three or more CTAs per
+  // SM (four targets need more than the 168 registers of three CTAs and spill);
+  // the ζ passes (6 or 12 sums) take four.
+  static constexpr int T = (PASS == PASS_UJ || PASS == PASS_UJD) ? 2 : 4;
+  static constexpr int TQ = kTreeBlock / T;
+  static constexpr int SL = kNearThreads / TQ;
+  static constexpr int NV = nval_of(PASS);
+  static constexpr bool UJ = PASS == PASS_UJ || PASS == PASS_UJD;
+  static constexpr int QUADS = UJ ? 2 : (PASS == PASS_ZETA ? 3 : 4);
+  static constexpr size_t kQuadBytes = size_t(kNearThreads) * QUADS * sizeof(float4);
+  static constexpr size_t kFoldBytes = size_t(kNearThreads) * T * NV * 2 * sizeof(float);
+  static constexpr size_t kSmem = kQuadBytes + kFoldBytes;
+  static constexpr int kMinBlocks = (PASS == PASS_UJD || PASS == PASS_ZETAD) ? 3 : 4;
+};
 
 template <int KERNEL, int PASS>
-__global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
+__global__ void __launch_bounds__(kNearThreads, NearShape<PASS>::kMinBlocks) near_tile_kernel(
     int nfront, const int* __restrict__ onear, const int* __restrict__ nnear,
     const int2* __restrict__ near_list, const float4* __restrict__ rec,
     const double* __restrict__ vw, int64_t ldv, double* raw, int64_t ldr, int64_t n,
     int* counters, unsigned long long* pairs) {
-  static_assert(kTreeBlock == 64, "two-warp scan below");
-  constexpr int NV = nval_of(PASS);
-  constexpr bool UJ = PASS == PASS_UJ || PASS == PASS_UJD;
+  using Sh = NearShape<PASS>;
+  constexpr int T = Sh::T, TQ = Sh::TQ, SL = Sh::SL, NV = Sh::NV;
+  constexpr bool UJ = Sh::UJ;
   constexpr bool D = PASS == PASS_UJD || PASS == PASS_ZETAD;
-  __shared__ __align__(16) NearTile tl;
-  __shared__ int s_start[kTreeBlock], s_pref[kTreeBlock + 1], s_w0;
-  const int tid = threadIdx.x, lane = tid & 31;
+  constexpr int PER = kNearThreads / SL;              // staged sources per thread and tile
+  constexpr int FOLD_TILES = kNearFoldSources / PER;  // tiles between two folds
+  static_assert(kTreeBlock == 64 && kNearThreads == 128, "four-warp scan below");
+  extern __shared__ __align__(16) unsigned char near_smem[];
+  float4* tA = reinterpret_cast<float4*>(near_smem);
+  float4* tB = tA + kNearThreads;
+  float4* tC = tB + kNearThreads;
+  float4* tD = tC + kNearThreads;
+  float* fold_hi = reinterpret_cast<float*>(near_smem + Sh::kQuadBytes);
+  float* fold_lo = fold_hi + size_t(kNearThreads) * T * NV;
+  __shared__ int s_start[kNearThreads], s_pref[kNearThreads + 1], s_wsum[4];
+
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int tq = tid % TQ, sl = tid / TQ;
   const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
   const float4 o0 = rec[3 * int64_t(a)], o1 = rec[3 * int64_t(a) + 1];
   const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
   const int l0 = onear[t0s], ln = onear[t1s] + nnear[t1s] - l0;
-  const int i = a + tid;
-  float tx = 0.f, ty = 0.f, tz = 0.f;
-  if (i < b) {
-    const float4 r0 = rec[3 * int64_t(i)], r1 = rec[3 * int64_t(i) + 1];
-    tx = rel_f32(r0.x, r1.x, o0.x, o1.x);
-    ty = rel_f32(r0.y, r1.y, o0.y, o1.y);
-    tz = rel_f32(r0.z, r1.z, o0.z, o1.z);
-  }
-  const float2 tx2 = bc2(tx), ty2 = bc2(ty), tz2 = bc2(tz);
-  float2 acc[NV];
-  float shi[NV], slo[NV];
+
+  float tx[T], ty[T], tz[T];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    acc[v] = bc2(0.f);
-    shi[v] = slo[v] = 0.f;
+  for (int k = 0; k < T; ++k) {
+    const int i = a + tq + TQ * k;
+    tx[k] = ty[k] = tz[k] = 0.f;
+    if (i < b) {
+      const float4 r0 = rec[3 * int64_t(i)], r1 = rec[3 * int64_t(i) + 1];
+      tx[k] = rel_f32(r0.x, r1.x, o0.x, o1.x);
+      ty[k] = rel_f32(r0.y, r1.y, o0.y, o1.y);
+      tz[k] = rel_f32(r0.z, r1.z, o0.z, o1.z);
+    }
   }
-  auto fold = [&]() {
+  float acc[T][NV];
+#pragma unroll
+  for (int k = 0; k < T; ++k)
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      float hs, es;
-      two_sum(shi[v], acc[v].x, hs, es);
-      shi[v] = hs;
-      slo[v] += es;
-      two_sum(shi[v], acc[v].y, hs, es);
-      shi[v] = hs;
-      slo[v] += es;
-      acc[v] = bc2(0.f);
+      acc[k][v] = 0.f;
+      fold_hi[(v * T + k) * kNearThreads + tid] = 0.f;
+      fold_lo[(v * T + k) * kNearThreads + tid] = 0.f;
     }
+  auto fold = [&]() {
+#pragma unroll
+    for (int k = 0; k < T; ++k)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const int o = (v * T + k) * kNearThreads + tid;
+        float s, e;
+        two_sum(fold_hi[o], acc[k][v], s, e);
+        fold_hi[o] = s;
+        fold_lo[o] += e;
+        acc[k][v] = 0.f;
+      }
   };
+
   int tiles = 0;
-  // The near ranges, kTreeBlock at a time: their lengths' prefix sums in shared
-  // memory; the concatenated sources are then staged in full tiles, each slot
-  // finding its range by binary search.
-  for (int rc0 = 0; rc0 < ln; rc0 += kTreeBlock) {
-    const int nr = min(kTreeBlock, ln - rc0);
+  // The near ranges, kNearThreads at a time: their lengths' prefix sums in
+  // shared memory; the concatenated sources are then staged in full tiles, each
+  // slot finding its range by binary search.
+  for (int rc0 = 0; rc0 < ln; rc0 += kNearThreads) {
+    const int nr = min(kNearThreads, ln - rc0);
     int len = 0;
     __syncthreads();   // previous chunk's tiles consumed
     if (tid < nr) {
@@ -771,25 +628,32 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
       }
       s_start[tid] = rg.x;
     }
-    int incl = len;   // inclusive scan over the 64 threads
+    int incl = len;   // inclusive scan over the 128 threads
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int v = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += v;
     }
-    if (tid == 31) s_w0 = incl;
+    if (lane == 31) s_wsum[wid] = incl;
     __syncthreads();
-    if (tid >= 32) incl += s_w0;
+    for (int w = 0; w < wid; ++w) incl += s_wsum[w];
     s_pref[tid + 1] = incl;
     if (tid == 0) s_pref[0] = 0;
     __syncthreads();
     const int total = s_pref[nr];
     if (tid == 0 && pairs) atomicAdd(&pairs[0], (unsigned long long)total * (unsigned long long)(b - a));
-    for (int q0 = 0; q0 < total; q0 += kTreeBlock) {
+    for (int q0 = 0; q0 < total; q0 += kNearThreads) {
       const int q = q0 + tid;
-      float sx = kNearPadX, sy = kNearPadX, sz = kNearPadX, gx = 0.f, gy = 0.f, gz = 0.f;
-      float k0 = -1.f, k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f;
-      float vx = 0.f, vy = 0.f, vz = 0.f, wx = 0.f, wy = 0.f, wz = 0.f;
+      float4 qa = make_float4(kNearPadX, kNearPadX, kNearPadX, 0.f);
+      float4 qb = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 qc = make_float4(0.f, 0.f, 0.f, 0.f), qd = qc;
+      // Padding constants: a unit core.
+      if (UJ && KERNEL == VPM_KERNEL_WINCKELMANS) {
+        qa.w = 1.f; qb.w = 1.5f;
+      } else {
+        qa.w = float(-0.5 * kLog2e);
+        qb.w = UJ ? 1.f : float(kZeta0Gauss);
+      }
       if (q < total) {
         int lo_r = 0, hi_r = nr - 1;   // last range r with s_pref[r] <= q
         while (lo_r < hi_r) {
@@ -799,63 +663,91 @@ __global__ void __launch_bounds__(kTreeBlock) near_f32_kernel(
         }
         const int64_t j = s_start[lo_r] + (q - s_pref[lo_r]);
         const float4 r0 = rec[3 * j], r1 = rec[3 * j + 1], r2 = rec[3 * j + 2];
-        sx = rel_f32(r0.x, r1.x, o0.x, o1.x);
-        sy = rel_f32(r0.y, r1.y, o0.y, o1.y);
-        sz = rel_f32(r0.z, r1.z, o0.z, o1.z);
-        gx = r2.x; gy = r2.y; gz = r2.z;
-        k0 = r0.w;
-        const float is1 = r1.w;
-        if (UJ && KERNEL == VPM_KERNEL_WINCKELMANS) {
-          k1 = r1.w;            // 3/2 σ²
-          k2 = r0.w + r1.w;     // 5/2 σ²
-        } else if (UJ) {
-          k1 = kErfcxP * is1;
-          k2 = -float(kSqrt2overPi) * is1;
-          k3 = float(kSqrt2overPi) * is1 * is1 * is1;
-          k4 = is1;
+        qa = make_float4(rel_f32(r0.x, r1.x, o0.x, o1.x), rel_f32(r0.y, r1.y, o0.y, o1.y),
+                         rel_f32(r0.z, r1.z, o0.z, o1.z), r0.w);
+        if (UJ) {
+          qb = make_float4(r2.x, r2.y, r2.z, r1.w);
         } else {
           // Gaussian-erf ζ constants: a = -log2(e)/(2σ²) (as for U/J), b = ζ(0)/σ³.
-          k1 = float(kZeta0Gauss) * is1 * is1 * is1;
-          vx = float(vw[j]); vy = float(vw[ldv + j]); vz = float(vw[2 * ldv + j]);
-          if (D) {
-            wx = float(vw[3 * ldv + j]); wy = float(vw[4 * ldv + j]); wz = float(vw[5 * ldv + j]);
-          }
+          const float is1 = r1.w;
+          qb = make_float4(r2.x, r2.y, r2.z, float(kZeta0Gauss) * is1 * is1 * is1);
+          qc = make_float4(float(vw[j]), float(vw[ldv + j]), float(vw[2 * ldv + j]), 0.f);
+          if (D) qd = make_float4(float(vw[3 * ldv + j]), float(vw[4 * ldv + j]),
+                                  float(vw[5 * ldv + j]), 0.f);
         }
       }
       __syncthreads();   // previous tile consumed
-      tl.nx[tid] = -sx; tl.ny[tid] = -sy; tl.nz[tid] = -sz;
-      tl.gx[tid] = gx; tl.gy[tid] = gy; tl.gz[tid] = gz;
-      tl.c0[tid] = k0; tl.c1[tid] = k1;
-      if constexpr (UJ) {
-        tl.ngx[tid] = -gx; tl.ngy[tid] = -gy; tl.ngz[tid] = -gz;
-        tl.c2[tid] = k2; tl.c3[tid] = k3; tl.c4[tid] = k4;
-      } else {
-        tl.vx[tid] = vx; tl.vy[tid] = vy; tl.vz[tid] = vz;
-        if constexpr (D) { tl.wx[tid] = wx; tl.wy[tid] = wy; tl.wz[tid] = wz; }
+      tA[tid] = qa;
+      tB[tid] = qb;
+      if (!UJ) {
+        tC[tid] = qc;
+        if (D) tD[tid] = qd;
       }
       __syncthreads();
-      const int npair = (min(kTreeBlock, total - q0) + 1) >> 1;
-      for (int pp = 0; pp < npair; ++pp) {
-        if constexpr (UJ) near_uj_pair<KERNEL, D, NV>(tl, pp, tx2, ty2, tz2, acc);
-        else near_zeta_pair<D, NV>(tl, pp, tx2, ty2, tz2, acc);
+#pragma unroll 1
+      for (int m = 0; m < PER; ++m) {
+        const int js = sl + SL * m;
+        if constexpr (PASS == PASS_UJ) {
+          if (KERNEL == VPM_KERNEL_WINCKELMANS) uj_source_winck<T, true>(tA[js], tB[js], tx, ty, tz, acc);
+          else uj_source_gauss<T, true>(tA[js], tB[js], tx, ty, tz, acc);
+        } else if constexpr (PASS == PASS_UJD) {
+          if (KERNEL == VPM_KERNEL_WINCKELMANS) ujd_source_winck<T, true>(tA[js], tB[js], tx, ty, tz, acc);
+          else ujd_source_gauss<T, true>(tA[js], tB[js], tx, ty, tz, acc);
+        } else {
+          zeta_source<KERNEL, T, true, D, true>(tA[js], tB[js], tC[js], D ? tD[js] : tC[js], tx,
+                                                ty, tz, acc);
+        }
       }
-      if (++tiles % 4 == 0) fold();
+      if (++tiles % FOLD_TILES == 0) fold();
     }
   }
   fold();
-  if (i < b) {
-    double v[NV];
+  __syncthreads();
+  if (tid < kTreeBlock) {
+    const int i = a + tid;
+    if (i < b) {
+      const int k = tid / TQ, s0 = tid % TQ;
+      // One value at a time (a fully unrolled epilogue would hold every slice's
+      // pairs of every value in registers at once).
+      double a00 = 0.0, a11 = 0.0, d00 = 0.0, d11 = 0.0;
+#pragma unroll 1
+      for (int w = 0; w < NV; ++w) {
+        double v = 0.0;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] = double(shi[k]) + double(slo[k]);
-    if constexpr (UJ && KERNEL == VPM_KERNEL_GAUSSIANERF) {
-#pragma unroll
-      for (int k = 3; k < 11; ++k) v[k] *= kGaussAScale;   // A holds p/(-3) sums
+        for (int l = 0; l < SL; ++l) {
+          const int o = (w * T + k) * kNearThreads + l * TQ + s0;
+          v += double(fold_hi[o]) + double(fold_lo[o]);
+        }
+        if (UJ && KERNEL == VPM_KERNEL_GAUSSIANERF && w >= 3 && w < 11)
+          v *= kGaussAScale;   // A holds p/(-3) sums
+        if (UJ) {   // A22: the FP32 forms keep J trace-free
+          if (w == 3) a00 = v;
+          if (w == 7) a11 = v;
+          if (w == 11) v = -(a00 + a11);
+        }
+        if (PASS == PASS_UJD) {
+          if (w == 15) d00 = v;
+          if (w == 19) d11 = v;
+          if (w == 23) v = -(d00 + d11);
+        }
+        raw[w * ldr + i] = v;
+      }
     }
-    if constexpr (UJ) v[11] = -(v[3] + v[7]);   // A22: the FP32 forms keep J trace-free
-    if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
-#pragma unroll
-    for (int k = 0; k < NV; ++k) raw[k * ldr + i] = v[k];
   }
+}
+
+template <int KERNEL, int PASS>
+void launch_near(int ngroups, int nfront, const FmmWork* w, const double* vw, int64_t ldv,
+                 int64_t ldr, int64_t n, unsigned long long* pairs, cudaStream_t st) {
+  static const bool once = [] {
+    cudaFuncSetAttribute(near_tile_kernel<KERNEL, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(NearShape<PASS>::kSmem));
+    return true;
+  }();
+  (void)once;
+  near_tile_kernel<KERNEL, PASS><<<ngroups, kNearThreads, NearShape<PASS>::kSmem, st>>>(
+      nfront, w->onear, w->nnear, w->near_list, w->rec, vw, ldv, w->near_raw, ldr, n, w->counters,
+      pairs);
 }
 
 // Rows of a Morton-ordered array back to the original order.
@@ -1003,7 +895,7 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
                           kp * v[9] + w1, kp * v[10] - w0, kp * v[11]};
 #pragma unroll
     for (int k = 0; k < 9; ++k) J[k * ldo + o] = -w * jn[k] + w * double(jf[k]);
-    if constexpr (D) {   // α-derivative: near field only (see near_f32_kernel)
+    if constexpr (D) {   // α-derivative: near field only (see near_tile_kernel)
       const double d0 = raw[24 * ldr + i], d1 = raw[25 * ldr + i], d2 = raw[26 * ldr + i];
       const double* a9 = raw + 15 * ldr + i;
       const double jd[9] = {kp * a9[0],          kp * a9[ldr] + d2,     kp * a9[2 * ldr] - d1,
@@ -1314,17 +1206,14 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
           w->counters);
   } else {
     if (dj)
-      near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_UJD><<<ngroups, kTreeBlock, 0, st>>>(
-          nfront, w->onear, w->nnear, w->near_list, w->rec, nullptr, 0, w->near_raw, ldw, n,
-          w->counters, w->pairs);
+      launch_near<VPM_KERNEL_GAUSSIANERF, PASS_UJD>(ngroups, nfront, w, nullptr, 0, ldw, n,
+                                                    w->pairs, st);
     else if (kernel == VPM_KERNEL_WINCKELMANS)
-      near_f32_kernel<VPM_KERNEL_WINCKELMANS, PASS_UJ><<<ngroups, kTreeBlock, 0, st>>>(
-          nfront, w->onear, w->nnear, w->near_list, w->rec, nullptr, 0, w->near_raw, ldw, n,
-          w->counters, w->pairs);
+      launch_near<VPM_KERNEL_WINCKELMANS, PASS_UJ>(ngroups, nfront, w, nullptr, 0, ldw, n,
+                                                   w->pairs, st);
     else
-      near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_UJ><<<ngroups, kTreeBlock, 0, st>>>(
-          nfront, w->onear, w->nnear, w->near_list, w->rec, nullptr, 0, w->near_raw, ldw, n,
-          w->counters, w->pairs);
+      launch_near<VPM_KERNEL_GAUSSIANERF, PASS_UJ>(ngroups, nfront, w, nullptr, 0, ldw, n,
+                                                   w->pairs, st);
   }
   if ((e = launched(1)) != cudaSuccess) return e;
   if (p == 2)
@@ -1374,13 +1263,11 @@ cudaError_t fmm_zeta(vpm_ctx* c, bool d, const double* vs, const double* ws, dou
   gather_rows_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, vs, c->ld, w->vw, ldw);
   if (d) gather_rows_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, ws, c->ld, w->vw + 3 * ldw, ldw);
   if (d)
-    near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_ZETAD><<<ngroups, kTreeBlock, 0, st>>>(
-        nfront, w->onear, w->nnear, w->near_list, w->rec, w->vw, ldw, w->near_raw, ldw, n,
-        w->counters, nullptr);
+    launch_near<VPM_KERNEL_GAUSSIANERF, PASS_ZETAD>(ngroups, nfront, w, w->vw, ldw, ldw, n,
+                                                    nullptr, st);
   else
-    near_f32_kernel<VPM_KERNEL_GAUSSIANERF, PASS_ZETA><<<ngroups, kTreeBlock, 0, st>>>(
-        nfront, w->onear, w->nnear, w->near_list, w->rec, w->vw, ldw, w->near_raw, ldw, n,
-        w->counters, nullptr);
+    launch_near<VPM_KERNEL_GAUSSIANERF, PASS_ZETA>(ngroups, nfront, w, w->vw, ldw, ldw, n,
+                                                   nullptr, st);
   scatter_rows_kernel<<<grid, 256, 0, st>>>(n, d ? 12 : 6, w->perm, w->near_raw, ldw, out, c->ld);
   c->launches += d ? 4 : 3;
   return cudaGetLastError();
