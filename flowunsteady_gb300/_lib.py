@@ -72,7 +72,8 @@ EXPORTS = [
 class Fmm(ctypes.Structure):
     """Mirror of struct vpm_fmm (treecode settings)."""
     _fields_ = [("p", ctypes.c_int32), ("ncrit", ctypes.c_int32), ("theta", ctypes.c_double),
-                ("sigma_factor", ctypes.c_double)]
+                ("sigma_factor", ctypes.c_double), ("local_order", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class Scheme(ctypes.Structure):
@@ -108,7 +109,7 @@ class Tile(ctypes.Structure):
 
 
 FMM_STATS = ["cells", "leaves", "groups", "far_entries", "near_entries", "near_pairs",
-             "far_evaluations"]
+             "far_evaluations", "local_terms"]
 
 
 def default_fmm():

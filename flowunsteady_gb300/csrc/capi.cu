@@ -198,12 +198,31 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   }
   if (cluster <= 1 && pc.max_chunks > 0 && n_chunk > pc.max_chunks)
     n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
+  // Whole waves of tiles over the whole source range, and only the rest split:
+  // the same time in units of a whole-tile CTA when CTAs of a wave take equal
+  // time, with partial sums (written, then read back by the reduction) for the
+  // split tiles only.
+  int64_t n_full = 0;
+  if (cluster <= 1 && n_chunk > 1 && n_tb > resident) {
+    const int64_t full_waves = n_tb / resident, nf = full_waves * resident, nr = n_tb - nf;
+    int64_t rchunk = 0;
+    const int rc = nr > 0 ? plan_chunks(nr, pc.ns, sh.block, resident, &rchunk, pc.max_chunks) : 1;
+    const double t_hybrid =
+        double(full_waves) + (nr > 0 ? double(ceil_div(nr * rc, resident)) / rc : 0.0);
+    const double t_split = double(ceil_div(n_tb * n_chunk, resident)) / n_chunk;
+    if (t_hybrid <= t_split * 1.001) {
+      n_full = nf;
+      n_chunk = nr > 0 ? rc : 1;
+      chunk = nr > 0 ? rchunk : pc.ns;
+    }
+  }
   PairPlan plan;
   plan.shape = sh;
   plan.n_tb = n_tb;
   plan.n_chunk = n_chunk;
   plan.chunk = chunk;
   plan.cluster = cluster;
+  plan.n_full = n_full;
   const int nv = nval_of(pc.pass);
   const size_t need = plan.slots() > 1 ? size_t(plan.slots()) * nv * size_t(ldp) : 0;
   if (need_part) *need_part = std::max(*need_part, need);
@@ -217,7 +236,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.sigma_scale = pc.sigma_scale;
   a.dj = pc.dj;
   a.t_off = pc.t0; a.nt = nt; a.ns = pc.ns; a.chunk = chunk;
-  a.n_tb = int(n_tb); a.n_chunk = n_chunk;
+  a.n_tb = int(n_tb); a.n_chunk = n_chunk; a.n_full = int(n_full);
   a.items = nullptr; a.n_items = 0; a.counter = nullptr;
   a.u = pc.u; a.j = pc.j; a.ldo = pc.ldo;
   a.part = part; a.ldp = ldp;
@@ -228,10 +247,12 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.coh = pc.coh;
   a.coh_blocks = ceil_div(pc.ns, 32);
   a.cluster = cluster;
-  cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
+  cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a,
+                              int(n_full + (n_tb - n_full) * n_chunk), st);
   if (e != cudaSuccess) return e;
   if (plan.slots() > 1) {
-    e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
+    const int64_t t_split = std::min(pc.t1, pc.t0 + n_full * TB);
+    e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, t_split, pc.t1,
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
   return e;
@@ -461,6 +482,8 @@ int validate_scheme(vpm_ctx* c, const vpm_scheme* s) {
     if (s->fmm.ncrit < 1 || !(s->fmm.theta > 0.0 && s->fmm.theta < 1.0) ||
         !(s->fmm.sigma_factor >= 0.0))
       return ctx_fail(c, VPM_ERR_INVALID, "treecode settings out of range");
+    if (!fmm_local_order_supported(s->fmm.local_order))
+      return ctx_fail(c, VPM_ERR_UNSUPPORTED, "local expansion order not compiled (0, 7)");
   }
   return VPM_OK;
 }
@@ -703,7 +726,7 @@ static cudaError_t uj_pass(vpm_ctx* c, const vpm_scheme* s, bool direct = false)
     if (c->dry) return cudaSuccess;
     const char* why = nullptr;
     cudaError_t e = fmm_eval(c, s->kernel, s->precision, s->fmm.p, s->fmm.ncrit, s->fmm.theta,
-                             s->fmm.sigma_factor, nullptr, &why);
+                             s->fmm.sigma_factor, s->fmm.local_order, nullptr, &why);
     if (e != cudaSuccess && why) c->err = why;
     return e;
   }
@@ -723,7 +746,7 @@ static cudaError_t ujd_pass(vpm_ctx* c, const vpm_scheme* s) {
     if (c->dry) return cudaSuccess;
     const char* why = nullptr;
     cudaError_t e = fmm_eval(c, s->kernel, s->precision, s->fmm.p, s->fmm.ncrit, s->fmm.theta,
-                             s->fmm.sigma_factor, c->Jt, &why);
+                             s->fmm.sigma_factor, s->fmm.local_order, c->Jt, &why);
     if (e != cudaSuccess && why) c->err = why;
     return e;
   }
@@ -1191,6 +1214,8 @@ void vpm_fmm_default(vpm_fmm* f) {
   f->ncrit = 50;
   f->theta = 0.4;
   f->sigma_factor = 7.1;
+  f->local_order = 7;
+  f->reserved = 0;
 }
 
 int vpm_eval_UJ_fmm(vpm_ctx* c, int kernel, int precision, const vpm_fmm* f) {
@@ -1201,12 +1226,15 @@ int vpm_eval_UJ_fmm(vpm_ctx* c, int kernel, int precision, const vpm_fmm* f) {
   if (!fmm_order_supported(f->p)) return ctx_fail(c, VPM_ERR_UNSUPPORTED, "expansion order not compiled (2, 4, 6)");
   if (f->ncrit < 1 || !(f->theta > 0.0 && f->theta < 1.0) || !(f->sigma_factor >= 0.0))
     return ctx_fail(c, VPM_ERR_INVALID, "treecode settings out of range");
+  if (!fmm_local_order_supported(f->local_order))
+    return ctx_fail(c, VPM_ERR_UNSUPPORTED, "local expansion order not compiled (0, 7)");
   int rc = check_inject(c);
   if (rc) return rc;
   DeviceGuard dg(c->device);
   const char* why = nullptr;
   cudaError_t e =
-      fmm_eval(c, kernel, precision, f->p, f->ncrit, f->theta, f->sigma_factor, nullptr, &why);
+      fmm_eval(c, kernel, precision, f->p, f->ncrit, f->theta, f->sigma_factor, f->local_order,
+               nullptr, &why);
   if (e == cudaErrorInvalidValue && why) return ctx_fail(c, VPM_ERR_CUDA, why);
   if (e != cudaSuccess)
     return cuda_fail(c, e, why ? (std::string("treecode evaluation, ") + why).c_str() : "treecode evaluation");

@@ -44,6 +44,7 @@ struct PairPlan {
   int n_chunk = 1;      // source chunks per target tile
   int64_t chunk = 0;    // sources per chunk
   int cluster = 1;      // > 1: the chunks of a tile are one cluster, summed on chip
+  int64_t n_full = 0;   // leading tiles over the whole source range (final values)
   // Partial slots the plan writes (and a reduction launch sums).
   int slots() const { return (n_chunk > 1 && cluster <= 1) ? n_chunk : 1; }
 };
@@ -132,8 +133,11 @@ void fmm_free(FmmWork* w);
 bool fmm_order_supported(int p);
 // U and J (and, when dj is given, the near-field α-derivative DJ: FP32
 // Gaussian-erf only) of every particle by the treecode.
+// With local_order > 0 (7; p = 4, FP32/FP32C) far cells at least as large as
+// the target group are taken by a local expansion per group.
 cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
-                     double sfac, double* dj, const char** why);
+                     double sfac, int local_order, double* dj, const char** why);
+bool fmm_local_order_supported(int q);
 // ζ sums over the near lists of the last fmm_eval of the same field.
 cudaError_t fmm_zeta(vpm_ctx* c, bool d, const double* vs, const double* ws, double* out,
                      const char** why);

@@ -20,12 +20,17 @@
 //      d - R_t - R_s >= sigma_factor·σmax_s (d = distance of the centres, FP32
 //      boxes), then it is evaluated from its moments; otherwise its leaves are
 //      summed directly, consecutive leaves merged into one range of particles
-//      (two passes: count, fill);
-//   5. the direct near field: one CTA per group over its near ranges, with the
+//      (two passes: count, fill); with local expansions, far cells at least
+//      as large as the group are marked for them;
+//   5. local expansions (FP32, P = 4): the marked cells' moments turned into
+//      one local expansion of ψ per group (M2L, tree.cuh);
+//   6. the direct near field: one CTA per group over its near ranges, with the
 //      regularised kernels of the direct sum (FP32 pair routines on positions
 //      relative to the group's first particle, or FP64);
-//   6. the far field: one thread per target over the far cells of its group
-//      (tree.cuh), added to the near field; results go to the original order.
+//   7. the far field: one thread per target over the unmarked far cells of its
+//      group (M2P, tree.cuh), added to the near field; results go to the
+//      original order; then the local expansion at every target (L2P) is
+//      added to them.
 // The far field uses the singular kernel, as FLOWVPM's nonzero_sigma=false;
 // sigma_factor keeps regularised pairs out of it (Gaussian-erf: beyond 7.1 σ
 // the kernels agree to FP32 rounding).
@@ -77,15 +82,17 @@ struct FmmWork {
   int* counters = nullptr;    // see kCntCells .. kGenBase
   int64_t meta_cap = 0;       // (group, frontier cell) walk slots
   float4* ggeom = nullptr;    // target-group boxes (centre, radius), FP32
-  float4* cgeom = nullptr;    // cell boxes (centre, radius), FP32
-  float* csig = nullptr;      // largest core per cell, FP32
+  float4* cgeom = nullptr;    // walk records, two per cell (see cell_walk_kernel)
   int* front = nullptr;       // frontier cells (walk roots)
   unsigned long long* pairs = nullptr;   // [0] near source pairs, [1] far (target, cell) pairs
   double* box = nullptr;      // bounding cube: min x y z, size
   double* box_part = nullptr; // per-block min/max partials
   // interaction lists
   int *nfar = nullptr, *nnear = nullptr, *ofar = nullptr, *onear = nullptr;
-  int* far_list = nullptr;    // far cell ids per target group
+  int* far_list = nullptr;    // far cell ids per target group (M2P at every target)
+  int *nloc = nullptr, *oloc = nullptr;   // local-expansion list counts, offsets
+  int* loc_list = nullptr;    // far cell ids per target group taken by its local expansion
+  int64_t loc_list_cap = 0;
   int2* near_list = nullptr;  // near source ranges [x, y) per target group
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
@@ -93,15 +100,18 @@ struct FmmWork {
   // statistics of the last evaluation
   int64_t last_cells = 0, last_leaves = 0, last_groups = 0, last_far = 0, last_near = 0;
   int64_t last_nfront = 0, last_n = -1;
-  unsigned long long h_pairs[2] = {0, 0};
+  unsigned long long h_pairs[3] = {0, 0, 0};
+  float* loc = nullptr;       // per target group: 3·ncoef(Q) local coefficients
+  int64_t loc_cap = 0;
 };
 
 void fmm_free(FmmWork* w) {
   if (!w) return;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
                   w->vw, w->lo, w->hi, w->child, w->nchild, w->geom, w->mom, w->momf, w->leaves,
-                  w->ggeom, w->cgeom, w->csig, w->front, w->pairs, w->counters, w->box, w->box_part,
-                  w->nfar, w->nnear, w->ofar, w->onear, w->far_list, w->near_list, w->cub_tmp};
+                  w->ggeom, w->cgeom, w->front, w->pairs, w->counters, w->box, w->box_part,
+                  w->nfar, w->nnear, w->ofar, w->onear, w->far_list, w->near_list, w->cub_tmp,
+                  w->loc, w->nloc, w->oloc, w->loc_list};
   for (void* p : ptrs) cudaFree(p);
   delete w;
 }
@@ -303,8 +313,18 @@ __device__ __forceinline__ void cell_centre(const double* g, double& cx, double&
   r = sqrt(ex * ex + ey * ey + ez * ez);
 }
 
+// Binomial coefficients C(n, k) for n, k <= 6 (the largest order is 6), as a
+// table: the moment shift's loops are too large to unroll completely, and a
+// binomial formed at run time costs integer divisions in its innermost loop.
+__constant__ double c_binom[7][7] = {
+    {1, 0, 0, 0, 0, 0, 0},   {1, 1, 0, 0, 0, 0, 0},    {1, 2, 1, 0, 0, 0, 0},
+    {1, 3, 3, 1, 0, 0, 0},   {1, 4, 6, 4, 1, 0, 0},    {1, 5, 10, 10, 5, 1, 0},
+    {1, 6, 15, 20, 15, 6, 1}};
+
 // Cells of generation g: leaves from their particles, parents from their
-// children (which belong to later generations, already done).
+// children (which belong to later generations, already done).  One thread per
+// (cell, vorticity component m): the three threads of a cell form the same box;
+// the one with m = 0 writes it.
 template <int P>
 __global__ void tree_upward_kernel(int g, const int* __restrict__ counters, const int* __restrict__ lo,
                                    const int* __restrict__ hi, const int* __restrict__ child,
@@ -312,12 +332,15 @@ __global__ void tree_upward_kernel(int g, const int* __restrict__ counters, cons
                                    int64_t ldw, double* geom, double* mom) {
   constexpr int NC = ncoef(P);
   const int begin = counters[kGenBase + g], end = counters[kGenBase + g + 1];
-  for (int cell = begin + int(blockIdx.x * blockDim.x + threadIdx.x); cell < end;
-       cell += int(gridDim.x * blockDim.x)) {
+  const int64_t nwork = int64_t(end - begin) * 3;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < nwork;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int cell = begin + int(t / 3), m = int(t % 3);
     double* gc = geom + int64_t(cell) * kGeom;
     const int nc = nchild[cell];
     double bx[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
     double smax = 0.0;
+    bool bad = false;
     if (nc == 0) {
       for (int i = lo[cell]; i < hi[cell]; ++i) {
 #pragma unroll
@@ -332,6 +355,7 @@ __global__ void tree_upward_kernel(int g, const int* __restrict__ counters, cons
       for (int k = 0; k < nc; ++k) {
         if (child[cell] + k >= counters[kCntCells]) {
           atomicOr(const_cast<int*>(&counters[kCntFlags]), 32);
+          bad = true;
           break;
         }
         const double* gk = geom + int64_t(child[cell] + k) * kGeom;
@@ -343,57 +367,60 @@ __global__ void tree_upward_kernel(int g, const int* __restrict__ counters, cons
         smax = fmax(smax, gk[6]);
       }
     }
+    if (m == 0) {
 #pragma unroll
-    for (int d = 0; d < 6; ++d) gc[d] = bx[d];
-    gc[6] = smax;
-    gc[7] = 0.0;
-    double cx, cy, cz, rad;
-    cell_centre(gc, cx, cy, cz, rad);
-    double* mc = mom + int64_t(cell) * 3 * NC;
-    for (int m = 0; m < 3; ++m) {
-      double acc[NC];
-#pragma unroll
-      for (int k = 0; k < NC; ++k) acc[k] = 0.0;
-      if (nc == 0) {
-        for (int i = lo[cell]; i < hi[cell]; ++i) {
-          double pw[NC];
-          monomials<P, double>(sorted[i] - cx, sorted[ldw + i] - cy, sorted[2 * ldw + i] - cz, pw);
-          const double gm = sorted[(3 + m) * ldw + i];
-#pragma unroll
-          for (int k = 0; k < NC; ++k) acc[k] += gm * pw[k];
-        }
-      } else {
-        for (int q = 0; q < nc; ++q) {
-          const int ch = child[cell] + q;
-          double qx, qy, qz, qr;
-          cell_centre(geom + int64_t(ch) * kGeom, qx, qy, qz, qr);
-          double tp[NC];
-          monomials<P, double>(qx - cx, qy - cy, qz - cz, tp);
-          const double* mq = mom + int64_t(ch) * 3 * NC + m * NC;
-          // (y - c)^k = Σ_{j<=k} C(k, j) (y - c_q)^j (c_q - c)^{k-j}
-#pragma unroll
-          for (int n = 0; n <= P; ++n)
-#pragma unroll
-            for (int a = n; a >= 0; --a)
-#pragma unroll
-              for (int b = n - a; b >= 0; --b) {
-                const int c = n - a - b;
-                double s = 0.0;
-#pragma unroll
-                for (int ja = 0; ja <= a; ++ja)
-#pragma unroll
-                  for (int jb = 0; jb <= b; ++jb)
-#pragma unroll
-                    for (int jc = 0; jc <= c; ++jc)
-                      s += double(binom(a, ja) * binom(b, jb) * binom(c, jc)) *
-                           tp[midx(a - ja, b - jb, c - jc)] * mq[midx(ja, jb, jc)];
-                acc[midx(a, b, c)] += s;
-              }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < NC; ++k) mc[m * NC + k] = acc[k];
+      for (int d = 0; d < 6; ++d) gc[d] = bx[d];
+      gc[6] = smax;
+      gc[7] = 0.0;
     }
+    double cx, cy, cz, rad;
+    {
+      double b8[8] = {bx[0], bx[1], bx[2], bx[3], bx[4], bx[5], smax, 0.0};
+      cell_centre(b8, cx, cy, cz, rad);
+    }
+    double* mc = mom + int64_t(cell) * 3 * NC;
+    double acc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+    if (nc == 0) {
+      for (int i = lo[cell]; i < hi[cell]; ++i) {
+        double pw[NC];
+        monomials<P, double>(sorted[i] - cx, sorted[ldw + i] - cy, sorted[2 * ldw + i] - cz, pw);
+        const double gm = sorted[(3 + m) * ldw + i];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) acc[k] += gm * pw[k];
+      }
+    } else if (!bad) {
+      for (int q = 0; q < nc; ++q) {
+        const int ch = child[cell] + q;
+        double qx, qy, qz, qr;
+        cell_centre(geom + int64_t(ch) * kGeom, qx, qy, qz, qr);
+        double tp[NC];
+        monomials<P, double>(qx - cx, qy - cy, qz - cz, tp);
+        const double* mq = mom + int64_t(ch) * 3 * NC + m * NC;
+        // (y - c)^k = Σ_{j<=k} C(k, j) (y - c_q)^j (c_q - c)^{k-j}
+#pragma unroll
+        for (int n = 0; n <= P; ++n)
+#pragma unroll
+          for (int a = n; a >= 0; --a)
+#pragma unroll
+            for (int b = n - a; b >= 0; --b) {
+              const int c = n - a - b;
+              double s = 0.0;
+#pragma unroll
+              for (int ja = 0; ja <= a; ++ja)
+#pragma unroll
+                for (int jb = 0; jb <= b; ++jb)
+#pragma unroll
+                  for (int jc = 0; jc <= c; ++jc)
+                    s += c_binom[a][ja] * c_binom[b][jb] * c_binom[c][jc] *
+                         tp[midx(a - ja, b - jb, c - jc)] * mq[midx(ja, jb, jc)];
+              acc[midx(a, b, c)] += s;
+            }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) mc[m * NC + k] = acc[k];
   }
 }
 
@@ -428,15 +455,25 @@ __global__ void group_geom_kernel(int64_t n, const double* __restrict__ sorted, 
   ggeom[g] = make_float4(float(cx), float(cy), float(cz), float(r + pad));
 }
 
-__global__ void cell_geom_f32_kernel(int ncells, const double* __restrict__ geom, float4* cgeom,
-                                     float* csig) {
+// Walk record of cell c, two float4 read together by the traversal:
+//   rec[2c]     = centre x, y, z and radius (FP32, inflated as above);
+//   rec[2c + 1] = largest core (FP32), then as integer bits: the first child
+//                 (or the first particle of a leaf), the end of a leaf's
+//                 particle range, the number of children (0 for a leaf).
+__global__ void cell_walk_kernel(int ncells, const double* __restrict__ geom,
+                                 const int* __restrict__ lo, const int* __restrict__ hi,
+                                 const int* __restrict__ child, const int* __restrict__ nchild,
+                                 float4* rec) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   double cx, cy, cz, r;
   cell_centre(geom + int64_t(c) * kGeom, cx, cy, cz, r);
   const double pad = 1e-6 * (fabs(cx) + fabs(cy) + fabs(cz) + r);
-  cgeom[c] = make_float4(float(cx), float(cy), float(cz), float(r + pad));
-  csig[c] = float(geom[int64_t(c) * kGeom + 6]);
+  rec[2 * c] = make_float4(float(cx), float(cy), float(cz), float(r + pad));
+  const int nc = nchild[c];
+  rec[2 * c + 1] = make_float4(float(geom[int64_t(c) * kGeom + 6]),
+                               __int_as_float(nc == 0 ? lo[c] : child[c]), __int_as_float(hi[c]),
+                               __int_as_float(nc));
 }
 
 // One thread per (target group g, frontier cell j), t = g·nfront + j: the
@@ -446,13 +483,12 @@ __global__ void cell_geom_f32_kernel(int ncells, const double* __restrict__ geom
 // Near leaves that continue the previous near range in Morton order extend it.
 template <bool FILL>
 __global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restrict__ front,
-                                const float4* __restrict__ ggeom, const float4* __restrict__ cgeom,
-                                const float* __restrict__ csig, const int* __restrict__ lo,
-                                const int* __restrict__ hi, const int* __restrict__ child,
-                                const int* __restrict__ nchild, float theta, float sfac, int* nfar,
-                                int* nnear, const int* __restrict__ ofar,
-                                const int* __restrict__ onear, int* far_list, int2* near_list,
-                                int* counters, int ncells) {
+                                const float4* __restrict__ ggeom, const float4* __restrict__ walk,
+                                float theta, float sfac, int mark_local, int* nfar,
+                                int* nnear, int* nloc, const int* __restrict__ ofar,
+                                const int* __restrict__ onear, const int* __restrict__ oloc,
+                                int* far_list, int2* near_list, int* loc_list, int* counters,
+                                int ncells) {
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= nthreads) return;
   const int64_t g = t / nfront;
@@ -460,30 +496,37 @@ __global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restr
   int stack[kStack];
   int sp = 0;
   stack[sp++] = front[t % nfront];
-  int cf = 0, cn = 0, last_hi = -1;
-  const int of = FILL ? ofar[t] : 0, on = FILL ? onear[t] : 0;
+  int cf = 0, cn = 0, cl = 0, last_hi = -1;
+  const int of = FILL ? ofar[t] : 0, on = FILL ? onear[t] : 0, ol = FILL && mark_local ? oloc[t] : 0;
   while (sp > 0) {
     const int s = stack[--sp];
     if (s < 0 || s >= ncells) {
       atomicOr(&counters[kCntFlags], 16);
       break;
     }
-    const float4 cs = cgeom[s];
+    const float4 cs = walk[2 * s], ck = walk[2 * s + 1];
+    const int first = __float_as_int(ck.y), end = __float_as_int(ck.z), nc = __float_as_int(ck.w);
     const float dx = tg.x - cs.x, dy = tg.y - cs.y, dz = tg.z - cs.z;
     const float d = sqrtf(dx * dx + dy * dy + dz * dz);
-    if (tg.w + cs.w < theta * d && d - tg.w - cs.w >= sfac * csig[s]) {
-      if (FILL) far_list[of + cf] = s;
-      ++cf;
-    } else if (nchild[s] == 0) {
-      if (cn > 0 && lo[s] == last_hi) {
-        if (FILL) near_list[on + cn - 1].y = hi[s];
+    if (tg.w + cs.w < theta * d && d - tg.w - cs.w >= sfac * ck.x) {
+      // Cells at least as large as the group go to its local expansion.
+      if (mark_local && cs.w >= tg.w) {
+        if (FILL) loc_list[ol + cl] = s;
+        ++cl;
       } else {
-        if (FILL) near_list[on + cn] = make_int2(lo[s], hi[s]);
+        if (FILL) far_list[of + cf] = s;
+        ++cf;
+      }
+    } else if (nc == 0) {
+      if (cn > 0 && first == last_hi) {
+        if (FILL) near_list[on + cn - 1].y = end;
+      } else {
+        if (FILL) near_list[on + cn] = make_int2(first, end);
         ++cn;
       }
-      last_hi = hi[s];
+      last_hi = end;
     } else {
-      const int c0 = child[s], nc = nchild[s];
+      const int c0 = first;
       if (sp + nc > kStack) {   // cannot happen for 21 Morton levels (7·21 + 1 entries)
         atomicOr(&counters[kCntFlags], 2);
         break;
@@ -494,6 +537,7 @@ __global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restr
   if (!FILL) {
     nfar[t] = cf;
     nnear[t] = cn;
+    if (mark_local) nloc[t] = cl;
   }
 }
 
@@ -531,11 +575,11 @@ constexpr int kNearFoldSources = 256;   // sources a thread sums in FP32 between
 
 template <int PASS>
 struct NearShape {
-  // The U/J passes hold 15 (27 with DJ) sums per target: two targets per
-  // thread keep their registers and fold pairs within three or more CTAs per
-  // SM (four targets need more than the 168 registers of three CTAs and spill);
-  // the ζ passes (6 or 12 sums) take four.
-  static constexpr int T = (PASS == PASS_UJ || PASS == PASS_UJD) ? 2 : 4;
+  // Targets per thread.  U/J: four, at three CTAs per SM (168 registers, of
+  // which the pass spills 192 bytes; measured at N = 1M it is still 4 % faster
+  // than two targets at four CTAs).  U/J + DJ holds 27 sums per target: two.
+  // The ζ passes (6 or 12 sums): four.
+  static constexpr int T = PASS == PASS_UJD ? 2 : 4;
   static constexpr int TQ = kTreeBlock / T;
   static constexpr int SL = kNearThreads / TQ;
   static constexpr int NV = nval_of(PASS);
@@ -544,7 +588,7 @@ struct NearShape {
   static constexpr size_t kQuadBytes = size_t(kNearThreads) * QUADS * sizeof(float4);
   static constexpr size_t kFoldBytes = size_t(kNearThreads) * T * NV * 2 * sizeof(float);
   static constexpr size_t kSmem = kQuadBytes + kFoldBytes;
-  static constexpr int kMinBlocks = (PASS == PASS_UJD || PASS == PASS_ZETAD) ? 3 : 4;
+  static constexpr int kMinBlocks = PASS == PASS_ZETA ? 4 : 3;
 };
 
 template <int KERNEL, int PASS>
@@ -843,10 +887,240 @@ __global__ void __launch_bounds__(kTreeBlock) near_f64_kernel(
   }
 }
 
+// ------------------------------------------------------------ local expansions --
+// Far cells at least as large as their target group are marked in the far
+// list as ~s (negative) when local expansions are on: m2l_kernel turns them
+// into the group's local expansion (tree.cuh), far_kernel evaluates it at each
+// target (L2P) and skips them in its M2P loop.
+constexpr int kLocalOrder = 7;   // Q for P = 4: L2P within a few per cent of M2P in J (tree.cuh)
+
+// One warp per target group.  The group's local-expansion cells are taken
+// kM2lChunk at a time; then
+//   1. each of the first kM2lChunk lanes forms its cell's ρ, s and powers, and
+//      B̃_j for |j| <= P + Q (one shared-memory row per cell);
+//   2. the warp loads the chunk's moments coalesced and scales them by
+//      ρ^{|k|}/k!;
+//   3. lane l accumulates the local coefficients n = l + 32·q over the chunk's
+//      cells, Σ_k M̃_k B̃_{k+n} times ρ(-s)^{|n|}/n!, two coefficients per
+//      packed FP32 instruction.
+// The group's coefficients go to loc[g·3·NQ + m·NQ + n].  Chunks of 16 cells
+// keep the shared memory of a warp near 33 KB (six warps per SM).
+constexpr int kM2lChunk = 16;
+
+template <int P, int Q>
+struct M2lShape {
+  static constexpr int NC = ncoef(P), NQ = ncoef(Q), NB = ncoef(P + Q);
+  static constexpr int ROW = NB % 2 ? NB : NB + 1;        // odd stride: lanes' rows hit distinct banks
+  static constexpr int NPOW = (P + 1) + (Q + 1);          // ρ^0..ρ^P, then ρ(-s)^0..ρ(-s)^Q
+  static constexpr int SLOTS = (NQ + 31) / 32;            // coefficients per lane
+  static constexpr size_t kSmem = size_t(kM2lChunk) * ROW * sizeof(float) +
+                                  size_t(kM2lChunk) * NC * sizeof(float4) +
+                                  size_t(kM2lChunk) * NPOW * sizeof(float);
+  static_assert(SLOTS % 2 == 0, "coefficient slots are packed in pairs");
+};
+
+__device__ __forceinline__ void decode_midx(int j, int& a, int& b, int& c) {
+  int n = 0;
+  while (ncoef(n) <= j) ++n;
+  int r = j - (n > 0 ? ncoef(n - 1) : 0);
+  a = n;
+  while (r >= n - a + 1) {
+    r -= n - a + 1;
+    --a;
+  }
+  b = n - a - r;
+  c = n - a - b;
+}
+
+__device__ __forceinline__ float inv_fact3(int a, int b, int c) {
+  float f = 1.f;
+  for (int i = 2; i <= a; ++i) f *= float(i);
+  for (int i = 2; i <= b; ++i) f *= float(i);
+  for (int i = 2; i <= c; ++i) f *= float(i);
+  return 1.f / f;
+}
+
+template <int P, int Q>
+__global__ void __launch_bounds__(32) m2l_kernel(int nfront, const int* __restrict__ oloc,
+                                                 const int* __restrict__ nloc,
+                                                 const int* __restrict__ loc_list,
+                                                 const double* __restrict__ geom,
+                                                 const float* __restrict__ momf,
+                                                 const float4* __restrict__ ggeom, int ncells,
+                                                 float* __restrict__ loc, int* counters) {
+  using Sh = M2lShape<P, Q>;
+  constexpr int NC = Sh::NC, NQ = Sh::NQ, ROW = Sh::ROW, NPOW = Sh::NPOW, SLOTS = Sh::SLOTS;
+  constexpr int CH = kM2lChunk, H = SLOTS / 2;
+  extern __shared__ __align__(16) unsigned char m2l_smem[];
+  float4* sM = reinterpret_cast<float4*>(m2l_smem);                            // [cell][k]
+  float* sB = reinterpret_cast<float*>(m2l_smem + size_t(CH) * NC * sizeof(float4));   // [cell][j]
+  float* sP = sB + CH * ROW;                                                     // [cell][NPOW]
+  __shared__ int ids[CH];
+  const int lane = threadIdx.x;
+  const int g = blockIdx.x;
+  const float4 tg = ggeom[g];
+  const double zx = tg.x, zy = tg.y, zz = tg.z;
+  const double h = tg.w;
+
+  // This lane's local coefficients n = lane + 32·q: index tables of k + n.
+  int t3[SLOTS][P + 1], t2[SLOTS][P + 1], ncs[SLOTS], nord[SLOTS];
+  float invf[SLOTS];
+#pragma unroll
+  for (int q = 0; q < SLOTS; ++q) {
+    const int n = lane + 32 * q;
+    int na = 0, nb = 0, nc = 0;
+    if (n < NQ) decode_midx(n, na, nb, nc);
+    const int nn = na + nb + nc;
+    ncs[q] = nc;
+    nord[q] = nn;
+    invf[q] = n < NQ ? inv_fact3(na, nb, nc) : 0.f;
+#pragma unroll
+    for (int K = 0; K <= P; ++K) {
+      const int N = K + nn;
+      t3[q][K] = N * (N + 1) * (N + 2) / 6;
+      const int M = K + nb + nc;
+      t2[q][K] = M * (M + 1) / 2;
+    }
+  }
+  // The moment elements e = lane + 32·i of a cell row this lane scales.
+  constexpr int NE = (3 * NC + 31) / 32;
+  int eord[NE];
+  float efac[NE];
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const int e = lane + 32 * i;
+    int a = 0, b = 0, c = 0;
+    if (e < 3 * NC) decode_midx(e % NC, a, b, c);
+    eord[i] = a + b + c;
+    efac[i] = inv_fact3(a, b, c);
+  }
+
+  float Lacc[SLOTS][3];
+#pragma unroll
+  for (int q = 0; q < SLOTS; ++q) Lacc[q][0] = Lacc[q][1] = Lacc[q][2] = 0.f;
+
+  const int64_t t0s = int64_t(g) * nfront, t1s = t0s + nfront - 1;
+  const int f0 = oloc[t0s], fn = oloc[t1s] + nloc[t1s] - f0;
+  for (int base = 0; base < fn; base += CH) {
+    const int cnt = min(CH, fn - base);
+    if (lane < cnt) {
+      int cell = loc_list[f0 + base + lane];
+      if (cell < 0 || cell >= ncells) {   // a list entry outside the tree: record, skip
+        atomicOr(&counters[kCntFlags], 4);
+        cell = -1;
+      }
+      ids[lane] = cell;
+    }
+    __syncwarp();
+    // 1. this lane's cell: scale factors and B̃ row.
+    if (lane < CH) {
+      const int cell = lane < cnt ? ids[lane] : -1;
+      double rho = 0.0;
+      float rx = 1.f, ry = 0.f, rz = 0.f;
+      if (cell >= 0) {
+        double cx, cy, cz, cr;
+        cell_centre(geom + int64_t(cell) * kGeom, cx, cy, cz, cr);
+        const double dx = zx - cx, dy = zy - cy, dz = zz - cz;
+        rho = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+        rx = float(dx * rho); ry = float(dy * rho); rz = float(dz * rho);
+      }
+      float* pw = sP + lane * NPOW;
+      float v = 1.f;
+#pragma unroll
+      for (int j = 0; j <= P; ++j) {
+        pw[j] = v;
+        v *= float(rho);
+      }
+      const float ns = -float(h * rho);
+      v = float(rho);
+#pragma unroll
+      for (int j = 0; j <= Q; ++j) {
+        pw[P + 1 + j] = v;
+        v *= ns;
+      }
+      scaled_taylor_unit<P + Q>(rx, ry, rz, sB + lane * ROW);
+    }
+    __syncwarp();
+    // 2. moments of the chunk's cells, coalesced, scaled by ρ^{|k|}/k!.
+    for (int c = 0; c < cnt; ++c) {
+      const int cell = ids[c];
+      const float* row = momf + int64_t(cell < 0 ? 0 : cell) * 3 * NC;
+      const float* pw = sP + c * NPOW;
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        const int e = lane + 32 * i;
+        if (e < 3 * NC) {
+          const int m = e / NC, k = e % NC;
+          reinterpret_cast<float*>(&sM[c * NC + k])[m] =
+              cell < 0 ? 0.f : row[e] * pw[eord[i]] * efac[i];
+        }
+      }
+    }
+    __syncwarp();
+    // 3. local coefficients, slots (2h, 2h + 1) packed.
+    for (int c = 0; c < cnt; ++c) {
+      const float* brow = sB + c * ROW;
+      const float4* mrow = sM + c * NC;
+      float2 acc[H][3];
+#pragma unroll
+      for (int q = 0; q < H; ++q) acc[q][0] = acc[q][1] = acc[q][2] = bc2(0.f);
+#pragma unroll
+      for (int n = 0; n <= P; ++n)
+#pragma unroll
+        for (int a = n; a >= 0; --a)
+#pragma unroll
+          for (int b = n - a; b >= 0; --b) {
+            const int cc = n - a - b;
+            const float4 mk = mrow[midx(a, b, cc)];
+            const float2 m0 = bc2(mk.x), m1 = bc2(mk.y), m2 = bc2(mk.z);
+#pragma unroll
+            for (int q = 0; q < H; ++q) {
+              const float2 bv =
+                  make_float2(brow[t3[2 * q][n] + t2[2 * q][b + cc] + cc + ncs[2 * q]],
+                              brow[t3[2 * q + 1][n] + t2[2 * q + 1][b + cc] + cc + ncs[2 * q + 1]]);
+              acc[q][0] = fma2(m0, bv, acc[q][0]);
+              acc[q][1] = fma2(m1, bv, acc[q][1]);
+              acc[q][2] = fma2(m2, bv, acc[q][2]);
+            }
+          }
+      const float* pw = sP + c * NPOW + P + 1;
+#pragma unroll
+      for (int q = 0; q < H; ++q) {
+        const float fa = pw[nord[2 * q]] * invf[2 * q], fb2 = pw[nord[2 * q + 1]] * invf[2 * q + 1];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          Lacc[2 * q][m] = fmaf(fa, acc[q][m].x, Lacc[2 * q][m]);
+          Lacc[2 * q + 1][m] = fmaf(fb2, acc[q][m].y, Lacc[2 * q + 1][m]);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  float* out = loc + int64_t(g) * 3 * NQ;
+#pragma unroll
+  for (int q = 0; q < SLOTS; ++q) {
+    const int n = lane + 32 * q;
+    if (n < NQ) {
+      out[n] = Lacc[q][0];
+      out[NQ + n] = Lacc[q][1];
+      out[2 * NQ + n] = Lacc[q][2];
+    }
+  }
+}
+
 // ---------------------------------------------------------------- far field --
-// One thread per target (CTA per target group): moments of the group's far
-// cells at the target, plus the near-field raw sums; U and J are written at
-// the target's original index.
+// One thread per target (CTA per target group): the moments of the group's far
+// cells at the target (M2P; the cells of the group's local expansion are on
+// their own list, and l2p_kernel adds them afterwards), plus the near-field
+// raw sums; U and J are written at the target's original index.
+// The group's far cells are taken kFarChunk at a time: the CTA stages their
+// moments and centres in shared memory with coalesced loads, then every thread
+// reads them from there (broadcast) for its target.
+template <int P, typename M>
+__host__ __device__ constexpr int far_chunk() {
+  return 12288 / int(3 * ncoef(P) * sizeof(M)) > 0 ? 12288 / int(3 * ncoef(P) * sizeof(M)) : 1;
+}
+
 template <int P, int KERNEL, typename R, typename M, bool D>
 __global__ void __launch_bounds__(kTreeBlock) far_kernel(
     int64_t n, int nfront,
@@ -855,30 +1129,50 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
     int64_t ldw, const double* __restrict__ raw, int64_t ldr, const int* __restrict__ perm,
     double* U, double* J, double* DJ, int64_t ldo, int ncells, int* counters,
     unsigned long long* pairs) {
-  constexpr int NC = ncoef(P);
+  constexpr int NC = ncoef(P), ROWM = 3 * NC, FCH = far_chunk<P, M>();
+  __shared__ M smom[FCH * ROWM];
+  __shared__ double sctr[FCH][3];
   const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
   const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
   const int f0 = ofar[t0s], fn = ofar[t1s] + nfar[t1s] - f0;
   if (threadIdx.x == 0) atomicAdd(&pairs[1], (unsigned long long)fn * (unsigned long long)(b - a));
-  for (int i = a + int(threadIdx.x); i < b; i += kTreeBlock) {
-    const double x = sorted[i], y = sorted[ldw + i], z = sorted[2 * ldw + i];
+  static_assert(kTreeBlock == 64, "one target per thread");
+  const int i = a + int(threadIdx.x);
+  const bool active = i < b;
+  {
+    const int ii = active ? i : a;
+    const double x = sorted[ii], y = sorted[ldw + ii], z = sorted[2 * ldw + ii];
     R dp[9], dd[18];
 #pragma unroll
     for (int k = 0; k < 9; ++k) dp[k] = R(0);
 #pragma unroll
     for (int k = 0; k < 18; ++k) dd[k] = R(0);
-    for (int f = 0; f < fn; ++f) {
-      const int s = far_list[f0 + f];
-      if (s < 0 || s >= ncells) {   // a list entry outside the tree: record, skip
-        atomicOr(&counters[kCntFlags], 4);
-        continue;
+    for (int c0 = 0; c0 < fn; c0 += FCH) {
+      const int cnt = min(FCH, fn - c0);
+      __syncthreads();   // previous chunk consumed
+      for (int e = int(threadIdx.x); e < cnt * ROWM; e += kTreeBlock) {
+        const int c = e / ROWM, k = e - c * ROWM;
+        const int s = far_list[f0 + c0 + c];
+        smom[e] = (s < 0 || s >= ncells) ? M(0) : mom[int64_t(s) * ROWM + k];
       }
-      double sx, sy, sz, sr;
-      cell_centre(geom + int64_t(s) * kGeom, sx, sy, sz, sr);
-      R bk[ncoef(P + 2)];
-      taylor_coefficients<P + 2, R>(R(x - sx), R(y - sy), R(z - sz), bk);
-      m2p_accumulate<P, R, M>(bk, mom + int64_t(s) * 3 * NC, dp, dd);
+      for (int c = int(threadIdx.x); c < cnt; c += kTreeBlock) {
+        const int s = far_list[f0 + c0 + c];
+        double sx = 1e18, sy = 0.0, sz = 0.0, sr;   // far away: finite, negligible terms
+        if (s < 0 || s >= ncells) {   // a list entry outside the tree: record, skip (zero moments)
+          atomicOr(&counters[kCntFlags], 4);
+        } else {
+          cell_centre(geom + int64_t(s) * kGeom, sx, sy, sz, sr);
+        }
+        sctr[c][0] = sx; sctr[c][1] = sy; sctr[c][2] = sz;
+      }
+      __syncthreads();
+      for (int c = 0; c < cnt; ++c) {
+        R bk[ncoef(P + 2)];
+        taylor_coefficients<P + 2, R>(R(x - sctr[c][0]), R(y - sctr[c][1]), R(z - sctr[c][2]), bk);
+        m2p_accumulate<P, R, M>(bk, smom + c * ROWM, dp, dd);
+      }
     }
+    if (!active) return;
     R uf[3], jf[9];
     curl_from_potential<R>(dp, dd, uf, jf);
     double v[15];
@@ -907,6 +1201,37 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
   }
 }
 
+// L2P: the group's local expansion at each of its targets, added to U and J
+// (after far_kernel wrote them) at the target's original index.  A kernel of
+// its own: inside far_kernel its registers would cut the M2P loop's occupancy.
+template <int Q>
+__global__ void __launch_bounds__(kTreeBlock) l2p_kernel(int64_t n, const float4* __restrict__ ggeom,
+                                                        const float* __restrict__ loc,
+                                                        const double* __restrict__ sorted,
+                                                        int64_t ldw, const int* __restrict__ perm,
+                                                        double* U, double* J, int64_t ldo) {
+  const int64_t i = int64_t(blockIdx.x) * kTreeBlock + threadIdx.x;
+  if (i >= n) return;
+  const float4 tg = ggeom[blockIdx.x];
+  const double ih = 1.0 / double(tg.w);
+  float dp[9], dd[18];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) dp[k] = 0.f;
+#pragma unroll
+  for (int k = 0; k < 18; ++k) dd[k] = 0.f;
+  l2p_accumulate<Q, float>(loc + int64_t(blockIdx.x) * 3 * ncoef(Q),
+                           float((sorted[i] - double(tg.x)) * ih),
+                           float((sorted[ldw + i] - double(tg.y)) * ih),
+                           float((sorted[2 * ldw + i] - double(tg.z)) * ih), float(ih), dp, dd);
+  float uf[3], jf[9];
+  curl_from_potential<float>(dp, dd, uf, jf);
+  const int64_t o = perm[i];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) U[k * ldo + o] += kInv4Pi * double(uf[k]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) J[k * ldo + o] += kInv4Pi * double(jf[k]);
+}
+
 // ------------------------------------------------------------------- host --
 namespace {
 
@@ -927,8 +1252,8 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   const int64_t cells = 2 * cap + 8;
   void* ptrs[] = {w->codes, w->codes_alt, w->idx, w->perm, w->sorted, w->rec, w->near_raw,
                   w->vw, w->lo, w->hi, w->child, w->nchild, w->geom, w->leaves, w->ggeom, w->cgeom,
-                  w->csig, w->front, w->pairs, w->counters, w->box, w->box_part, w->nfar, w->nnear,
-                  w->ofar, w->onear, w->cub_tmp};
+                  w->front, w->pairs, w->counters, w->box, w->box_part, w->nfar, w->nnear,
+                  w->ofar, w->onear, w->nloc, w->oloc, w->cub_tmp};
   for (void* p : ptrs) cudaFree(p);
   cudaError_t e = cudaSuccess;
   auto al = [&](auto*& p, size_t count) {
@@ -940,10 +1265,11 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
   al(w->lo, cells); al(w->hi, cells); al(w->child, cells); al(w->nchild, cells);
   const int64_t meta = (cap / kTreeBlock + 2) * kMaxFront;
   al(w->geom, size_t(cells) * kGeom); al(w->leaves, cells);
-  al(w->ggeom, cap / kTreeBlock + 2); al(w->cgeom, cells); al(w->csig, cells);
-  al(w->front, kMaxFront); al(w->pairs, 2);
+  al(w->ggeom, cap / kTreeBlock + 2); al(w->cgeom, 2 * size_t(cells));
+  al(w->front, kMaxFront); al(w->pairs, 3);
   al(w->counters, kNumCounters); al(w->box, 4); al(w->box_part, kBoxBlocks * 6);
   al(w->nfar, meta); al(w->nnear, meta); al(w->ofar, meta); al(w->onear, meta);
+  al(w->nloc, meta); al(w->oloc, meta);
   if (e != cudaSuccess) {
     w->cap = 0;
     return e;
@@ -968,21 +1294,36 @@ cudaError_t reserve_particles(FmmWork* w, int64_t n) {
 
 template <int P>
 void launch_upward(FmmWork* w, int g, int ncells_in_gen, int64_t ldw, cudaStream_t st) {
-  const int grid = std::max(1, std::min((ncells_in_gen + 63) / 64, 4096));
+  const int grid = std::max(1, std::min((3 * ncells_in_gen + 63) / 64, 4096));
   tree_upward_kernel<P><<<grid, 64, 0, st>>>(g, w->counters, w->lo, w->hi, w->child, w->nchild,
                                              w->sorted, ldw, w->geom, w->mom);
 }
 
+template <int P, int Q>
+void launch_m2l(FmmWork* w, int ngroups, int nfront, int ncells, cudaStream_t st) {
+  static const bool once = [] {
+    cudaFuncSetAttribute(m2l_kernel<P, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(M2lShape<P, Q>::kSmem));
+    return true;
+  }();
+  (void)once;
+  m2l_kernel<P, Q><<<ngroups, 32, M2lShape<P, Q>::kSmem, st>>>(
+      nfront, w->oloc, w->nloc, w->loc_list, w->geom, w->momf, w->ggeom, ncells, w->loc,
+      w->counters);
+}
+
+// The far field with local expansions where `local` (FP32, p = 4; see
+// fmm_eval), else M2P at every target.
 template <int P>
-cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int64_t n, int ngroups, int nfront,
-                       int ncells, int64_t ldw, double* U, double* J, double* DJ, int64_t ldo,
-                       cudaStream_t st) {
+cudaError_t launch_far(FmmWork* w, int kernel, bool f64, bool local, int64_t n, int ngroups,
+                       int nfront, int ncells, int64_t ldw, double* U, double* J, double* DJ,
+                       int64_t ldo, cudaStream_t st) {
   const dim3 grid(ngroups), block(kTreeBlock);
 #define VPM_FAR(K, R, M, DD, mp)                                                                   \
-  far_kernel<P, K, R, M, DD><<<grid, block, 0, st>>>(n, nfront, w->ofar, w->nfar,                 \
-                                                     w->far_list, w->geom, mp, w->sorted, ldw,    \
-                                                     w->near_raw, ldw, w->perm, U, J, DJ, ldo,    \
-                                                     ncells, w->counters, w->pairs)
+  far_kernel<P, K, R, M, DD><<<grid, block, 0, st>>>(n, nfront, w->ofar, w->nfar, w->far_list,    \
+                                                     w->geom, mp, w->sorted, ldw, w->near_raw, ldw, \
+                                                     w->perm, U, J, DJ, ldo, ncells, w->counters,   \
+                                                     w->pairs)
   if (DJ) {   // FP32 Gaussian-erf only (checked by the caller)
     VPM_FAR(VPM_KERNEL_GAUSSIANERF, float, float, true, w->momf);
   } else if (kernel == VPM_KERNEL_WINCKELMANS) {
@@ -993,12 +1334,18 @@ cudaError_t launch_far(FmmWork* w, int kernel, bool f64, int64_t n, int ngroups,
     else VPM_FAR(VPM_KERNEL_GAUSSIANERF, float, float, false, w->momf);
   }
 #undef VPM_FAR
+  if constexpr (P == 4) {
+    if (local)
+      l2p_kernel<kLocalOrder><<<grid, block, 0, st>>>(n, w->ggeom, w->loc, w->sorted, ldw, w->perm,
+                                                      U, J, ldo);
+  }
   return cudaGetLastError();
 }
 
 }  // namespace
 
 bool fmm_order_supported(int p) { return p == 2 || p == 4 || p == 6; }
+bool fmm_local_order_supported(int q) { return q == 0 || q == kLocalOrder; }
 
 void fmm_stats(const FmmWork* w, int64_t* out) {
   out[0] = w ? w->last_cells : 0;
@@ -1008,13 +1355,14 @@ void fmm_stats(const FmmWork* w, int64_t* out) {
   out[4] = w ? w->last_near : 0;
   out[5] = w ? int64_t(w->h_pairs[0]) : 0;
   out[6] = w ? int64_t(w->h_pairs[1]) : 0;
+  out[7] = w ? int64_t(w->h_pairs[2]) : 0;
 }
 
 // U and J of every particle of the context by the treecode (see the header).
 // Returns a CUDA error, or cudaErrorInvalidValue with *why set for a tree that
 // outgrew its bounds (cannot happen for the 2n + 8 cells reserved).
 cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double theta,
-                     double sfac, double* dj, const char** why) {
+                     double sfac, int local_order, double* dj, const char** why) {
   *why = nullptr;
   const int64_t n = c->n;
   if (n == 0) return cudaSuccess;
@@ -1025,6 +1373,8 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   cudaStream_t st = c->st;
   const int64_t ldw = w->cap;
   const bool f64 = prec == VPM_PREC_FP64;
+  // Local expansions: FP32 far fields of order-4 moments.
+  const int local = local_order > 0 && p == 4 && !f64;
   // VPM_FMM_SYNC=1: synchronise after every stage so that an error names it.
   static const bool stage_sync = [] {
     const char* v = std::getenv("VPM_FMM_SYNC");
@@ -1136,7 +1486,8 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     if ((e = launched(1)) != cudaSuccess) return e;
   }
 
-  cell_geom_f32_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, w->geom, w->cgeom, w->csig);
+  cell_walk_kernel<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, w->geom, w->lo, w->hi, w->child,
+                                                         w->nchild, w->cgeom);
   group_geom_kernel<<<(ngroups + 127) / 128, 128, 0, st>>>(n, w->sorted, ldw, w->ggeom);
   if ((e = launched(2)) != cudaSuccess) return e;
 
@@ -1144,10 +1495,9 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   stage = "traversal";
   const int tgrid = int((nwalk + 127) / 128);
   traverse_kernel<false><<<tgrid, 128, 0, st>>>(nwalk, nfront, w->front, w->ggeom, w->cgeom,
-                                                w->csig, w->lo, w->hi, w->child, w->nchild,
-                                                float(theta), float(sfac), w->nfar, w->nnear,
-                                                nullptr, nullptr, nullptr, nullptr, w->counters,
-                                                ncells);
+                                                float(theta), float(sfac), local, w->nfar,
+                                                w->nnear, w->nloc, nullptr, nullptr, nullptr,
+                                                nullptr, nullptr, nullptr, w->counters, ncells);
   if ((e = launched(1)) != cudaSuccess) return e;
   bytes = w->cub_bytes;
   e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nfar, w->ofar, int(nwalk), st);
@@ -1155,9 +1505,13 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     bytes = w->cub_bytes;
     e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nnear, w->onear, int(nwalk), st);
   }
+  if (e == cudaSuccess && local) {
+    bytes = w->cub_bytes;
+    e = cub::DeviceScan::ExclusiveSum(w->cub_tmp, bytes, w->nloc, w->oloc, int(nwalk), st);
+  }
   if (e != cudaSuccess) return e;
-  c->launches += 2;
-  int tail[4];
+  c->launches += local ? 3 : 2;
+  int tail[6] = {0, 0, 0, 0, 0, 0};
   e = cudaMemcpyAsync(&tail[0], w->ofar + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&tail[1], w->nfar + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -1165,10 +1519,15 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     e = cudaMemcpyAsync(&tail[2], w->onear + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&tail[3], w->nnear + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && local)
+    e = cudaMemcpyAsync(&tail[4], w->oloc + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && local)
+    e = cudaMemcpyAsync(&tail[5], w->nloc + nwalk - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
   const int64_t nf = int64_t(tail[0]) + tail[1], nn = int64_t(tail[2]) + tail[3];
-  if (nf > INT32_MAX || nn > INT32_MAX) {
+  const int64_t nl = int64_t(tail[4]) + tail[5];
+  if (nf > INT32_MAX || nn > INT32_MAX || nl > INT32_MAX) {
     *why = "treecode interaction lists exceed 2^31 entries";
     return cudaErrorInvalidValue;
   }
@@ -1184,17 +1543,41 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
     if (e != cudaSuccess) return e;
     w->list_cap = need;
   }
+  if (local && std::max<int64_t>(nl, 1) > w->loc_list_cap) {
+    cudaFree(w->loc_list);
+    w->loc_list = nullptr;
+    w->loc_list_cap = 0;
+    e = cudaMalloc(&w->loc_list, std::max<int64_t>(nl, 1) * sizeof(int));
+    if (e != cudaSuccess) return e;
+    w->loc_list_cap = std::max<int64_t>(nl, 1);
+  }
+  e = cudaMemsetAsync(w->pairs, 0, 2 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
   traverse_kernel<true><<<tgrid, 128, 0, st>>>(nwalk, nfront, w->front, w->ggeom, w->cgeom,
-                                               w->csig, w->lo, w->hi, w->child, w->nchild,
-                                               float(theta), float(sfac), w->nfar, w->nnear,
-                                               w->ofar, w->onear, w->far_list, w->near_list,
+                                               float(theta), float(sfac), local, w->nfar,
+                                               w->nnear, w->nloc, w->ofar, w->onear, w->oloc,
+                                               w->far_list, w->near_list, w->loc_list,
                                                w->counters, ncells);
   if ((e = launched(1)) != cudaSuccess) return e;
 
-  // 5. near field, 6. far field + output
+  // 5. local expansions of the groups (M2L)
+  if (local) {
+    stage = "local expansions";
+    constexpr int NQ = ncoef(kLocalOrder);
+    if (int64_t(ngroups) * 3 * NQ > w->loc_cap) {
+      cudaFree(w->loc);
+      w->loc = nullptr;
+      w->loc_cap = 0;
+      e = cudaMalloc(&w->loc, size_t(ngroups) * 3 * NQ * sizeof(float));
+      if (e != cudaSuccess) return e;
+      w->loc_cap = int64_t(ngroups) * 3 * NQ;
+    }
+    launch_m2l<4, kLocalOrder>(w, ngroups, nfront, ncells, st);
+    if ((e = launched(1)) != cudaSuccess) return e;
+  }
+
+  // 6. near field, 7. far field + output
   stage = "near field";
-  e = cudaMemsetAsync(w->pairs, 0, 2 * sizeof(unsigned long long), st);
-  if (e != cudaSuccess) return e;
   if (f64) {
     if (kernel == VPM_KERNEL_WINCKELMANS)
       near_f64_kernel<VPM_KERNEL_WINCKELMANS><<<ngroups, kTreeBlock, 0, st>>>(
@@ -1217,13 +1600,16 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   }
   if ((e = launched(1)) != cudaSuccess) return e;
   if (p == 2)
-    e = launch_far<2>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj, c->ld, st);
+    e = launch_far<2>(w, kernel, f64, local, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj,
+                      c->ld, st);
   else if (p == 4)
-    e = launch_far<4>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj, c->ld, st);
+    e = launch_far<4>(w, kernel, f64, local, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj,
+                      c->ld, st);
   else
-    e = launch_far<6>(w, kernel, f64, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj, c->ld, st);
+    e = launch_far<6>(w, kernel, f64, local, n, ngroups, nfront, ncells, ldw, c->U, c->J, dj,
+                      c->ld, st);
   stage = "far field";
-  if ((e = e == cudaSuccess ? launched(1) : e) != cudaSuccess) return e;
+  if ((e = e == cudaSuccess ? launched(local ? 2 : 1) : e) != cudaSuccess) return e;
   e = cudaMemcpyAsync(hc, w->counters, sizeof(int) * kGenBase, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(w->h_pairs, w->pairs, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
@@ -1237,7 +1623,8 @@ cudaError_t fmm_eval(vpm_ctx* c, int kernel, int prec, int p, int ncrit, double 
   w->last_leaves = nleaves;
   w->last_groups = ngroups;
   w->last_nfront = nfront;
-  w->last_far = nf;
+  w->last_far = nf + nl;
+  w->h_pairs[2] = (unsigned long long)nl;
   w->last_near = nn;
   w->last_n = n;
   return cudaSuccess;

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace vpm {
 
 // Number of multi-indices with |k| <= q.
@@ -131,6 +133,98 @@ __device__ __forceinline__ void curl_from_potential(const R (&dp)[9], const R (&
     j[0 * 3 + b] = D(b, 1, 2) - D(b, 2, 1);
     j[1 * 3 + b] = D(b, 2, 0) - D(b, 0, 2);
     j[2 * 3 + b] = D(b, 0, 1) - D(b, 1, 0);
+  }
+}
+
+
+// ---------------------------------------------------------- local expansions --
+// A far cell of centre c whose box is at least as large as the target group's
+// (radius h, centre z) is taken once per group as a local expansion of ψ about
+// z instead of once per target (M2P).  With R0 = z - c = |R0| R̂, ρ = 1/|R0|,
+// s = hρ and the homogeneity b_j(R0) = ρ^{|j|+1} b_j(R̂), the expansion
+//   ψ_m(z + y) = Σ_{|n|<=Q} L_n^m (y/h)^n,
+//   L_n^m = ρ (-s)^{|n|} / n! · Σ_{|k|<=P} [M_k^m ρ^{|k|} / k!] [(k+n)! b_{k+n}(R̂)]
+// follows from L_n^m h^{-|n|} = Σ_k M_k^m (-1)^{|n|} C(k+n, n) b_{k+n}(R0)
+// (∂_{R_i} b_k = -(k_i + 1) b_{k+e_i}), with C(k+n, n) = (k+n)!/(k! n!).  Every
+// factor is O(1) in these scaled variables (|R̂| = 1, s < θ), so FP32 holds
+// them for any length unit.  B̃_j = j! b_j(R̂) follows from the recurrence of
+// the header multiplied by j!:
+//   B̃_0 = 1,  |j| B̃_j = (2|j| - 1) Σ_i j_i R̂_i B̃_{j-e_i} - (|j| - 1) Σ_i j_i (j_i - 1) B̃_{j-2e_i}.
+// At a target x = z + h u (L2P), with the 1/(4π) left out as in m2p_accumulate,
+//   ∂_i ψ_m     = (1/h)  Σ_n n_i L_n^m u^{n-e_i},
+//   ∂_i ∂_j ψ_m = (1/h²) Σ_n n_i (n_j - δ_ij) L_n^m u^{n-e_i-e_j}.
+
+// B̃_j (j! b_j at a unit vector) for |j| <= O into out[j] (shared memory), by
+// the recurrence above (unrolled); each order reads the two before it back
+// from out, which holds O(O³) values, more than the registers of a thread.
+template <int O>
+__device__ __forceinline__ void scaled_taylor_unit(float rx, float ry, float rz, float* out) {
+  out[0] = 1.f;
+#pragma unroll
+  for (int n = 1; n <= O; ++n) {
+    const float f1 = float(2 * n - 1) / float(n);
+    const float f2 = float(n - 1) / float(n);
+#pragma unroll
+    for (int a = n; a >= 0; --a)
+#pragma unroll
+      for (int b = n - a; b >= 0; --b) {
+        const int c = n - a - b;
+        float s1 = 0.f, s2 = 0.f;
+        if (a > 0) s1 += float(a) * rx * out[midx(a - 1, b, c)];
+        if (b > 0) s1 += float(b) * ry * out[midx(a, b - 1, c)];
+        if (c > 0) s1 += float(c) * rz * out[midx(a, b, c - 1)];
+        if (a > 1) s2 += float(a * (a - 1)) * out[midx(a - 2, b, c)];
+        if (b > 1) s2 += float(b * (b - 1)) * out[midx(a, b - 2, c)];
+        if (c > 1) s2 += float(c * (c - 1)) * out[midx(a, b, c - 2)];
+        out[midx(a, b, c)] = f1 * s1 - f2 * s2;
+      }
+  }
+}
+
+// L2P: add the derivatives of the local expansion L (L[m·NQ + n], scaled as
+// above) at u = (x - z)/h to dpsi and ddpsi (layouts of m2p_accumulate).  One
+// vorticity component at a time (not unrolled), so that only a third of the
+// coefficients and sums is live at once.
+template <int Q, typename R>
+__device__ __forceinline__ void l2p_accumulate(const float* __restrict__ L, R ux, R uy, R uz,
+                                               R ih, R (&dpsi)[9], R (&ddpsi)[18]) {
+  constexpr int NQ = ncoef(Q);
+  R pw[ncoef(Q - 1)];
+  monomials<Q - 1, R>(ux, uy, uz, pw);
+  const R ih2 = ih * ih;
+#pragma unroll 1
+  for (int m = 0; m < 3; ++m) {
+    const float* Lm = L + m * NQ;
+    R p0 = R(0), p1 = R(0), p2 = R(0);
+    R q00 = R(0), q01 = R(0), q02 = R(0), q11 = R(0), q12 = R(0), q22 = R(0);
+#pragma unroll
+    for (int n = 1; n <= Q; ++n)
+#pragma unroll
+      for (int a = n; a >= 0; --a)
+#pragma unroll
+        for (int b = n - a; b >= 0; --b) {
+          const int c = n - a - b;
+          const R l = R(Lm[midx(a, b, c)]);
+          if (a > 0) p0 += R(a) * pw[midx(a - 1, b, c)] * l;
+          if (b > 0) p1 += R(b) * pw[midx(a, b - 1, c)] * l;
+          if (c > 0) p2 += R(c) * pw[midx(a, b, c - 1)] * l;
+          if (a > 1) q00 += R(a * (a - 1)) * pw[midx(a - 2, b, c)] * l;
+          if (a > 0 && b > 0) q01 += R(a * b) * pw[midx(a - 1, b - 1, c)] * l;
+          if (a > 0 && c > 0) q02 += R(a * c) * pw[midx(a - 1, b, c - 1)] * l;
+          if (b > 1) q11 += R(b * (b - 1)) * pw[midx(a, b - 2, c)] * l;
+          if (b > 0 && c > 0) q12 += R(b * c) * pw[midx(a, b - 1, c - 1)] * l;
+          if (c > 1) q22 += R(c * (c - 1)) * pw[midx(a, b, c - 2)] * l;
+        }
+    // dpsi[3i + m], ddpsi[3s + m] with constant indices in each branch.
+    auto put = [&](auto mm) {
+      constexpr int M = decltype(mm)::value;
+      dpsi[M] += ih * p0; dpsi[3 + M] += ih * p1; dpsi[6 + M] += ih * p2;
+      ddpsi[M] += ih2 * q00; ddpsi[3 + M] += ih2 * q01; ddpsi[6 + M] += ih2 * q02;
+      ddpsi[9 + M] += ih2 * q11; ddpsi[12 + M] += ih2 * q12; ddpsi[15 + M] += ih2 * q22;
+    };
+    if (m == 0) put(std::integral_constant<int, 0>());
+    else if (m == 1) put(std::integral_constant<int, 1>());
+    else put(std::integral_constant<int, 2>());
   }
 }
 

@@ -321,6 +321,8 @@ def run_fmm(args):
     f = Field(X, G, S)
     k = L.KERNEL_GAUSSIANERF
     fm = L.default_fmm()
+    if args.local_order is not None:
+        fm.local_order = args.local_order
     L.check(f.lib.vpm_eval_UJ_fmm(f.p, k, L.PREC_FP32C, ctypes.byref(fm)), f.p)   # warm-up
     ts = []
     for _ in range(3):
@@ -351,12 +353,13 @@ def run_fmm(args):
     U64, J64 = U.cpu().numpy().T, J.cpu().numpy().T.reshape(4096, 3, 3)
     return {"workload": f"helical wake N={n}", "kernel": "gaussianerf", "precision": "fp32c",
             "fmm": {"p": fm.p, "ncrit": fm.ncrit, "theta": fm.theta,
-                    "sigma_factor": fm.sigma_factor},
+                    "sigma_factor": fm.sigma_factor, "local_order": fm.local_order},
             "seconds_fmm": min(ts), "seconds_direct": t_direct,
             "speedup": t_direct / min(ts),
             **stats,
             "near_sources_per_target": stats["near_pairs"] / n,
             "far_cells_per_target": stats["far_evaluations"] / n,
+            "local_cells_per_group": stats["local_terms"] / max(stats["groups"], 1),
             "fmm_rel_l2_U": rel_l2(Uf[idx], U64), "fmm_rel_l2_J": rel_l2(Jf[idx], J64),
             "direct_rel_l2_U": rel_l2(Ud[idx], U64), "direct_rel_l2_J": rel_l2(Jd[idx], J64)}
 
@@ -435,6 +438,8 @@ def main(argv=None):
     p.add_argument("--autotune", action="store_true",
                    help="step, batch: tune the tile shapes first (per size bucket for a batch)")
     p.add_argument("--tree", action="store_true", help="step: U/J passes by the treecode")
+    p.add_argument("--local-order", type=int, default=None,
+                   help="fmm: treecode local expansion order (0: M2P only)")
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,

@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define VPM_ABI_VERSION 2
+#define VPM_ABI_VERSION 3
 
 /* ---------------------------------------------------------------- status -- */
 enum {
@@ -111,6 +111,13 @@ typedef struct vpm_fmm {
                             regularised pairs in the direct near field (7.1: Gaussian-erf
                             cores agree with the singular kernel to FP32 rounding there;
                             0 = as FLOWVPM's nonzero_sigma=false)                         */
+  int32_t local_order;   /* far cells at least as large as the target group (64 consecutive
+                            particles of the Morton order) are taken by one local expansion
+                            of ψ of this order per group (M2L, then L2P at each target),
+                            the others by their moments at every target (M2P); 0 = M2P
+                            for every far cell.  Compiled: 0, 7.  Used with p = 4 and
+                            FP32/FP32C; other settings take M2P throughout (7)          */
+  int32_t reserved;      /* 0 */
 } vpm_fmm;
 
 /* U/J evaluation of the plain pair passes of vpm_step (FLOWUnsteady's vpm_UJ). */
@@ -284,7 +291,8 @@ int vpm_ffv_direct(vpm_ctx* ctx, int kernel, int64_t nb, const double* Xb, int64
                    double* M, int64_t stride_m);
 
 /* ------------------------------------------------------------- treecode -- */
-/* p 4, ncrit 50, theta 0.4 (FLOWUnsteady's defaults), sigma_factor 7.1. */
+/* p 4, ncrit 50, theta 0.4 (FLOWUnsteady's defaults), sigma_factor 7.1,
+ * local_order 7. */
 void vpm_fmm_default(vpm_fmm* f);
 
 /* U and J at every particle of the context by the treecode (replaces
@@ -297,8 +305,9 @@ int vpm_eval_UJ_fmm(vpm_ctx* ctx, int kernel, int precision, const vpm_fmm* fmm)
 
 /* Size of the last treecode evaluation into out[VPM_FMM_STATS]: cells, leaves,
  * target groups, far-cell list entries, near-range list entries, near
- * (target, source) pairs, far (target, cell) evaluations. */
-enum { VPM_FMM_STATS = 7 };
+ * (target, source) pairs, far (target, cell) moment evaluations (M2P), far
+ * (group, cell) local-expansion terms (M2L). */
+enum { VPM_FMM_STATS = 8 };
 int vpm_fmm_stats(const vpm_ctx* ctx, int64_t* out);
 
 /* ------------------------------------------------------------ state files -- */

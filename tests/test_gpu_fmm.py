@@ -1,6 +1,7 @@
 """GPU treecode (vpm_eval_UJ_fmm, the role of FLOWVPM's UJ_fmm): against the
-FP64 oracle's direct sum, its convergence in θ and p, and the near-field limit
-where it must reproduce the direct FP32C sum."""
+FP64 oracle's direct sum, its convergence in θ and p, the near-field limit
+where it must reproduce the direct FP32C sum, and the far field by local
+expansions (M2L, L2P) against the same oracle and against M2P."""
 import ctypes
 
 import numpy as np
@@ -13,9 +14,10 @@ from tests.helpers import Ctx, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def fmm(p=4, ncrit=50, theta=0.4, sigma_factor=7.1):
+def fmm(p=4, ncrit=50, theta=0.4, sigma_factor=7.1, local_order=0):
     f = L.Fmm()
     f.p, f.ncrit, f.theta, f.sigma_factor = p, ncrit, theta, sigma_factor
+    f.local_order = local_order
     return f
 
 
@@ -34,9 +36,56 @@ def stats(c):
     return d["cells"], d["leaves"], d["far_entries"], d["near_entries"]
 
 
+def all_stats(c):
+    out = (ctypes.c_int64 * len(L.FMM_STATS))()
+    c.rc(c.lib.vpm_fmm_stats(c.p, out))
+    return dict(zip(L.FMM_STATS, out))
+
+
 def test_defaults_follow_flowunsteady():
     f = L.default_fmm()
     assert (f.p, f.ncrit, f.theta) == (4, 50, 0.4) and f.sigma_factor == 7.1
+    assert f.local_order == 7
+
+
+@pytest.mark.parametrize("k", [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF])
+def test_local_expansions_match_oracle_and_m2p(oracle, k):
+    # Far cells at least as large as the target group by one local expansion of
+    # order 7 per group: as accurate against the oracle's direct sum as M2P at
+    # every target (within 10 %), with fewer (target, cell) moment evaluations.
+    n = 60000
+    X, G, S = helical_wake(n)
+    idx = np.sort(np.random.default_rng(4).choice(n, 600, replace=False))
+    U0, J0 = oracle.uj_direct(k, X, G, S, Xt=X[idx])
+    with Ctx(n) as c:
+        c.set(X, G, S)
+        Up, Jp = eval_fmm(c, k, L.PREC_FP32C, fmm(local_order=0))
+        sp = all_stats(c)
+        Ul, Jl = eval_fmm(c, k, L.PREC_FP32C, fmm(local_order=7))
+        sl = all_stats(c)
+    assert sp["local_terms"] == 0 and sl["local_terms"] > 0
+    assert sl["far_entries"] == sp["far_entries"]
+    assert sl["far_evaluations"] < sp["far_evaluations"]
+    epu, epj = rel_l2(Up[idx], U0), rel_l2(Jp[idx], J0)
+    elu, elj = rel_l2(Ul[idx], U0), rel_l2(Jl[idx], J0)
+    assert elu <= 1.1 * epu + 1e-7 and elj <= 1.1 * epj + 1e-7, (epu, epj, elu, elj)
+    assert elu <= 1e-4 and elj <= 1e-4
+    # The two far forms differ by the local truncation only.
+    assert rel_l2(Ul, Up) <= 1e-4 and rel_l2(Jl, Jp) <= 1e-4
+
+
+def test_local_expansions_leave_fp64_and_other_orders_on_m2p():
+    # FP64 and p != 4 take M2P throughout: the results are those of local_order 0.
+    X, G, S = helical_wake(12000)
+    with Ctx(12000) as c:
+        c.set(X, G, S)
+        for prec, p in ((L.PREC_FP64, 4), (L.PREC_FP32C, 2)):
+            U0, J0 = eval_fmm(c, 1, prec, fmm(p=p, local_order=0))
+            U1, J1 = eval_fmm(c, 1, prec, fmm(p=p, local_order=7))
+            assert all_stats(c)["local_terms"] == 0
+            assert np.array_equal(U0, U1) and np.array_equal(J0, J1)
+        bad = fmm(local_order=6)
+        assert c.lib.vpm_eval_UJ_fmm(c.p, 1, L.PREC_FP32C, ctypes.byref(bad)) == L.ERR_UNSUPPORTED
 
 
 @pytest.mark.parametrize("k", [L.KERNEL_WINCKELMANS, L.KERNEL_GAUSSIANERF])

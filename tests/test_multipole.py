@@ -80,3 +80,46 @@ def test_local_expansion_reproduces_the_cell_expansion():
     U, J = mp.local_to_target(2, L, z, z)
     U0, J0 = mp.far_field(p, M, c, z)
     assert np.allclose(U, U0, rtol=1e-12, atol=0) and np.allclose(J, J0, rtol=1e-10, atol=1e-14)
+
+
+def _ball(rng, n, r):
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1)[:, None]
+    return v * (r * rng.random(n) ** (1 / 3))[:, None]
+
+
+@pytest.mark.parametrize("ratio", [1.0, 1.5, 2.0, 4.0])
+def test_local_order_7_matches_m2p_for_cells_not_smaller_than_the_group(ratio):
+    # The treecode takes a far cell by the group's local expansion only when the
+    # cell's radius R_s is at least the group's R_t.  At the acceptance limit
+    # R_t + R_s = θ d (θ = 0.4, the worst case; most far cells lie well inside
+    # it), J with local order 7 stays within 1 % of the cell expansion at every
+    # target (M2P, p = 4) from R_s = 1.5 R_t on, and within 25 % at equal radii
+    # (mean over the trials 5 %), where order 6 is up to twice M2P's error.
+    rng = np.random.default_rng(7 + int(10 * ratio))
+    theta, p = 0.4, 4
+    rt = theta / (1.0 + ratio)
+    rs = ratio * rt
+    worst = {6: 0.0, 7: 0.0}
+    for trial in range(4):
+        d = rng.normal(size=3)
+        c = d / np.linalg.norm(d)
+        Y = c + _ball(rng, 40, rs)
+        G = rng.normal(size=(40, 3))
+        X = _ball(rng, 12, rt)
+        M = mp.moments(p, Y, G, c)
+        err = {"m2p": 0.0, 6: 0.0, 7: 0.0}
+        ref = 0.0
+        Ls = {q: mp.local_from_moments(p, q, M, c, np.zeros(3)) for q in (6, 7)}
+        for x in X:
+            _, J0 = mp.direct_singular(Y, G, x)
+            ref += np.sum(J0 ** 2)
+            err["m2p"] += np.sum((mp.far_field(p, M, c, x)[1] - J0) ** 2)
+            for q in (6, 7):
+                err[q] += np.sum((mp.local_to_target(q, Ls[q], np.zeros(3), x)[1] - J0) ** 2)
+        for q in (6, 7):
+            worst[q] = max(worst[q], np.sqrt(err[q] / ref) / np.sqrt(err["m2p"] / ref))
+    if ratio == 1.0:
+        assert worst[7] <= 1.25 and worst[6] > 1.5 * worst[7], worst
+    else:
+        assert worst[7] <= 1.01, worst
