@@ -147,11 +147,14 @@ int batch_plan(vpm_ctx* c, int kernel, int precision) {
   const int nf = bp->nfields;
   std::vector<int> fields(nf);
   std::vector<Shape> shape(nf);
+  const bool tuned = int(bp->h_tuned.size()) == nf && bp->tuned_kernel == kernel &&
+                     bp->tuned_precision == precision;
   for (int f = 0; f < nf; ++f) {
     fields[f] = f;
-    shape[f] = lookup_shape(c->device, PASS_UJ, kernel, precision,
-                            std::max<int64_t>(bp->h_n[f], 1),
-                            &c->pinned[PASS_UJ][kernel][precision]);
+    shape[f] = tuned ? bp->h_tuned[f]
+                     : lookup_shape(c->device, PASS_UJ, kernel, precision,
+                                    std::max<int64_t>(bp->h_n[f], 1),
+                                    &c->pinned[PASS_UJ][kernel][precision]);
   }
   const int rc = build_queue(c, kernel, precision, fields, shape);
   if (rc != VPM_OK) return rc;
@@ -333,8 +336,12 @@ int vpm_batch_autotune(vpm_batch* b, int kernel, int precision, double* ms) {
                                         std::string("batch autotune: ") + cudaGetErrorString(x));
   };
   // Fields by size bucket; each bucket's fields alone are timed with every
-  // compiled shape as one persistent queue, and the fastest shape is stored
-  // for that bucket.
+  // compiled shape as one persistent queue, which gives the per-bucket
+  // assignment.  Shapes of different buckets run as separate launches one after
+  // another, each with its own tail, so the whole batch is then timed with that
+  // assignment, with one shape for every field (each compiled shape), and with
+  // the per-device table's shapes; the fastest whole-batch plan is kept for
+  // this batch (the per-device table is left alone).
   std::vector<std::pair<int, std::vector<int>>> buckets;
   for (int f = 0; f < bp.nfields; ++f) {
     if (bp.h_n[f] == 0) continue;
@@ -346,6 +353,7 @@ int vpm_batch_autotune(vpm_batch* b, int kernel, int precision, double* ms) {
   }
   static const Shape cands[] = {{128, 2}, {128, 4}, {256, 2}, {128, 1}};
   std::vector<Shape> shape(bp.nfields, Shape{128, 2});
+  bp.h_tuned.clear();
   for (size_t q = 0; q < buckets.size() && e == cudaSuccess && rc == VPM_OK; ++q) {
     const std::vector<int>& fs = buckets[q].second;
     Shape best{0, 0};
@@ -363,12 +371,39 @@ int vpm_batch_autotune(vpm_batch* b, int kernel, int precision, double* ms) {
       }
     }
     if (rc == VPM_OK && best.block > 0)
-      store_shape(c->device, PASS_UJ, kernel, precision, bp.h_n[fs.front()], best);
+      for (int f : fs) shape[f] = best;
   }
-  float t = 0.f;
-  if (rc == VPM_OK && e == cudaSuccess) {
+  // Whole-batch candidates: the per-bucket assignment, one shape for all, the table.
+  std::vector<std::vector<Shape>> plans;
+  plans.push_back(shape);
+  for (const Shape& s : cands)
+    if (pair_shape_supported(precision, s)) plans.push_back(std::vector<Shape>(bp.nfields, s));
+  {
+    std::vector<Shape> table(bp.nfields);
+    for (int f = 0; f < bp.nfields; ++f)
+      table[f] = lookup_shape(c->device, PASS_UJ, kernel, precision,
+                              std::max<int64_t>(bp.h_n[f], 1), &c->pinned[PASS_UJ][kernel][precision]);
+    plans.push_back(table);
+  }
+  std::vector<int> all;
+  for (int f = 0; f < bp.nfields; ++f)
+    if (bp.h_n[f] > 0) all.push_back(f);
+  float t = 1e30f;
+  int best_plan = -1;
+  for (size_t q = 0; q < plans.size() && e == cudaSuccess && rc == VPM_OK; ++q) {
+    rc = build_queue(c, kernel, precision, all, plans[q]);
+    float tq = 0.f;
+    if (rc == VPM_OK) rc = time_queue(&tq);
+    if (rc == VPM_OK && tq < t) {
+      t = tq;
+      best_plan = int(q);
+    }
+  }
+  if (rc == VPM_OK && e == cudaSuccess && best_plan >= 0) {
+    bp.h_tuned = plans[best_plan];
+    bp.tuned_kernel = kernel;
+    bp.tuned_precision = precision;
     rc = batch_plan(c, kernel, precision);
-    if (rc == VPM_OK) rc = time_queue(&t);
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

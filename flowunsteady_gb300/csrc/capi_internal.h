@@ -110,6 +110,8 @@ struct BatchPlan {
   int kernel = -1, precision = -1;   // plan built for this pair
   std::vector<int64_t> h_off, h_n;   // field offsets and sizes
   std::vector<Shape> h_shape;        // tile shape of each field in the current plan
+  std::vector<Shape> h_tuned;        // per-field shapes chosen by vpm_batch_autotune (empty: table)
+  int tuned_kernel = -1, tuned_precision = -1;   // the pass h_tuned was timed for
 };
 
 }  // namespace vpm

@@ -323,6 +323,10 @@ def run_fmm(args):
     fm = L.default_fmm()
     if args.local_order is not None:
         fm.local_order = args.local_order
+    if args.fmm_p is not None:
+        fm.p = args.fmm_p
+    if args.theta is not None:
+        fm.theta = args.theta
     L.check(f.lib.vpm_eval_UJ_fmm(f.p, k, L.PREC_FP32C, ctypes.byref(fm)), f.p)   # warm-up
     ts = []
     for _ in range(3):
@@ -440,6 +444,8 @@ def main(argv=None):
     p.add_argument("--tree", action="store_true", help="step: U/J passes by the treecode")
     p.add_argument("--local-order", type=int, default=None,
                    help="fmm: treecode local expansion order (0: M2P only)")
+    p.add_argument("--fmm-p", type=int, default=None, help="fmm: expansion order of the moments")
+    p.add_argument("--theta", type=float, default=None, help="fmm: acceptance parameter")
     p.add_argument("--out", default=None)
     args = p.parse_args(argv)
     fn = {"sweep": run_sweep, "rings": run_rings, "batch": run_batch, "large": run_large,

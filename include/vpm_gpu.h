@@ -396,9 +396,13 @@ int vpm_batch_step(vpm_batch* b, double dt, const vpm_scheme* s, int64_t nsteps,
  * fields of one shape form one persistent launch per pair pass (the default,
  * before tuning: every bucket below 196,608 particles takes 128x2).
  * vpm_batch_autotune times, for each bucket present, that bucket's fields
- * alone as one persistent U/J launch with every compiled shape, stores the
- * fastest for the bucket, rebuilds the batch's work queue and returns the time
- * of one U/J pass of the whole batch (ms).  vpm_batch_get_shapes reads the
+ * alone as one persistent U/J launch with every compiled shape (the per-bucket
+ * assignment); then one U/J pass of the whole batch with that assignment, with
+ * each compiled shape for every field, and with the table's shapes.  Launches
+ * of different shapes run one after another, so the per-bucket assignment can
+ * lose to one shape for all.  The fastest whole-batch plan is kept for this
+ * batch (the per-device table is not changed), the work queue is rebuilt, and
+ * its time of one U/J pass is returned (ms).  vpm_batch_get_shapes reads the
  * shape of each field (arrays of nfields). */
 int vpm_batch_autotune(vpm_batch* b, int kernel, int precision, double* ms);
 int vpm_batch_get_shapes(vpm_batch* b, int32_t* block, int32_t* tpt);
