@@ -56,7 +56,11 @@ constexpr int kMaxGen = 23;        // root + at most 21 Morton digits (+1 spare)
 constexpr int kCntCells = 0, kCntLeaves = 1, kCntFlags = 2, kCntGroups = 3, kGenBase = 4;
 constexpr int kNumCounters = kGenBase + kMaxGen + 2;
 constexpr int kStack = 256;        // traversal stack (cells)
-constexpr int kTreeBlock = 64;     // threads of the near/far evaluation CTAs = group size
+// Target group size (consecutive particles of the Morton order).  32-particle
+// groups were measured at N = 1M too: at θ = 0.4 they take 0.131 s instead of
+// 0.142 s but lose accuracy (rel-L2 U 5.3e-5, J 1.46e-5 against 4.4e-5, 1.15e-5),
+// and at equal accuracy (θ ≈ 0.39) the two sizes take the same time.
+constexpr int kTreeBlock = 64;     // threads of the far CTAs = group size
 constexpr int kMaxFront = 1 + 8 + 64;   // walk roots: leaves of generations 0-1, generation 2
 
 // ------------------------------------------------------------- workspace --
@@ -545,7 +549,7 @@ __global__ void traverse_kernel(int64_t nthreads, int nfront, const int* __restr
 // One CTA of kNearThreads threads per target group against every particle of
 // its near source ranges, with the pair routines of the direct sum
 // (vpm_device.cuh) on T targets per thread:
-//   - the group's 64 targets are held as TQ = 64/T target sets of T targets
+//   - the group's kTreeBlock targets are held as TQ = kTreeBlock/T target sets of T targets
 //     (target t = tq + TQ·k), each set by SL = kNearThreads/TQ threads, one per
 //     source slice;
 //   - the concatenated near ranges are staged kNearThreads sources at a time
@@ -603,7 +607,8 @@ __global__ void __launch_bounds__(kNearThreads, NearShape<PASS>::kMinBlocks) nea
   constexpr bool D = PASS == PASS_UJD || PASS == PASS_ZETAD;
   constexpr int PER = kNearThreads / SL;              // staged sources per thread and tile
   constexpr int FOLD_TILES = kNearFoldSources / PER;  // tiles between two folds
-  static_assert(kTreeBlock == 64 && kNearThreads == 128, "four-warp scan below");
+  static_assert(kNearThreads == 128 && kNearThreads % TQ == 0 && kTreeBlock <= kNearThreads,
+                "four-warp scan below; whole target sets");
   extern __shared__ __align__(16) unsigned char near_smem[];
   float4* tA = reinterpret_cast<float4*>(near_smem);
   float4* tB = tA + kNearThreads;
@@ -1136,7 +1141,6 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
   const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
   const int f0 = ofar[t0s], fn = ofar[t1s] + nfar[t1s] - f0;
   if (threadIdx.x == 0) atomicAdd(&pairs[1], (unsigned long long)fn * (unsigned long long)(b - a));
-  static_assert(kTreeBlock == 64, "one target per thread");
   const int i = a + int(threadIdx.x);
   const bool active = i < b;
   {
