@@ -47,9 +47,11 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch of the
 # benchmark workload per (N, tile shape), from an ncu capture.  Whole waves of
 # target tiles take the whole source range and only the last wave's tiles are
-# split (partial sums), so the writes are small; the U/J output (25 MB) is
-# still in L2 when the launch ends.
-PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 19558144 + 4343040}
+# split (partial sums), so the writes are small with 128x4 (56 split tiles;
+# the U/J output, 25 MB, is still in L2 when the launch ends) and larger with
+# 256x2 (208 of 512 tiles split into 13 chunks).
+PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 19558144 + 4343040,
+                       (262144, "256x2"): 27405824 + 121591296}
 
 
 def parse():

@@ -31,6 +31,7 @@ struct PairCall {
   double* dj = nullptr;         // PASS_UJD: DJ rows
   int64_t ldo;
   int max_chunks = 0;   // upper bound on source chunks (0 = planner's choice)
+  int64_t chunk = 0;    // pinned source chunk length (0 = planner's choice)
   // FP32 U/J passes: packed records of the ns sources (launch_pack_sources),
   // or null to read the FP64 rows in the kernel.  Bulk copies stage records.
   const float4* rec = nullptr;
@@ -168,6 +169,7 @@ struct vpm_ctx {
   double* h_stage = nullptr;
   size_t h_stage_elems = 0;
   vpm::Shape pinned[2][2][3];
+  int64_t pinned_chunk[2][2][3];   // source chunk length pinned by vpm_set_tile (0: planner)
   std::vector<vpm::GraphEntry> graphs;
   int64_t fail_after = 0;
   std::string err;

@@ -416,7 +416,8 @@ int vpm_batch_get_shapes(vpm_batch* b, int32_t* block, int32_t* tpt);
 typedef struct vpm_tile {
   int32_t block;        /* threads per CTA                         */
   int32_t tpt;          /* targets per thread (register blocking)  */
-  int32_t chunk;        /* sources per work item (0 = all)         */
+  int32_t chunk;        /* sources per work item: 0 = the planner's choice; pinned by
+                           vpm_set_tile, rounded up to whole tiles of `block` sources */
   int32_t reserved;     /* vpm_autotune: ζ-pass shape as block*16 + tpt */
 } vpm_tile;
 int vpm_autotune(vpm_ctx* ctx, int kernel, int precision, vpm_tile* chosen, double* ms);

@@ -380,3 +380,25 @@ def test_jacobian_row_order_is_dU_a_dx_b():
         fd[:, :, b] = (up - um) / (2 * h)       # column b: dU_a/dx_b for a = 0..2
     assert rel_l2(Jc, fd) <= 1e-7
     assert rel_l2(np.transpose(Jc, (0, 2, 1)), fd) > 1e-2
+
+
+@pytest.mark.parametrize("chunk", [1, 128, 300, 1000, 100000])
+def test_pinned_source_chunk_matches_oracle(oracle, chunk):
+    # vpm_set_tile's chunk pins the source range of a work item (rounded up to
+    # whole tiles of the block size); every split goes through the partial
+    # slots and their fixed-order reduction.  A negative length is refused.
+    from flowunsteady_gb300.workloads import leapfrog_rings
+    X, G, S = leapfrog_rings()
+    n = X.shape[0]
+    idx = np.sort(np.random.default_rng(31).choice(n, 300, replace=False))
+    U0, J0 = oracle.uj_direct(L.KERNEL_GAUSSIANERF, X, G, S, Xt=X[idx])
+    with Ctx(n) as c:
+        c.set(X, G, S)
+        Ud, Jd = c.uj(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+        t = L.Tile(128, 2, chunk, 0)
+        c.rc(c.lib.vpm_set_tile(c.p, L.KERNEL_GAUSSIANERF, L.PREC_FP32C, ctypes.byref(t)))
+        U, J = c.uj(L.KERNEL_GAUSSIANERF, L.PREC_FP32C)
+        bad = L.Tile(128, 2, -1, 0)
+        assert c.lib.vpm_set_tile(c.p, L.KERNEL_GAUSSIANERF, L.PREC_FP32C, ctypes.byref(bad)) == L.ERR_INVALID
+    assert rel_l2(U[idx], U0) <= 1e-5 and rel_l2(J[idx], J0) <= 1e-5
+    assert rel_l2(U, Ud) <= 1e-6 and rel_l2(J, Jd) <= 1e-6
