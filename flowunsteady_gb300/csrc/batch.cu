@@ -45,6 +45,16 @@ int from_ctx(vpm_batch* b, int rc) {
 // multiple of the block that keeps the group's queue near four items per
 // resident CTA, and items are sorted by cost (largest first).  Writes the
 // device queue, per-field chunk counts and groups into bp.
+// Work items of a batch queue: the sources of a field are split into chunks of
+// the shortest power-of-two length (in source tiles) for which the queue holds
+// at most this many items per resident CTA.  Items of one field cost alike, but
+// across fields and chunks they differ by orders of magnitude, and the
+// persistent CTAs balance finer items better.  Measured on 48 fields of
+// 2,302-120,610 particles (FP32C U/J pass): 4 items per CTA (whole source
+// ranges) 93.7 ms, 16 90.0 ms, 32 89.4 ms, 64 89.1 ms; 32 bounds the partial
+// sums at 8 chunks per field there.
+constexpr int kBatchItemWaves = 32;
+
 static int build_queue(vpm_ctx* c, int kernel, int precision, const std::vector<int>& fields,
                        const std::vector<Shape>& shape) {
   BatchPlan* bp = c->bp;
@@ -79,7 +89,7 @@ static int build_queue(vpm_ctx* c, int kernel, int precision, const std::vector<
     };
     int64_t L = round_up(nmax, sh.block);
     for (int64_t cand = 2 * sh.block; cand < round_up(nmax, sh.block); cand *= 2) {
-      if (count_items(cand) <= 4 * int64_t(r_uj)) {
+      if (count_items(cand) <= kBatchItemWaves * int64_t(r_uj)) {
         L = cand;
         break;
       }
