@@ -45,13 +45,13 @@ BYTES_H2D = 56          # X, Γ, σ per particle (FP64)
 BYTES_D2H = 96          # U (3) and J (9) per particle (FP64)
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch of the
-# benchmark workload per (N, tile shape), from an ncu capture.  Whole waves of
-# target tiles take the whole source range and only the last wave's tiles are
-# split (partial sums), so the writes are small with 128x4 (56 split tiles;
-# the U/J output, 25 MB, is still in L2 when the launch ends) and larger with
-# 256x2 (208 of 512 tiles split into 13 chunks).
-PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 19558144 + 4343040,
-                       (262144, "256x2"): 27405824 + 121591296}
+# benchmark workload per (N, tile shape), from an ncu capture.  The plain U/J
+# pass is split into about 64 waves of short work items (57 source chunks per
+# target tile with 128x4, 38 with 256x2), which measured 5 % faster than whole
+# tiles; the writes are those chunks' FP64 partial sums, which the reduction
+# launch reads back (1.8 GB, about 0.3 ms of DRAM time).
+PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 69945856 + 1735043328,
+                       (262144, "256x2"): 54719488 + 1136783872}
 
 
 def parse():

@@ -170,8 +170,10 @@ static int plan_cluster(int device, const PairCall& pc, Shape sh, int64_t n_tb,
   return best_nc;
 }
 
-// Waves of work items a pass with fewer target tiles than resident CTAs is split into.
+// Waves of work items the plain U/J pass is split into: with fewer target tiles
+// than resident CTAs, and with more.
 constexpr int kSmallWaves = 8;
+constexpr int kLargeWaves = 64;
 
 // Plan and enqueue one pair pass.  `need_part` (elements) is raised to what
 // the launch needs; when dry, nothing is launched.  A split source range goes
@@ -208,8 +210,16 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   // µs, 40,000 2,100 -> 2,010 µs, 65,536 5,182 -> 5,136 µs, 131,072
   // unchanged.  The ζ and α-derivative passes did not get faster, while
   // their reductions read the extra partial sums, so they keep the wave plan.
-  if (cluster <= 1 && pc.chunk <= 0 && pc.pass == PASS_UJ && n_tb < resident) {
-    const int64_t cc = ceil_div(int64_t(kSmallWaves) * resident, n_tb);
+  // With a wave of tiles or more, the plain U/J pass is split still finer,
+  // about kLargeWaves waves of items: measured at N = 262,144 (128x4) the pass
+  // took 74.4 ms with whole waves of whole tiles (only the last wave split),
+  // 71.8 / 71.0 / 70.6 ms with 16,384 / 8,192 / 4,096-source chunks, and at
+  // N = 1,048,576 1,125 ms against 1,084-1,088 ms with 131,072 to 16,384.
+  // The partial sums this writes (15 values per target and chunk) and the
+  // reduction reads back cost about 0.5 ms of DRAM time at 262,144.
+  if (cluster <= 1 && pc.chunk <= 0 && pc.pass == PASS_UJ) {
+    const int waves = n_tb < resident ? kSmallWaves : kLargeWaves;
+    const int64_t cc = ceil_div(int64_t(waves) * resident, n_tb);
     chunk = round_up(std::max<int64_t>(ceil_div(pc.ns, cc), 1), sh.block);
     n_chunk = int(std::max<int64_t>(ceil_div(pc.ns, chunk), 1));
   }
@@ -219,12 +229,12 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   }
   if (cluster <= 1 && pc.max_chunks > 0 && n_chunk > pc.max_chunks)
     n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
-  // Whole waves of tiles over the whole source range, and only the rest split:
-  // the same time in units of a whole-tile CTA when CTAs of a wave take equal
-  // time, with partial sums (written, then read back by the reduction) for the
-  // split tiles only.
+  // The other passes: whole waves of tiles over the whole source range, and
+  // only the rest split: the same time in units of a whole-tile CTA when CTAs
+  // of a wave take equal time, with partial sums (written, then read back by
+  // the reduction) for the split tiles only.
   int64_t n_full = 0;
-  if (cluster <= 1 && n_chunk > 1 && n_tb > resident && pc.chunk <= 0) {
+  if (cluster <= 1 && n_chunk > 1 && n_tb > resident && pc.chunk <= 0 && pc.pass != PASS_UJ) {
     const int64_t full_waves = n_tb / resident, nf = full_waves * resident, nr = n_tb - nf;
     int64_t rchunk = 0;
     const int rc = nr > 0 ? plan_chunks(nr, pc.ns, sh.block, resident, &rchunk, pc.max_chunks) : 1;
