@@ -174,6 +174,7 @@ static int plan_cluster(int device, const PairCall& pc, Shape sh, int64_t n_tb,
 // than resident CTAs, and with more.
 constexpr int kSmallWaves = 8;
 constexpr int kLargeWaves = 64;
+constexpr int64_t kLargeField = 131072;
 
 // Plan and enqueue one pair pass.  `need_part` (elements) is raised to what
 // the launch needs; when dry, nothing is launched.  A split source range goes
@@ -210,15 +211,21 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   // µs, 40,000 2,100 -> 2,010 µs, 65,536 5,182 -> 5,136 µs, 131,072
   // unchanged.  The ζ and α-derivative passes did not get faster, while
   // their reductions read the extra partial sums, so they keep the wave plan.
-  // With a wave of tiles or more, the plain U/J pass is split still finer,
-  // about kLargeWaves waves of items: measured at N = 262,144 (128x4) the pass
-  // took 74.4 ms with whole waves of whole tiles (only the last wave split),
-  // 71.8 / 71.0 / 70.6 ms with 16,384 / 8,192 / 4,096-source chunks, and at
-  // N = 1,048,576 1,125 ms against 1,084-1,088 ms with 131,072 to 16,384.
-  // The partial sums this writes (15 values per target and chunk) and the
-  // reduction reads back cost about 0.5 ms of DRAM time at 262,144.
-  if (cluster <= 1 && pc.chunk <= 0 && pc.pass == PASS_UJ) {
-    const int waves = n_tb < resident ? kSmallWaves : kLargeWaves;
+  // With a wave of tiles or more, every pass is split still finer, about
+  // kLargeWaves waves of items: measured at N = 262,144 (128x4) the plain U/J
+  // pass took 74.4 ms with whole waves of whole tiles (only the last wave
+  // split), 71.8 / 71.0 / 70.6 ms with 16,384 / 8,192 / 4,096-source chunks,
+  // and at N = 1,048,576 1,125 ms against 1,084-1,088 ms with 131,072 to
+  // 16,384; an SFS evaluation at 262,144 84.3 -> 82.4 ms (prescribed C_d) and
+  // 103.4 -> 99.2 ms (dynamic, analytic ∂/∂σ).  The partial sums this writes
+  // (15 values per target and chunk for U/J) and the reduction reads back
+  // cost about 0.7 ms of DRAM time per U/J pass at 262,144.
+  // Every pass of a field of kLargeField sources or more takes the finer split
+  // too: the ζ pass at 262,144 (128x4, fewer tiles than its resident CTAs)
+  // measured 1.7 ms faster with 4,608-source chunks.
+  const bool large = n_tb >= resident || pc.ns >= kLargeField;
+  if (cluster <= 1 && pc.chunk <= 0 && (pc.pass == PASS_UJ || large)) {
+    const int waves = large ? kLargeWaves : kSmallWaves;
     const int64_t cc = ceil_div(int64_t(waves) * resident, n_tb);
     chunk = round_up(std::max<int64_t>(ceil_div(pc.ns, cc), 1), sh.block);
     n_chunk = int(std::max<int64_t>(ceil_div(pc.ns, chunk), 1));
@@ -229,31 +236,12 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   }
   if (cluster <= 1 && pc.max_chunks > 0 && n_chunk > pc.max_chunks)
     n_chunk = plan_chunks(n_tb, pc.ns, sh.block, resident, &chunk, pc.max_chunks);
-  // The other passes: whole waves of tiles over the whole source range, and
-  // only the rest split: the same time in units of a whole-tile CTA when CTAs
-  // of a wave take equal time, with partial sums (written, then read back by
-  // the reduction) for the split tiles only.
-  int64_t n_full = 0;
-  if (cluster <= 1 && n_chunk > 1 && n_tb > resident && pc.chunk <= 0 && pc.pass != PASS_UJ) {
-    const int64_t full_waves = n_tb / resident, nf = full_waves * resident, nr = n_tb - nf;
-    int64_t rchunk = 0;
-    const int rc = nr > 0 ? plan_chunks(nr, pc.ns, sh.block, resident, &rchunk, pc.max_chunks) : 1;
-    const double t_hybrid =
-        double(full_waves) + (nr > 0 ? double(ceil_div(nr * rc, resident)) / rc : 0.0);
-    const double t_split = double(ceil_div(n_tb * n_chunk, resident)) / n_chunk;
-    if (t_hybrid <= t_split * 1.001) {
-      n_full = nf;
-      n_chunk = nr > 0 ? rc : 1;
-      chunk = nr > 0 ? rchunk : pc.ns;
-    }
-  }
   PairPlan plan;
   plan.shape = sh;
   plan.n_tb = n_tb;
   plan.n_chunk = n_chunk;
   plan.chunk = chunk;
   plan.cluster = cluster;
-  plan.n_full = n_full;
   const int nv = nval_of(pc.pass);
   const size_t need = plan.slots() > 1 ? size_t(plan.slots()) * nv * size_t(ldp) : 0;
   if (need_part) *need_part = std::max(*need_part, need);
@@ -267,7 +255,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.sigma_scale = pc.sigma_scale;
   a.dj = pc.dj;
   a.t_off = pc.t0; a.nt = nt; a.ns = pc.ns; a.chunk = chunk;
-  a.n_tb = int(n_tb); a.n_chunk = n_chunk; a.n_full = int(n_full);
+  a.n_tb = int(n_tb); a.n_chunk = n_chunk;
   a.items = nullptr; a.n_items = 0; a.counter = nullptr;
   a.u = pc.u; a.j = pc.j; a.ldo = pc.ldo;
   a.part = part; a.ldp = ldp;
@@ -278,12 +266,10 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.coh = pc.coh;
   a.coh_blocks = ceil_div(pc.ns, 32);
   a.cluster = cluster;
-  cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a,
-                              int(n_full + (n_tb - n_full) * n_chunk), st);
+  cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
   if (plan.slots() > 1) {
-    const int64_t t_split = std::min(pc.t1, pc.t0 + n_full * TB);
-    e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, t_split, pc.t1,
+    e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
   return e;

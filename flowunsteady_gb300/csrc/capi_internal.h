@@ -45,7 +45,6 @@ struct PairPlan {
   int n_chunk = 1;      // source chunks per target tile
   int64_t chunk = 0;    // sources per chunk
   int cluster = 1;      // > 1: the chunks of a tile are one cluster, summed on chip
-  int64_t n_full = 0;   // leading tiles over the whole source range (final values)
   // Partial slots the plan writes (and a reduction launch sums).
   int slots() const { return (n_chunk > 1 && cluster <= 1) ? n_chunk : 1; }
 };

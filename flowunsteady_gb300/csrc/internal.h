@@ -46,10 +46,8 @@ struct PairArgs {
   int64_t ldt;
   double sigma_scale;
   // Decomposition without a table: targets [t_off, t_off+nt) x sources [0, ns).
-  // The first n_full target tiles take the whole source range (final values);
-  // the other n_tb - n_full are split into n_chunk chunks (partial slots).
   int64_t t_off, nt, ns, chunk;
-  int32_t n_tb, n_chunk, n_full;
+  int32_t n_tb, n_chunk;
   // Decomposition from a table (batches): n_items entries, dynamic queue when
   // counter != null.
   const PairItem* items;

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   __shared__ int s_item;
 
   const int tid = threadIdx.x;
-  const int n_items = a.items ? a.n_items : a.n_full + (a.n_tb - a.n_full) * a.n_chunk;
+  const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
   // Packed records replace the FP64 source reads (and their conversion) when
   // the host provides them; bulk copies need them.
   const bool use_rec = Tr::kRec && a.rec != nullptr;
@@ -241,20 +241,11 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     if (a.items) {
       const PairItem it = a.items[item];
       t0 = it.t0; t1 = it.t1; s0 = it.s0; s1 = it.s1; slot = it.slot;
-    } else if (!CLU && item < a.n_full) {
-      // Whole source range of one of the first n_full tiles: final values.
-      t0 = a.t_off + int64_t(item) * TB;
-      t1 = min(t0 + TB, a.t_off + a.nt);
-      s0 = 0;
-      s1 = a.ns;
-      slot = -1;
     } else {
       // Clusters: consecutive CTAs share a target tile, cluster rank = chunk;
-      // otherwise chunk-major items over the split tiles, a partial slot per chunk.
-      const int r = CLU ? item : item - a.n_full;
-      const int n_split = a.n_tb - a.n_full;
-      const int tb = CLU ? item / a.cluster : a.n_full + r % n_split;
-      const int c = CLU ? item % a.cluster : r / n_split;
+      // otherwise chunk-major items with a partial slot per chunk.
+      const int tb = CLU ? item / a.cluster : item % a.n_tb;
+      const int c = CLU ? item % a.cluster : item / a.n_tb;
       t0 = a.t_off + int64_t(tb) * TB;
       t1 = min(t0 + TB, a.t_off + a.nt);
       s0 = int64_t(c) * a.chunk;
