@@ -47,11 +47,11 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one Gaussian-erf FP32C U/J launch of the
 # benchmark workload per (N, tile shape), from an ncu capture.  The plain U/J
 # pass is split into about 64 waves of short work items (57 source chunks per
-# target tile with 128x4, 38 with 256x2), which measured 5 % faster than whole
-# tiles; the writes are those chunks' FP64 partial sums, which the reduction
-# launch reads back (1.8 GB, about 0.3 ms of DRAM time).
-PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 69945856 + 1735043328,
-                       (262144, "256x2"): 54719488 + 1136783872}
+# target tile with 128x4), which measured 5 % faster than whole tiles.  The
+# last CTA of each tile sums the chunks' FP64 partial sums from L2 and drops
+# them there; what still reaches DRAM is partial sums evicted before their tile
+# was complete.  (With a separate reduction launch the partial sums took 1.8 GB.)
+PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 64656640 + 138696448}
 
 
 def parse():

@@ -129,6 +129,15 @@ int active_clusters(int device, int pass, int kernel, int precision, Shape s, in
   return n;
 }
 
+int fused_reduce_mode() {
+  static const int mode = [] {
+    const char* v = std::getenv("VPM_FUSED_REDUCE");
+    if (!v || !v[0]) return -1;
+    return v[0] == '0' ? 0 : 1;
+  }();
+  return mode;
+}
+
 int cluster_mode() {
   static const int mode = [] {
     const char* v = std::getenv("VPM_CLUSTER");
@@ -178,8 +187,17 @@ constexpr int64_t kLargeField = 131072;
 
 // Plan and enqueue one pair pass.  `need_part` (elements) is raised to what
 // the launch needs; when dry, nothing is launched.  A split source range goes
-// through partial slots summed by a reduction launch, or (FP32C, single field,
-// VPM_CLUSTER=1) through thread-block clusters that sum on chip.
+// through partial slots summed by a reduction launch, or by the last CTA of
+// each target tile (the fused form: plain U/J passes of large fields, or any
+// split pass with VPM_FUSED_REDUCE=1), or (FP32C, single field, VPM_CLUSTER=1)
+// through thread-block clusters that sum on chip.
+// Measured on GB300 with FP32C (fused against a reduction launch):
+// - U/J at N = 7,600: 0.324 against 0.150 ms; one CTA summing a tile's ~120
+//   chunks is a serial tail;
+// - U/J at 65,536: 5.15-5.25 against 5.12-5.13 ms;
+// - U/J at 262,144: 70.46 against 70.63 ms (Gaussian-erf), with DRAM traffic
+//   of 203 MB instead of 1.8 GB + 1.8 GB;
+// - SFS evaluations at 262,144, fusing every pass: 0.2-0.6 % slower.
 cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* pinned,
                      double* part, int64_t ldp, size_t part_elems, size_t* need_part, bool dry,
                      cudaStream_t st, PairPlan* plan_out) {
@@ -242,8 +260,12 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   plan.n_chunk = n_chunk;
   plan.chunk = chunk;
   plan.cluster = cluster;
+  const int fmode = fused_reduce_mode();
+  plan.fused = plan.slots() > 1 && (fmode == 1 || (fmode < 0 && large && pc.pass == PASS_UJ));
   const int nv = nval_of(pc.pass);
-  const size_t need = plan.slots() > 1 ? size_t(plan.slots()) * nv * size_t(ldp) : 0;
+  const size_t slot_elems = plan.slots() > 1 ? size_t(plan.slots()) * nv * size_t(ldp) : 0;
+  // One 32-bit counter per target tile after the slots (two per double).
+  const size_t need = slot_elems + (plan.fused ? size_t((n_tb + 1) / 2) : 0);
   if (need_part) *need_part = std::max(*need_part, need);
   if (plan_out) *plan_out = plan;
   if (dry) return cudaSuccess;
@@ -266,9 +288,16 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   a.coh = pc.coh;
   a.coh_blocks = ceil_div(pc.ns, 32);
   a.cluster = cluster;
-  cudaError_t e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
+  a.tile_done = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (plan.fused) {
+    a.tile_done = reinterpret_cast<unsigned int*>(part + slot_elems);
+    e = cudaMemsetAsync(a.tile_done, 0, size_t(n_tb) * sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+  }
+  e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
-  if (plan.slots() > 1) {
+  if (plan.slots() > 1 && !plan.fused) {
     e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
@@ -611,7 +640,7 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
   e = run_pair(pc, c->device, c->num_sms, pinned, c->part, ld, c->part_elems, &c->part_need,
                c->dry, c->st, &plan);
   if (c->dry || e != cudaSuccess) return e;
-  c->launches += plan.slots() > 1 ? 2 : 1;
+  c->launches += plan.launches();
   return scatter_outputs(c, pass, perm, u, j, dj);
 }
 
@@ -719,7 +748,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
   PairPlan plan;
   cudaError_t e = run_pair(pc, c->device, c->num_sms, pinned, c->part, c->ld, c->part_elems,
                            &c->part_need, c->dry, c->st, &plan);
-  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += plan.slots() > 1 ? 2 : 1;
+  if (!c->dry && e == cudaSuccess && t1 > t0) c->launches += plan.launches();
   return e;
 }
 

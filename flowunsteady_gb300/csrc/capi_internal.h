@@ -45,9 +45,18 @@ struct PairPlan {
   int n_chunk = 1;      // source chunks per target tile
   int64_t chunk = 0;    // sources per chunk
   int cluster = 1;      // > 1: the chunks of a tile are one cluster, summed on chip
-  // Partial slots the plan writes (and a reduction launch sums).
+  // The last CTA of each target tile sums its partial slots (no reduction
+  // launch); the tiles' counters follow the slots in the scratch.
+  bool fused = false;
+  // Partial slots the plan writes (and a reduction launch, or the fused form, sums).
   int slots() const { return (n_chunk > 1 && cluster <= 1) ? n_chunk : 1; }
+  // Kernel launches of the pass: the pair kernel, and the reduction unless fused.
+  int launches() const { return (slots() > 1 && !fused) ? 2 : 1; }
 };
+
+// Fused reduction of split source ranges: -1 (default) the planner's rule,
+// 0 (VPM_FUSED_REDUCE=0) always a reduction launch, 1 (=1) always fused.
+int fused_reduce_mode();
 
 // Plan of the last stateless U/J call (vpm_uj_device_async/_noalloc) on this
 // host thread, for vpm_debug_last_plan.

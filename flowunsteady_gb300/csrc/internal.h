@@ -81,6 +81,12 @@ struct PairArgs {
   // n_tb x cluster, cluster rank = chunk) that sum their compensated partial
   // sums through distributed shared memory in rank order; no partial slots.
   int32_t cluster;
+  // Single-field form with split sources, when non-null: the items run
+  // tile-major (item = tile * n_chunk + chunk), and the last CTA of a target
+  // tile to finish (n_tb counters, zero at launch) sums the tile's partial
+  // slots in chunk order, writes the final values and discards the summed
+  // lines from L2, so that they are not written back to DRAM.
+  unsigned int* tile_done;
 };
 
 // Tile shape of a launch.

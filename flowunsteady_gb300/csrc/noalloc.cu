@@ -37,7 +37,7 @@ namespace {
 constexpr int64_t kScratchDoubles = int64_t(1) << 19;          // 4 MiB
 // Largest target count accepted: two source chunks of 15 values per target fit.
 constexpr int64_t kMaxTargets = 16384;
-static_assert(2 * kNvalUJ * kMaxTargets <= kScratchDoubles, "scratch too small");
+static_assert((2 * kNvalUJ + 1) * kMaxTargets <= kScratchDoubles, "scratch too small");
 
 static __device__ __align__(256) double g_uj_scratch[kScratchDoubles];
 
@@ -143,7 +143,8 @@ extern "C" int vpm_uj_device_noalloc(int kernel, int precision, int64_t ns, cons
   pc.u = U; pc.j = J; pc.ldo = ld_o;
   // Every partial slot a launch uses is written before it is read, so the
   // scratch needs no clearing between calls.
-  pc.max_chunks = int(kScratchDoubles / (int64_t(kNvalUJ) * nt));
+  // The room of nt doubles left over holds the fused form's tile counters.
+  pc.max_chunks = int((kScratchDoubles - nt) / (int64_t(kNvalUJ) * nt));
   size_t need = 0;
   PairPlan plan;
   run_pair(pc, dev, sms, nullptr, nullptr, nt, 0, &need, true, nullptr, &plan);

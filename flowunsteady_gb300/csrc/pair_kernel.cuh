@@ -24,7 +24,9 @@
 //     thread-private slots), so the long sum keeps ~48 bits while the pair
 //     arithmetic stays FP32;
 //   - the epilogue converts to FP64 and writes final values (single source
-//     chunk) or raw sums into a partial slot reduced later in fixed order.
+//     chunk) or raw sums into a partial slot, which a reduction launch sums in
+//     fixed chunk order, or (the fused form) the last CTA of the target tile
+//     does, in the same order.
 // Work items are (target tile, source chunk); grids are sized by the host to
 // a whole number of waves, or a persistent grid pulls items from a queue.
 #pragma once
@@ -92,18 +94,21 @@ constexpr int min_blocks() {
 constexpr int kFoldSources = 256;
 
 // J_ab = -(KP·A_ab + ε_abc W_c)/(4π) from 12 raw sums (A 9 then W 3) at v.
+// The products and sums are fused explicitly, so that every kernel that forms
+// final values (pass epilogue, reduction launch, fused reduction) rounds them
+// the same way, whatever the compiler would contract in each.
 template <int KERNEL>
 __device__ inline void write_jacobian(const double* v, double* out, int64_t ld, int64_t i) {
   const double s = -kInv4Pi, kp = kp_to_qr<KERNEL>();
   const double w0 = v[9], w1 = v[10], w2 = v[11];
   out[0 * ld + i] = s * (kp * v[0]);
-  out[1 * ld + i] = s * (kp * v[1] + w2);
-  out[2 * ld + i] = s * (kp * v[2] - w1);
-  out[3 * ld + i] = s * (kp * v[3] - w2);
+  out[1 * ld + i] = s * __fma_rn(kp, v[1], w2);
+  out[2 * ld + i] = s * __fma_rn(kp, v[2], -w1);
+  out[3 * ld + i] = s * __fma_rn(kp, v[3], -w2);
   out[4 * ld + i] = s * (kp * v[4]);
-  out[5 * ld + i] = s * (kp * v[5] + w0);
-  out[6 * ld + i] = s * (kp * v[6] + w1);
-  out[7 * ld + i] = s * (kp * v[7] - w0);
+  out[5 * ld + i] = s * __fma_rn(kp, v[5], w0);
+  out[6 * ld + i] = s * __fma_rn(kp, v[6], w1);
+  out[7 * ld + i] = s * __fma_rn(kp, v[7], -w0);
   out[8 * ld + i] = s * (kp * v[8]);
 }
 
@@ -165,6 +170,72 @@ __device__ __forceinline__ void cluster_epilogue(const PairArgs& a, const float*
   }
 }
 
+// Chunk of the j-th item of a tile in the fused form: the chunk cs that holds
+// the tile's own particles (targets and sources share an order) first, then
+// outwards, alternating sides: cs, cs-1, cs+1, cs-2, ... (a permutation of
+// [0, n)).  The near chunks are the costly ones (close pairs take the general
+// form), so each tile's items end close together and its partial sums wait in
+// L2 for a shorter time.
+__device__ __forceinline__ int near_first_chunk(int j, int cs, int n) {
+  const int m = min(cs, n - 1 - cs);
+  if (j <= 2 * m) {
+    const int d = (j + 1) >> 1;
+    return (j & 1) ? cs - d : cs + d;
+  }
+  const int k = j - 2 * m;
+  return cs > m ? cs - m - k : cs + m + k;
+}
+
+// Fused form of the reduction, run by the last CTA of target tile [t0, t1) to
+// finish: the tile's partial slots summed in chunk order from L2 (the same FP64
+// additions in the same order as reduce_kernel), the final values written, and
+// the summed lines that hold only this tile's targets dropped from L2 without
+// a write-back.
+template <int PASS, int KERNEL, int BLOCK, int T>
+__device__ __noinline__ void tile_reduce(const PairArgs& a, int64_t t0, int64_t t1) {
+  constexpr int NV = nval_of(PASS);
+  // Values summed side by side: 2G loads in flight per thread, in few enough
+  // registers that the summation adds little to the kernel's count.
+  constexpr int G = 4;
+  const int tid = threadIdx.x;
+  const int64_t step = int64_t(NV) * a.ldp;
+#pragma unroll 1
+  for (int k = 0; k < T; ++k) {
+    const int64_t i = t0 + k * BLOCK + tid;
+    if (i >= t1) break;
+    double v[NV];
+#pragma unroll
+    for (int w0 = 0; w0 < NV; w0 += G) {
+      double s[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) s[g] = 0.0;
+      const double* p = a.part + int64_t(w0) * a.ldp + i;
+#pragma unroll 2
+      for (int c = 0; c < a.n_chunk; ++c, p += step) {
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+          if (w0 + g < NV) s[g] += __ldcg(p + int64_t(g) * a.ldp);
+      }
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+        if (w0 + g < NV) v[w0 + g] = s[g];
+    }
+    write_final<PASS, KERNEL>(v, a, i);
+  }
+  __syncthreads();   // every read of the tile's slots is done
+  // Row r = slot * NV + w holds the tile's targets at bytes [s, e); only the
+  // 128-byte lines inside that range are dropped.
+  constexpr int kLines = (BLOCK * T * 8) / 128 + 1;
+  const int rows = a.n_chunk * NV;
+  for (int idx = tid; idx < rows * kLines; idx += BLOCK) {
+    const int r = idx / kLines, l = idx - r * kLines;
+    const uintptr_t s = reinterpret_cast<uintptr_t>(a.part + int64_t(r) * a.ldp + t0);
+    const uintptr_t e = s + uintptr_t(t1 - t0) * sizeof(double);
+    const uintptr_t line = ((s + 127) & ~uintptr_t(127)) + uintptr_t(l) * 128;
+    if (line + 128 <= e) discard_l2_line(reinterpret_cast<const void*>(line));
+  }
+}
+
 // CLU: the split-source cluster form (FP32C only; launched with a cluster
 // dimension of a.cluster CTAs, one item per CTA).
 template <int PASS, int KERNEL, int PREC, int BLOCK, int T, bool CLU = false>
@@ -199,6 +270,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
                                             (COMP ? size_t(BLOCK) * T * NV * 2 * sizeof(float) : 0));
   uint64_t* bar = reinterpret_cast<uint64_t*>(stage + size_t(BLOCK) * 3);
   __shared__ int s_item;
+  __shared__ int s_last;
 
   const int tid = threadIdx.x;
   const int n_items = a.items ? a.n_items : a.n_tb * a.n_chunk;
@@ -242,11 +314,16 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       const PairItem it = a.items[item];
       t0 = it.t0; t1 = it.t1; s0 = it.s0; s1 = it.s1; slot = it.slot;
     } else {
-      // Clusters: consecutive CTAs share a target tile, cluster rank = chunk;
-      // otherwise chunk-major items with a partial slot per chunk.
-      const int tb = CLU ? item / a.cluster : item % a.n_tb;
-      const int c = CLU ? item % a.cluster : item / a.n_tb;
+      // Clusters: consecutive CTAs share a target tile, cluster rank = chunk.
+      // The fused reduction runs the chunks of a tile as consecutive items,
+      // so that their partial sums are still in L2 when the last one sums
+      // them; otherwise the items are chunk-major.
+      const bool tile_major = CLU || a.tile_done;
+      const int per = CLU ? a.cluster : a.n_chunk;
+      const int tb = tile_major ? item / per : item % a.n_tb;
+      int c = tile_major ? item % per : item / a.n_tb;
       t0 = a.t_off + int64_t(tb) * TB;
+      if (!CLU && a.tile_done) c = near_first_chunk(c, min(int(t0 / a.chunk), a.n_chunk - 1), a.n_chunk);
       t1 = min(t0 + TB, a.t_off + a.nt);
       s0 = int64_t(c) * a.chunk;
       s1 = min(s0 + a.chunk, a.ns);
@@ -639,10 +716,26 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
       }
       if (slot >= 0) {
+        // The fused form keeps the slot in L2 (evict_last) until the tile is summed.
+        const uint64_t pol = l2_policy(a.tile_done != nullptr);
 #pragma unroll
-        for (int w = 0; w < NV; ++w) a.part[(int64_t(slot) * NV + w) * a.ldp + i] = v[w];
+        for (int w = 0; w < NV; ++w)
+          st_global_hint(a.part + (int64_t(slot) * NV + w) * a.ldp + i, v[w], pol);
       } else {
         write_final<PASS, KERNEL>(v, a, i);
+      }
+    }
+    if (!a.items && a.tile_done && slot >= 0) {
+      // The slot reaches L2 before the tile's count; the CTA that counts the
+      // tile's last chunk sums the slots (the counter pattern of a fenced
+      // last-block reduction).
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) s_last = atomicAdd(a.tile_done + item / a.n_chunk, 1u) == unsigned(a.n_chunk - 1);
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        tile_reduce<PASS, KERNEL, BLOCK, T>(a, t0, t1);
       }
     }
 

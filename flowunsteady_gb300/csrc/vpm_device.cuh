@@ -1250,6 +1250,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int po
   return false;
 }
 
+// An L2 cache policy for every access it covers: evict_last (the lines are
+// kept over normal ones) when last is true, else evict_normal.
+__device__ __forceinline__ uint64_t l2_policy(bool last) {
+  uint64_t keep, normal;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
+  asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(normal));
+  return last ? keep : normal;
+}
+
+// Store v at p with the L2 cache policy pol.
+__device__ __forceinline__ void st_global_hint(double* p, double v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(__cvta_generic_to_global(p)),
+               "d"(v), "l"(pol)
+               : "memory");
+}
+
+// Drop the 128-byte L2 line at p (128-byte aligned, device memory) without a
+// write-back: its contents become undefined, so only data that no one reads
+// again may be discarded.
+__device__ __forceinline__ void discard_l2_line(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(__cvta_generic_to_global(p)) : "memory");
+}
+
 }  // namespace vpm
 
 // ------------------------------------------------------------------------------
