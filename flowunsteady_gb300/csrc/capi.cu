@@ -298,7 +298,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   e = launch_pair(pc.pass, pc.kernel, pc.prec, sh, a, int(n_tb * n_chunk), st);
   if (e != cudaSuccess) return e;
   if (plan.slots() > 1 && !plan.fused) {
-    e = launch_reduce(pc.pass, pc.kernel, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
+    e = launch_reduce(pc.pass, pc.kernel, pc.prec, part, ldp, nullptr, nullptr, 0, n_chunk, pc.t0, pc.t1,
                       pc.u, pc.j, pc.dj, pc.ldo, st);
   }
   return e;
@@ -715,7 +715,7 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
       c->launches += 1;
     }
     if (bp->max_chunks > 1) {
-      e = launch_reduce(pass, kernel, c->part, ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
+      e = launch_reduce(pass, kernel, prec, c->part, ld, bp->d_foff, bp->d_fchunks, bp->nfields, 0,
                         0, c->n, uo, jo, djo, ld, c->st);
       c->launches += 1;
       if (e != cudaSuccess) return e;

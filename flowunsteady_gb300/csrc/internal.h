@@ -118,7 +118,9 @@ int pair_ctas_per_sm(int pass, int kernel, int precision, Shape shape);
 // Whether a shape is compiled.
 bool pair_shape_supported(int precision, Shape shape);
 
-// Sum partial slots in fixed order and write the final values.
+// Sum partial slots in fixed order and write the final values.  FP64 passes
+// hold FP64 slots, summed in FP64; the FP32 passes hold float pairs (hi, lo),
+// summed as a double-float (PairSum in pair_kernel.cuh).
 //   UJ: U = -Uacc/(4π), J = -(Aacc·KP + ε·Wacc)/(4π); ZETA: raw sums.
 // Targets are [t_begin, t_end); the slot count of target i is scalar_chunks
 // when foff is null, else found from the device field table (foff[f] <= i,
@@ -129,7 +131,7 @@ bool pair_shape_supported(int precision, Shape shape);
 cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
                                 const double* S, int64_t ld, double scale, float4* rec,
                                 unsigned int* compact, cudaStream_t st);
-cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
+cudaError_t launch_reduce(int pass, int kernel, int precision, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
                           double* j, double* dj, int64_t ldo, cudaStream_t st);
@@ -138,7 +140,7 @@ cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
 // pair_smem_bytes forward to these for PASS_UJD and PASS_ZETAD.
 cudaError_t launch_pair_d(int pass, int kernel, int precision, Shape shape, const PairArgs& a,
                           int grid, cudaStream_t st);
-cudaError_t launch_reduce_d(int pass, int kernel, const double* part, int64_t ldp,
+cudaError_t launch_reduce_d(int pass, int kernel, int precision, const double* part, int64_t ldp,
                             const int64_t* foff, const int32_t* fchunks, int nfields,
                             int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
                             double* j, double* dj, int64_t ldo, cudaStream_t st);

@@ -90,17 +90,17 @@ cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const do
   return cudaGetLastError();
 }
 
-cudaError_t launch_reduce(int pass, int kernel, const double* part, int64_t ldp,
+cudaError_t launch_reduce(int pass, int kernel, int precision, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
                           double* j, double* dj, int64_t ldo, cudaStream_t st) {
   if (pass == PASS_UJ)
-    return reduce<PASS_UJ>(kernel, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
+    return reduce<PASS_UJ>(kernel, precision, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
                            t_end, u, j, dj, ldo, st);
   if (pass == PASS_ZETA)
-    return reduce<PASS_ZETA>(kernel, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
+    return reduce<PASS_ZETA>(kernel, precision, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
                              t_end, u, j, dj, ldo, st);
-  return launch_reduce_d(pass, kernel, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
+  return launch_reduce_d(pass, kernel, precision, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
                          t_end, u, j, dj, ldo, st);
 }
 

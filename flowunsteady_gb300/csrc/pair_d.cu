@@ -24,14 +24,14 @@ cudaError_t launch_pair_d(int pass, int kernel, int precision, Shape s, const Pa
                           : launch<PASS_ZETAD>(kernel, precision, s, a, grid, st);
 }
 
-cudaError_t launch_reduce_d(int pass, int kernel, const double* part, int64_t ldp,
+cudaError_t launch_reduce_d(int pass, int kernel, int precision, const double* part, int64_t ldp,
                             const int64_t* foff, const int32_t* fchunks, int nfields,
                             int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,
                             double* j, double* dj, int64_t ldo, cudaStream_t st) {
   if (pass == PASS_UJD)
-    return reduce<PASS_UJD>(kernel, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
+    return reduce<PASS_UJD>(kernel, precision, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
                             t_end, u, j, dj, ldo, st);
-  return reduce<PASS_ZETAD>(kernel, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
+  return reduce<PASS_ZETAD>(kernel, precision, part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin,
                             t_end, u, j, dj, ldo, st);
 }
 

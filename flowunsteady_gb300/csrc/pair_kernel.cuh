@@ -129,6 +129,40 @@ __device__ inline void write_final(const double* v, const PairArgs& a, int64_t i
   }
 }
 
+// Partial slots of the FP32 passes hold a chunk's raw FP32 sums as a float
+// pair (hi, lo) in the 8 bytes of a slot element: the fold pair (FP32C) or
+// (sum, 0) (FP32).  The chunks are summed in chunk order as a double-float
+// (s, c): s + hi by Knuth's TwoSum, its error and lo into c, all FP32
+// additions on the FMA pipe; the value is s + c in FP64.  (GB300 retires about
+// two FP64 additions per SM and cycle, which bounded the FP64 form of this sum
+// at small N: 21 µs for the 60 chunks of a U/J pass at N = 7,600.)  One chunk
+// gives hi + lo exactly, as the pass epilogue does without slots.
+struct PairSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float2 x) {
+    const float t = __fadd_rn(s, x.x);
+    const float bp = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x.x, bp));
+    c = __fadd_rn(c, __fadd_rn(e, x.y));
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return double(s) + double(c); }
+};
+
+// FP32 U/J passes: the Gaussian-erf A sums carry a scale, and A22 (DA22) is not
+// accumulated (the pairs are trace-free); both are applied to the FP64 sums.
+template <int PASS, int KERNEL>
+__device__ __forceinline__ void finish_f32_sums(double* v) {
+  if constexpr (PASS == PASS_UJ || PASS == PASS_UJD) {
+    if constexpr (KERNEL == VPM_KERNEL_GAUSSIANERF) {
+#pragma unroll
+      for (int w = 3; w < 11; ++w) v[w] *= kGaussAScale;
+    }
+    v[11] = -(v[3] + v[7]);
+    if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
+  }
+}
+
 // Cluster form of the epilogue (FP32C): after every rank's (hi, lo) pairs are
 // final, rank r forms the values of the targets [r·per, (r+1)·per) of the
 // tile from every rank's pairs, in rank order: the same FP64 sums, in the same
@@ -191,7 +225,7 @@ __device__ __forceinline__ int near_first_chunk(int j, int cs, int n) {
 // additions in the same order as reduce_kernel), the final values written, and
 // the summed lines that hold only this tile's targets dropped from L2 without
 // a write-back.
-template <int PASS, int KERNEL, int BLOCK, int T>
+template <int PASS, int KERNEL, int BLOCK, int T, bool F2>
 __device__ __noinline__ void tile_reduce(const PairArgs& a, int64_t t0, int64_t t1) {
   constexpr int NV = nval_of(PASS);
   // Values summed side by side: 2G loads in flight per thread, in few enough
@@ -206,20 +240,35 @@ __device__ __noinline__ void tile_reduce(const PairArgs& a, int64_t t0, int64_t 
     double v[NV];
 #pragma unroll
     for (int w0 = 0; w0 < NV; w0 += G) {
-      double s[G];
-#pragma unroll
-      for (int g = 0; g < G; ++g) s[g] = 0.0;
-      const double* p = a.part + int64_t(w0) * a.ldp + i;
+      if constexpr (F2) {
+        PairSum s[G];
+        const float2* p = reinterpret_cast<const float2*>(a.part) + int64_t(w0) * a.ldp + i;
 #pragma unroll 2
-      for (int c = 0; c < a.n_chunk; ++c, p += step) {
+        for (int c = 0; c < a.n_chunk; ++c, p += step) {
+#pragma unroll
+          for (int g = 0; g < G; ++g)
+            if (w0 + g < NV) s[g].add(__ldcg(p + int64_t(g) * a.ldp));
+        }
 #pragma unroll
         for (int g = 0; g < G; ++g)
-          if (w0 + g < NV) s[g] += __ldcg(p + int64_t(g) * a.ldp);
-      }
+          if (w0 + g < NV) v[w0 + g] = s[g].value();
+      } else {
+        double s[G];
 #pragma unroll
-      for (int g = 0; g < G; ++g)
-        if (w0 + g < NV) v[w0 + g] = s[g];
+        for (int g = 0; g < G; ++g) s[g] = 0.0;
+        const double* p = a.part + int64_t(w0) * a.ldp + i;
+#pragma unroll 2
+        for (int c = 0; c < a.n_chunk; ++c, p += step) {
+#pragma unroll
+          for (int g = 0; g < G; ++g)
+            if (w0 + g < NV) s[g] += __ldcg(p + int64_t(g) * a.ldp);
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+          if (w0 + g < NV) v[w0 + g] = s[g];
+      }
     }
+    if constexpr (F2) finish_f32_sums<PASS, KERNEL>(v);
     write_final<PASS, KERNEL>(v, a, i);
   }
   __syncthreads();   // every read of the tile's slots is done
@@ -692,10 +741,23 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     }
 
     // ---- epilogue ------------------------------------------------------------
+    // A slot is kept in L2 (evict_last) in the fused form until its tile is summed.
 #pragma unroll
     for (int k = 0; k < T; ++k) {
       const int64_t i = t0 + k * BLOCK + tid;
       if (i >= t1) continue;
+      if constexpr (F32) {
+        if (slot >= 0) {   // the raw float pairs (PairSum)
+          const uint64_t pol = l2_policy(a.tile_done != nullptr);
+#pragma unroll
+          for (int w = 0; w < NV; ++w) {
+            const int o = (w * T + k) * BLOCK + tid;
+            st_global_hint_f2(a.part + (int64_t(slot) * NV + w) * a.ldp + i,
+                              COMP ? fold_hi[o] : acc[k][w], COMP ? fold_lo[o] : 0.f, pol);
+          }
+          continue;
+        }
+      }
       double v[NV];
 #pragma unroll
       for (int w = 0; w < NV; ++w) {
@@ -706,17 +768,8 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
           v[w] = double(acc[k][w]);
         }
       }
-      // FP32 U/J passes do not accumulate A22 (trace-free pairs): rebuild it.
-      if constexpr (Tr::kUJ && F32) {
-        if constexpr (KERNEL == VPM_KERNEL_GAUSSIANERF) {
-#pragma unroll
-          for (int w = 3; w < 11; ++w) v[w] *= kGaussAScale;
-        }
-        v[11] = -(v[3] + v[7]);
-        if constexpr (PASS == PASS_UJD) v[23] = -(v[15] + v[19]);
-      }
+      if constexpr (F32) finish_f32_sums<PASS, KERNEL>(v);
       if (slot >= 0) {
-        // The fused form keeps the slot in L2 (evict_last) until the tile is summed.
         const uint64_t pol = l2_policy(a.tile_done != nullptr);
 #pragma unroll
         for (int w = 0; w < NV; ++w)
@@ -735,7 +788,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
       __syncthreads();
       if (s_last) {
         __threadfence();
-        tile_reduce<PASS, KERNEL, BLOCK, T>(a, t0, t1);
+        tile_reduce<PASS, KERNEL, BLOCK, T, F32>(a, t0, t1);
       }
     }
 
@@ -752,20 +805,23 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 }
 
 // Fixed-order sum of the partial slots.  A block holds 32 targets (x) and
-// kReduceRows value rows (y): thread (x, y) sums rows y, y + kReduceRows, ...
-// of its target over the chunks in chunk order, four loads in flight (the same
-// FP64 additions in the same order as one thread per target walking every
-// row, so the result is bitwise that one), and one warp then forms the final
-// values from shared memory.  A target per thread alone left most SMs idle at
-// small N (30 blocks at N = 7,600) with one dependent chain per thread.
-constexpr int kReduceRows = 8;
+// reduce_rows(NV) value rows (y): thread (x, y) sums rows y, y + rows, ... of
+// its target over the chunks in chunk order, loading kReduceLoads chunks ahead
+// (the same FP64 additions in the same order as one thread per target walking
+// every row, so the result is bitwise that one), and one warp then forms the
+// final values from shared memory.  The sum is latency-bound: at N = 7,600 (60
+// chunks) two rows per thread with four loads in flight took 20.5 µs per U/J
+// reduction with warm caches.
+__host__ __device__ constexpr int reduce_rows(int nv) { return nv <= 16 ? nv : (nv + 1) / 2; }
+constexpr int kReduceLoads = 8;
 
-template <int PASS, int KERNEL>
-__global__ void __launch_bounds__(32 * kReduceRows) reduce_kernel(
+template <int PASS, int KERNEL, bool F2>
+__global__ void __launch_bounds__(32 * reduce_rows(nval_of(PASS))) reduce_kernel(
     const double* __restrict__ part, int64_t ldp, const int64_t* __restrict__ foff,
     const int32_t* __restrict__ fchunks, int nfields, int scalar_chunks, int64_t t_begin,
     int64_t t_end, PairArgs out) {
   constexpr int NV = nval_of(PASS);
+  constexpr int kRows = reduce_rows(NV);
   __shared__ double sv[NV][33];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t i = t_begin + int64_t(blockIdx.x) * 32 + tx;
@@ -784,17 +840,33 @@ __global__ void __launch_bounds__(32 * kReduceRows) reduce_kernel(
   const bool live = nc > 1;
   if (live) {
     const int64_t step = int64_t(NV) * ldp;
-    for (int w = ty; w < NV; w += kReduceRows) {
-      const double* p = part + int64_t(w) * ldp + i;
-      double v = 0.0;
+    for (int w = ty; w < NV; w += kRows) {
       int c = 0;
-      for (; c + 4 <= nc; c += 4) {
-        const double a0 = p[int64_t(c) * step], a1 = p[int64_t(c + 1) * step];
-        const double a2 = p[int64_t(c + 2) * step], a3 = p[int64_t(c + 3) * step];
-        v += a0; v += a1; v += a2; v += a3;
+      if constexpr (F2) {
+        const float2* p = reinterpret_cast<const float2*>(part) + int64_t(w) * ldp + i;
+        PairSum sum;
+        for (; c + kReduceLoads <= nc; c += kReduceLoads) {
+          float2 a[kReduceLoads];
+#pragma unroll
+          for (int l = 0; l < kReduceLoads; ++l) a[l] = p[int64_t(c + l) * step];
+#pragma unroll
+          for (int l = 0; l < kReduceLoads; ++l) sum.add(a[l]);
+        }
+        for (; c < nc; ++c) sum.add(p[int64_t(c) * step]);
+        sv[w][tx] = sum.value();
+      } else {
+        const double* p = part + int64_t(w) * ldp + i;
+        double v = 0.0;
+        for (; c + kReduceLoads <= nc; c += kReduceLoads) {
+          double a[kReduceLoads];
+#pragma unroll
+          for (int l = 0; l < kReduceLoads; ++l) a[l] = p[int64_t(c + l) * step];
+#pragma unroll
+          for (int l = 0; l < kReduceLoads; ++l) v += a[l];
+        }
+        for (; c < nc; ++c) v += p[int64_t(c) * step];
+        sv[w][tx] = v;
       }
-      for (; c < nc; ++c) v += p[int64_t(c) * step];
-      sv[w][tx] = v;
     }
   }
   __syncthreads();
@@ -802,6 +874,7 @@ __global__ void __launch_bounds__(32 * kReduceRows) reduce_kernel(
     double v[NV];
 #pragma unroll
     for (int w = 0; w < NV; ++w) v[w] = sv[w][tx];
+    if constexpr (F2) finish_f32_sums<PASS, KERNEL>(v);
     write_final<PASS, KERNEL>(v, out, i);
   }
 }
@@ -949,23 +1022,29 @@ int max_active_clusters(int kernel, int precision, Shape s, int cluster) {
 }
 
 template <int PASS>
-cudaError_t reduce(int kernel, const double* part, int64_t ldp, const int64_t* foff,
-                   const int32_t* fchunks, int nfields, int scalar_chunks, int64_t t_begin,
-                   int64_t t_end, double* u, double* j, double* dj, int64_t ldo,
-                   cudaStream_t st) {
+cudaError_t reduce(int kernel, int precision, const double* part, int64_t ldp,
+                   const int64_t* foff, const int32_t* fchunks, int nfields, int scalar_chunks,
+                   int64_t t_begin, int64_t t_end, double* u, double* j, double* dj,
+                   int64_t ldo, cudaStream_t st) {
   const int64_t n = t_end - t_begin;
   if (n <= 0) return cudaSuccess;
   PairArgs out;
   memset(&out, 0, sizeof(out));
   out.u = u; out.j = j; out.dj = dj; out.ldo = ldo;
-  const dim3 bs(32, kReduceRows);
+  const dim3 bs(32, reduce_rows(nval_of(PASS)));
   const int grid = int((n + 31) / 32);
-  if (kernel == VPM_KERNEL_WINCKELMANS)
-    reduce_kernel<PASS, VPM_KERNEL_WINCKELMANS><<<grid, bs, 0, st>>>(
-        part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin, t_end, out);
-  else
-    reduce_kernel<PASS, VPM_KERNEL_GAUSSIANERF><<<grid, bs, 0, st>>>(
-        part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin, t_end, out);
+  const bool f2 = precision != VPM_PREC_FP64;   // float-pair slots (PairSum)
+  auto go = [&](auto kern) {
+    kern<<<grid, bs, 0, st>>>(part, ldp, foff, fchunks, nfields, scalar_chunks, t_begin, t_end,
+                              out);
+  };
+  if (kernel == VPM_KERNEL_WINCKELMANS) {
+    if (f2) go(reduce_kernel<PASS, VPM_KERNEL_WINCKELMANS, true>);
+    else go(reduce_kernel<PASS, VPM_KERNEL_WINCKELMANS, false>);
+  } else {
+    if (f2) go(reduce_kernel<PASS, VPM_KERNEL_GAUSSIANERF, true>);
+    else go(reduce_kernel<PASS, VPM_KERNEL_GAUSSIANERF, false>);
+  }
   return cudaGetLastError();
 }
 

@@ -1266,6 +1266,14 @@ __device__ __forceinline__ void st_global_hint(double* p, double v, uint64_t pol
                : "memory");
 }
 
+// Store the float pair (h, l) in the 8 bytes at p with the L2 cache policy pol.
+__device__ __forceinline__ void st_global_hint_f2(double* p, float h, float l, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(
+                   __cvta_generic_to_global(p)),
+               "f"(h), "f"(l), "l"(pol)
+               : "memory");
+}
+
 // Drop the 128-byte L2 line at p (128-byte aligned, device memory) without a
 // write-back: its contents become undefined, so only data that no one reads
 // again may be discarded.
