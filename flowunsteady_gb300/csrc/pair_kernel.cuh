@@ -165,8 +165,8 @@ __device__ __forceinline__ void finish_f32_sums(double* v) {
 
 // Cluster form of the epilogue (FP32C): after every rank's (hi, lo) pairs are
 // final, rank r forms the values of the targets [r·per, (r+1)·per) of the
-// tile from every rank's pairs, in rank order: the same FP64 sums, in the same
-// order, as the partial-slot form and its fixed-order reduction.
+// tile from every rank's pairs, in rank order, as FP64 sums of each rank's
+// hi + lo (the partial-slot form sums the same pairs as a double-float).
 template <int PASS, int KERNEL, int PREC, int BLOCK, int T>
 __device__ __forceinline__ void cluster_epilogue(const PairArgs& a, const float* fold_hi,
                                               const float* fold_lo, int64_t t0, int64_t t1) {
