@@ -1,15 +1,17 @@
 """The fused reduction of split source ranges.
 
-When a target tile's sources are split into chunks, every chunk writes FP64
-partial sums into its slot.  Either a second launch sums the slots in chunk
-order, or (the fused form) the last CTA of each tile to finish sums them, in
-the same order, inside the pair launch.  The planner fuses the passes of large
+When a target tile's sources are split into chunks, every chunk writes its
+partial sums into its slot (FP64 values, or the FP32 passes' float pairs).
+Either a second launch sums the slots in chunk order, or (the fused form) the
+last CTA of each tile to finish sums them, in the same order and arithmetic,
+inside the pair launch.  The planner fuses the passes of large
 fields; VPM_FUSED_REDUCE=1 fuses every split pass and =0 none.
 
 Checked here, with each form forced in its own process: the fused form runs
 (one launch fewer per split pass), gives bitwise the values of the separate
-reduction for U/J (FP32C and FP64), a target subset, and three dynamic-SFS
-RK3 steps, and matches the CPU FP64 oracle."""
+reduction for U/J (FP32C and FP64), a target subset, the two stateless entry
+points (the no-alloc one with its static scratch), and three dynamic-SFS RK3
+steps, and matches the CPU FP64 oracle."""
 import os
 import subprocess
 import sys
@@ -44,6 +46,26 @@ with Ctx(n) as c:
             c.rc(L.lib().vpm_get_launch_count(c.p, ctypes.byref(l1)))
             out[f"launches{k}{p}"] = np.array(l1.value - l0.value)
     out["Us"], out["Js"] = c.uj(1, L.PREC_FP32C, 1000, n - 777)
+# The stateless entry points (caller's device arrays; the no-alloc one keeps
+# the slots and the tile counters in its static scratch): all targets, and
+# 3,000 probe targets against all sources.
+import torch
+dev = torch.device("cuda:0")
+Xd, Gd, Sd = (torch.tensor(np.ascontiguousarray(a), device=dev) for a in (X.T, G.T, S))
+Xp = torch.tensor(np.ascontiguousarray(X[:3000].T * 0.9), device=dev)
+for name in ("vpm_uj_device_async", "vpm_uj_device_noalloc"):
+    fn = getattr(L.lib(), name)
+    for m, Xt in ((n, None), (3000, Xp)):
+        if name.endswith("noalloc") and m > 16384:
+            continue
+        Ud = torch.zeros((3, m), dtype=torch.float64, device=dev)
+        Jd = torch.zeros((9, m), dtype=torch.float64, device=dev)
+        rc = fn(1, L.PREC_FP32C, n, Xd.data_ptr(), Gd.data_ptr(), Sd.data_ptr(), n, m,
+                None if Xt is None else Xt.data_ptr(), m, Ud.data_ptr(), Jd.data_ptr(), m, None)
+        assert rc == 0, L.last_error()
+        torch.cuda.synchronize()
+        out[f"{name}_{m}_U"] = Ud.cpu().numpy().T
+        out[f"{name}_{m}_J"] = Jd.cpu().numpy().T
 flags = L.SFS_CLIP_BACKSCATTER | L.SFS_FORCE_POSITIVE | L.SFS_ANALYTIC_DSIGMA
 with Ctx(n) as c:
     c.set(X * 0.5, G * 200.0, S * 1.5)
