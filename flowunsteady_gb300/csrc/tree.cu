@@ -1136,8 +1136,14 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
     unsigned long long* pairs) {
   constexpr int NC = ncoef(P), ROWM = 3 * NC, FCH = far_chunk<P, M>();
   __shared__ M smom[FCH * ROWM];
-  __shared__ double sctr[FCH][3];
+  __shared__ R sctr[FCH][3];
   const int a = int(blockIdx.x) * kTreeBlock, b = int(min(int64_t(a) + kTreeBlock, n));
+  // Targets and cell centres relative to the group's first target, formed in
+  // FP64 once per target and once per staged cell, so that the evaluations
+  // subtract in R (GB300's FP64 pipe retires about two operations per SM and
+  // cycle; three FP64 differences and conversions per evaluation cost more
+  // than the FP32 work they feed).
+  const double ox = sorted[a], oy = sorted[ldw + a], oz = sorted[2 * ldw + a];
   const int64_t t0s = int64_t(blockIdx.x) * nfront, t1s = t0s + nfront - 1;
   const int f0 = ofar[t0s], fn = ofar[t1s] + nfar[t1s] - f0;
   if (threadIdx.x == 0) atomicAdd(&pairs[1], (unsigned long long)fn * (unsigned long long)(b - a));
@@ -1145,7 +1151,7 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
   const bool active = i < b;
   {
     const int ii = active ? i : a;
-    const double x = sorted[ii], y = sorted[ldw + ii], z = sorted[2 * ldw + ii];
+    const R x = R(sorted[ii] - ox), y = R(sorted[ldw + ii] - oy), z = R(sorted[2 * ldw + ii] - oz);
     R dp[9], dd[18];
 #pragma unroll
     for (int k = 0; k < 9; ++k) dp[k] = R(0);
@@ -1167,12 +1173,12 @@ __global__ void __launch_bounds__(kTreeBlock) far_kernel(
         } else {
           cell_centre(geom + int64_t(s) * kGeom, sx, sy, sz, sr);
         }
-        sctr[c][0] = sx; sctr[c][1] = sy; sctr[c][2] = sz;
+        sctr[c][0] = R(sx - ox); sctr[c][1] = R(sy - oy); sctr[c][2] = R(sz - oz);
       }
       __syncthreads();
       for (int c = 0; c < cnt; ++c) {
         R bk[ncoef(P + 2)];
-        taylor_coefficients<P + 2, R>(R(x - sctr[c][0]), R(y - sctr[c][1]), R(z - sctr[c][2]), bk);
+        taylor_coefficients<P + 2, R>(x - sctr[c][0], y - sctr[c][1], z - sctr[c][2], bk);
         m2p_accumulate<P, R, M>(bk, smom + c * ROWM, dp, dd);
       }
     }
