@@ -327,6 +327,8 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
   // the host provides them; bulk copies need them.
   const bool use_rec = Tr::kRec && a.rec != nullptr;
   const bool use_tma = Tr::kTma && use_rec && a.tma != 0;
+  // The targets are the sources (same rows): their records hold their split.
+  const bool tgt_rec = use_rec && a.xt == a.xs && a.ldt == a.lds;
   // Gaussian-erf FP32 passes classify (warp, 32 sources) blocks by distance.
   constexpr bool kFarKernel = F32 && KERNEL == VPM_KERNEL_GAUSSIANERF;
   const bool use_far =
@@ -381,26 +383,41 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 
     // Reference point of the CTA: its first target (FP32C only).
     double cx = 0.0, cy = 0.0, cz = 0.0;
-    if (COMP) {
-      cx = a.xt[t0];
-      cy = a.xt[a.ldt + t0];
-      cz = a.xt[2 * a.ldt + t0];
-    }
     // With records, relative positions come from the (hi, lo) float split of
     // both ends, (h - ch) + (l - cl), for targets and sources alike, so that
-    // coincident particles stay exactly coincident.
+    // coincident particles stay exactly coincident.  Targets that are the
+    // sources themselves take their split from the records, which hold the
+    // same split_f32 pairs: no FP64 work per target (GB300's FP64 pipe
+    // retires about two operations per SM and cycle, and every work item
+    // loads its targets anew).
     float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
-    if (use_rec && COMP) {
-      split_f32(cx, chx, clx);
-      split_f32(cy, chy, cly);
-      split_f32(cz, chz, clz);
+    if (COMP) {
+      if (tgt_rec) {
+        const float4 r0 = a.rec[3 * t0], r1 = a.rec[3 * t0 + 1];
+        chx = r0.x; chy = r0.y; chz = r0.z;
+        clx = r1.x; cly = r1.y; clz = r1.z;
+      } else {
+        cx = a.xt[t0];
+        cy = a.xt[a.ldt + t0];
+        cz = a.xt[2 * a.ldt + t0];
+        if (use_rec) {
+          split_f32(cx, chx, clx);
+          split_f32(cy, chy, cly);
+          split_f32(cz, chz, clz);
+        }
+      }
     }
 
     R tx[T], ty[T], tz[T];
 #pragma unroll
     for (int k = 0; k < T; ++k) {
       const int64_t i = t0 + k * BLOCK + tid;
-      if (i < t1) {
+      if (i < t1 && tgt_rec) {
+        const float4 r0 = a.rec[3 * i], r1 = a.rec[3 * i + 1];
+        tx[k] = R(rel_f32(r0.x, r1.x, chx, clx));
+        ty[k] = R(rel_f32(r0.y, r1.y, chy, cly));
+        tz[k] = R(rel_f32(r0.z, r1.z, chz, clz));
+      } else if (i < t1) {
         const double px = a.xt[i], py = a.xt[a.ldt + i], pz = a.xt[2 * a.ldt + i];
         if (use_rec) {
           float h, l;
