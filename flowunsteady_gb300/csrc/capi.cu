@@ -605,7 +605,7 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
                                    double* dj) {
   const int64_t n = c->n, ld = c->ld;
   const bool uj = pass == PASS_UJ || pass == PASS_UJD;
-  const bool recs = uj && prec != VPM_PREC_FP64;   // FP32 U/J passes read packed records
+  const bool recs = prec != VPM_PREC_FP64;   // FP32 passes read packed records
   cudaError_t e = cudaSuccess;
   const int* perm = nullptr;
   if (c->dry) {
@@ -615,9 +615,13 @@ static cudaError_t ctx_pair_sorted(vpm_ctx* c, int pass, int kernel, int prec, d
     if (!c->sortw || !c->srt || !c->sout) return cudaErrorInvalidValue;
     e = sort_order(c->sortw, n, c->X, ld, c->st, &perm);
     if (e == cudaSuccess) e = gather_inputs(c, perm, vs, ws);
-    if (e == cudaSuccess && recs)
+    if (e == cudaSuccess && recs && uj)
       e = launch_pack_sources(kernel, n, c->srt, c->srt + 3 * ld, c->srt + 6 * ld, ld, scale,
                               c->rec, nullptr, c->st);
+    else if (e == cudaSuccess && recs)
+      e = launch_pack_zeta_sources(kernel, pass == PASS_ZETAD, n, c->srt, c->srt + 3 * ld,
+                                   c->srt + 6 * ld, vs ? c->srt + 7 * ld : nullptr,
+                                   ws ? c->srt + 10 * ld : nullptr, ld, scale, c->rec, c->st);
     if (e != cudaSuccess) return e;
     c->launches += 3 + (recs ? 1 : 0);
   }
@@ -701,6 +705,12 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
       c->launches += 1;
       a.rec = c->rec;
       a.tma = tma_disabled() ? 0 : 1;
+    } else if (prec != VPM_PREC_FP64) {
+      e = launch_pack_zeta_sources(kernel, pass == PASS_ZETAD, c->n, xs, gs, ss, vq, wq, ld, scale,
+                                   c->rec, c->st);
+      if (e != cudaSuccess) return e;
+      c->launches += 1;
+      a.rec = c->rec;
     }
     // One persistent launch per tile-shape group, each over its own queue.
     for (size_t g = 0; g < bp->groups.size(); ++g) {
@@ -738,6 +748,14 @@ cudaError_t ctx_pair(vpm_ctx* c, int pass, int kernel, int prec, int64_t t0, int
     if (!c->dry) {
       cudaError_t e = launch_pack_sources(kernel, c->n, c->X, c->G, c->S, c->ld, scale, c->rec,
                                           pc.coh ? c->coh : nullptr, c->st);
+      if (e != cudaSuccess) return e;
+      c->launches += 1;
+    }
+    pc.rec = c->rec;
+  } else if (prec != VPM_PREC_FP64) {
+    if (!c->dry) {
+      cudaError_t e = launch_pack_zeta_sources(kernel, pass == PASS_ZETAD, c->n, c->X, c->G, c->S,
+                                               vs, ws, c->ld, scale, c->rec, c->st);
       if (e != cudaSuccess) return e;
       c->launches += 1;
     }
@@ -1036,7 +1054,8 @@ int vpm_ctx_create(int device, int64_t capacity, vpm_ctx** out) {
   cudaError_t e = cudaMemset(c->base, 0, rows * ld * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c->stat, size_t(c->ld));
   if (e == cudaSuccess) e = cudaMemset(c->stat, 0, size_t(c->ld));
-  if (e == cudaSuccess) e = cudaMalloc(&c->rec, 3 * ld * sizeof(float4));
+  // Packed source records: 3 float4 per particle for the U/J passes, up to 5 for ζ.
+  if (e == cudaSuccess) e = cudaMalloc(&c->rec, 5 * ld * sizeof(float4));
   // Until the first packing the particle order counts as coherent.
   if (e == cudaSuccess) e = cudaMalloc(&c->coh, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMemset(c->coh, 0xff, sizeof(unsigned int));

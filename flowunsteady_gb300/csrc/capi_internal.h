@@ -32,8 +32,9 @@ struct PairCall {
   int64_t ldo;
   int max_chunks = 0;   // upper bound on source chunks (0 = planner's choice)
   int64_t chunk = 0;    // pinned source chunk length (0 = planner's choice)
-  // FP32 U/J passes: packed records of the ns sources (launch_pack_sources),
-  // or null to read the FP64 rows in the kernel.  Bulk copies stage records.
+  // FP32 passes: packed records of the ns sources (launch_pack_sources for
+  // U/J, launch_pack_zeta_sources for ζ), or null to read the FP64 rows in the
+  // kernel.  Bulk copies stage the U/J records.
   const float4* rec = nullptr;
   const unsigned int* coh = nullptr;   // compact-block count (see PairArgs::coh)
   int* status = nullptr;

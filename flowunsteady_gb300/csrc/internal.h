@@ -62,8 +62,9 @@ struct PairArgs {
   int64_t ldo;
   double* part;
   int64_t ldp;
-  // FP32 U/J passes: packed source records, 3 float4 per source (null: read
-  // and convert the FP64 rows in the kernel).  Records are 16-byte aligned.
+  // FP32 passes: packed source records, 3 float4 per source for U/J, 4 for ζ,
+  // 5 for ζ + α-derivative (null: read and convert the FP64 rows in the
+  // kernel).  Records are 16-byte aligned.
   const float4* rec;
   // Stage the records with bulk asynchronous copies (PASS_UJ; needs rec).
   int32_t tma;
@@ -131,6 +132,13 @@ bool pair_shape_supported(int precision, Shape shape);
 cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
                                 const double* S, int64_t ld, double scale, float4* rec,
                                 unsigned int* compact, cudaStream_t st);
+// Packed source records of the FP32 ζ passes (4 float4 per source, 5 with d
+// for PASS_ZETAD): split positions and ζ constants of σ·scale, Γ, v_q (V rows,
+// zero when null) and w_q (W rows).
+cudaError_t launch_pack_zeta_sources(int kernel, bool d, int64_t n, const double* X,
+                                     const double* G, const double* S, const double* V,
+                                     const double* W, int64_t ld, double scale, float4* rec,
+                                     cudaStream_t st);
 cudaError_t launch_reduce(int pass, int kernel, int precision, const double* part, int64_t ldp,
                           const int64_t* foff, const int32_t* fchunks, int nfields,
                           int scalar_chunks, int64_t t_begin, int64_t t_end, double* u,

@@ -72,6 +72,54 @@ __global__ void __launch_bounds__(256) pack_sources_kernel(int64_t n, const doub
   }
 }
 
+// Packed source records of the FP32 ζ passes, per source
+//   (xh, yh, zh, a), (xl, yl, zl, b), (Γx, Γy, Γz, c), (v_q, 0) [, (w_q, 0)]
+// with (a, b, c) the ζ constants of σ·scale (zeta_consts_f32) and v_q, w_q
+// from the rows V, W (zero when V is null).  Staging these instead of the FP64
+// rows keeps FP64 arithmetic (differences, the constants' divisions, and for
+// Winckelmans a pow) out of the pair kernels, where every CTA would repeat it
+// for every source it stages.
+template <int KERNEL, bool D>
+__global__ void __launch_bounds__(256) pack_zeta_sources_kernel(
+    int64_t n, const double* __restrict__ X, const double* __restrict__ G,
+    const double* __restrict__ S, const double* __restrict__ V, const double* __restrict__ W,
+    int64_t ld, double scale, float4* __restrict__ rec) {
+  constexpr int Q = D ? 5 : 4;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float xh, xl, yh, yl, zh, zl, ka, kb, kc;
+  split_f32(X[i], xh, xl);
+  split_f32(X[ld + i], yh, yl);
+  split_f32(X[2 * ld + i], zh, zl);
+  zeta_consts_f32<KERNEL>(S[i] * scale, ka, kb, kc);
+  float4* r = rec + Q * i;
+  r[0] = make_float4(xh, yh, zh, ka);
+  r[1] = make_float4(xl, yl, zl, kb);
+  r[2] = make_float4(float(G[i]), float(G[ld + i]), float(G[2 * ld + i]), kc);
+  r[3] = V ? make_float4(float(V[i]), float(V[ld + i]), float(V[2 * ld + i]), 0.f)
+           : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (D)
+    r[Q - 1] = W ? make_float4(float(W[i]), float(W[ld + i]), float(W[2 * ld + i]), 0.f)
+                 : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+cudaError_t launch_pack_zeta_sources(int kernel, bool d, int64_t n, const double* X,
+                                     const double* G, const double* S, const double* V,
+                                     const double* W, int64_t ld, double scale, float4* rec,
+                                     cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = int((n + 255) / 256);
+  auto go = [&](auto kern) { kern<<<grid, 256, 0, st>>>(n, X, G, S, V, W, ld, scale, rec); };
+  if (kernel == VPM_KERNEL_WINCKELMANS) {
+    if (d) go(pack_zeta_sources_kernel<VPM_KERNEL_WINCKELMANS, true>);
+    else go(pack_zeta_sources_kernel<VPM_KERNEL_WINCKELMANS, false>);
+  } else {
+    if (d) go(pack_zeta_sources_kernel<VPM_KERNEL_GAUSSIANERF, true>);
+    else go(pack_zeta_sources_kernel<VPM_KERNEL_GAUSSIANERF, false>);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack_sources(int kernel, int64_t n, const double* X, const double* G,
                                 const double* S, int64_t ld, double scale, float4* rec,
                                 unsigned int* compact, cudaStream_t st) {

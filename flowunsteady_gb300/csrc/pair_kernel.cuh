@@ -54,11 +54,14 @@ struct PairTraits {
   static constexpr bool kD = PASS == PASS_UJD || PASS == PASS_ZETAD;
   // shared quads per source: (x, a), (Γ, b), and for ζ passes v_q (and w_q)
   static constexpr int kQuads = kUJ ? 2 : (PASS == PASS_ZETA ? 3 : 4);
-  // The FP32 U/J passes read packed source records (3 float4 per source, see
-  // pack_sources_kernel); the plain U/J pass stages them with bulk copies.
-  static constexpr bool kRec = kUJ && PREC != VPM_PREC_FP64;
+  // The FP32 passes read packed source records (pack_sources_kernel for U/J,
+  // pack_zeta_sources_kernel for ζ); the plain U/J pass stages them with bulk
+  // copies.
+  static constexpr bool kRec = PREC != VPM_PREC_FP64;
   static constexpr bool kTma = PASS == PASS_UJ && PREC != VPM_PREC_FP64;
-  static constexpr int kRecBytes = 48;
+  // float4 per source record: U/J 3, ζ 4 (+ v_q), ζ + α-derivative 5 (+ w_q).
+  static constexpr int kRecQuads = kUJ ? 3 : (PASS == PASS_ZETA ? 4 : 5);
+  static constexpr int kRecBytes = 16 * kRecQuads;
 };
 
 // Shared memory: source quads, then (FP32) the far-field boxes (per warp two
@@ -393,7 +396,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
     if (COMP) {
       if (tgt_rec) {
-        const float4 r0 = a.rec[3 * t0], r1 = a.rec[3 * t0 + 1];
+        const float4 r0 = a.rec[Tr::kRecQuads * t0], r1 = a.rec[Tr::kRecQuads * t0 + 1];
         chx = r0.x; chy = r0.y; chz = r0.z;
         clx = r1.x; cly = r1.y; clz = r1.z;
       } else {
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
     for (int k = 0; k < T; ++k) {
       const int64_t i = t0 + k * BLOCK + tid;
       if (i < t1 && tgt_rec) {
-        const float4 r0 = a.rec[3 * i], r1 = a.rec[3 * i + 1];
+        const float4 r0 = a.rec[Tr::kRecQuads * i], r1 = a.rec[Tr::kRecQuads * i + 1];
         tx[k] = R(rel_f32(r0.x, r1.x, chx, clx));
         ty[k] = R(rel_f32(r0.y, r1.y, chy, cly));
         tz[k] = R(rel_f32(r0.z, r1.z, chz, clz));
@@ -504,13 +507,23 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
         qc.x = qc.y = qc.z = qc.w = R(0);
         qd.x = qd.y = qd.z = qd.w = R(0);
         if (use_rec && jj < s1) {
-          const float4 r0 = a.rec[3 * jj], r1 = a.rec[3 * jj + 1], r2 = a.rec[3 * jj + 2];
+          const float4* r = a.rec + Tr::kRecQuads * jj;
+          const float4 r0 = r[0], r1 = r[1], r2 = r[2];
           qa.x = R(rel_f32(r0.x, r1.x, chx, clx));
           qa.y = R(rel_f32(r0.y, r1.y, chy, cly));
           qa.z = R(rel_f32(r0.z, r1.z, chz, clz));
           qa.w = R(r0.w);
           qb.x = R(r2.x); qb.y = R(r2.y); qb.z = R(r2.z);
           qb.w = R(r1.w);
+          if constexpr (!Tr::kUJ) {   // ζ: (v_q, c) and (w_q, 0)
+            const float4 r3 = r[3];
+            qc.x = R(r3.x); qc.y = R(r3.y); qc.z = R(r3.z);
+            qc.w = R(r2.w);
+            if constexpr (PASS == PASS_ZETAD) {
+              const float4 r4 = r[4];
+              qd.x = R(r4.x); qd.y = R(r4.y); qd.z = R(r4.z);
+            }
+          }
         } else if (jj < s1) {
           const double px = a.xs[jj], py = a.xs[a.lds + jj], pz = a.xs[2 * a.lds + jj];
           const double sig = a.ss[jj] * a.sigma_scale;
