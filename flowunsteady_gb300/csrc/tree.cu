@@ -76,7 +76,7 @@ struct FmmWork {
   double* sorted = nullptr;   // X 3, Γ 3, σ 1 rows of length cap
   float4* rec = nullptr;      // packed FP32 source records of the sorted particles
   double* near_raw = nullptr; // up to 27 raw near-field sums per sorted particle
-  double* vw = nullptr;       // v_q, w_q rows of the ζ passes in Morton order
+  float* vw = nullptr;        // v_q, w_q rows of the ζ passes in Morton order, FP32
   // cells
   int *lo = nullptr, *hi = nullptr, *child = nullptr, *nchild = nullptr;
   double* geom = nullptr;     // per cell: box min x y z, box max x y z, σmax, unused
@@ -599,7 +599,7 @@ template <int KERNEL, int PASS>
 __global__ void __launch_bounds__(kNearThreads, NearShape<PASS>::kMinBlocks) near_tile_kernel(
     int nfront, const int* __restrict__ onear, const int* __restrict__ nnear,
     const int2* __restrict__ near_list, const float4* __restrict__ rec,
-    const double* __restrict__ vw, int64_t ldv, double* raw, int64_t ldr, int64_t n,
+    const float* __restrict__ vw, int64_t ldv, double* raw, int64_t ldr, int64_t n,
     int* counters, unsigned long long* pairs) {
   using Sh = NearShape<PASS>;
   constexpr int T = Sh::T, TQ = Sh::TQ, SL = Sh::SL, NV = Sh::NV;
@@ -720,9 +720,8 @@ __global__ void __launch_bounds__(kNearThreads, NearShape<PASS>::kMinBlocks) nea
           // Gaussian-erf ζ constants: a = -log2(e)/(2σ²) (as for U/J), b = ζ(0)/σ³.
           const float is1 = r1.w;
           qb = make_float4(r2.x, r2.y, r2.z, float(kZeta0Gauss) * is1 * is1 * is1);
-          qc = make_float4(float(vw[j]), float(vw[ldv + j]), float(vw[2 * ldv + j]), 0.f);
-          if (D) qd = make_float4(float(vw[3 * ldv + j]), float(vw[4 * ldv + j]),
-                                  float(vw[5 * ldv + j]), 0.f);
+          qc = make_float4(vw[j], vw[ldv + j], vw[2 * ldv + j], 0.f);
+          if (D) qd = make_float4(vw[3 * ldv + j], vw[4 * ldv + j], vw[5 * ldv + j], 0.f);
         }
       }
       __syncthreads();   // previous tile consumed
@@ -786,7 +785,7 @@ __global__ void __launch_bounds__(kNearThreads, NearShape<PASS>::kMinBlocks) nea
 }
 
 template <int KERNEL, int PASS>
-void launch_near(int ngroups, int nfront, const FmmWork* w, const double* vw, int64_t ldv,
+void launch_near(int ngroups, int nfront, const FmmWork* w, const float* vw, int64_t ldv,
                  int64_t ldr, int64_t n, unsigned long long* pairs, cudaStream_t st) {
   static const bool once = [] {
     cudaFuncSetAttribute(near_tile_kernel<KERNEL, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -817,6 +816,18 @@ __global__ void gather_rows_kernel(int64_t n, int rows, const int* __restrict__ 
   if (i >= n) return;
   const int64_t o = perm[i];
   for (int r = 0; r < rows; ++r) dst[r * ldd + i] = src[r * lds + o];
+}
+
+// Rows of an FP64 array in the original order into FP32 rows of the Morton
+// order: the ζ passes' v_q and w_q, converted once per pass rather than once
+// per staged source in the near field (GB300 converts FP64 at its FP64 rate).
+__global__ void gather_rows_f32_kernel(int64_t n, int rows, const int* __restrict__ perm,
+                                       const double* __restrict__ src, int64_t lds, float* dst,
+                                       int64_t ldd) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = perm[i];
+  for (int r = 0; r < rows; ++r) dst[r * ldd + i] = float(src[r * lds + o]);
 }
 
 // FP64 near field on the sorted FP64 state (positions relative to the leaf's
@@ -1657,8 +1668,9 @@ cudaError_t fmm_zeta(vpm_ctx* c, bool d, const double* vs, const double* ws, dou
   const int64_t ldw = w->cap;
   const int ngroups = int(w->last_groups), nfront = int(w->last_nfront);
   const int grid = int((n + 255) / 256);
-  gather_rows_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, vs, c->ld, w->vw, ldw);
-  if (d) gather_rows_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, ws, c->ld, w->vw + 3 * ldw, ldw);
+  gather_rows_f32_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, vs, c->ld, w->vw, ldw);
+  if (d)
+    gather_rows_f32_kernel<<<grid, 256, 0, st>>>(n, 3, w->perm, ws, c->ld, w->vw + 3 * ldw, ldw);
   if (d)
     launch_near<VPM_KERNEL_GAUSSIANERF, PASS_ZETAD>(ngroups, nfront, w, w->vw, ldw, ldw, n,
                                                     nullptr, st);
