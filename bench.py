@@ -48,7 +48,7 @@ L2_FLUSH_BYTES = 256 << 20
 # benchmark workload per (N, tile shape), from an ncu capture.  The plain U/J
 # pass is split into about 64 waves of short work items (57 source chunks per
 # target tile with 128x4), which measured 5 % faster than whole tiles.  The
-# last CTA of each tile sums the chunks' FP64 partial sums from L2 and drops
+# last CTA of each tile sums the chunks' partial sums from L2 and drops
 # them there; what still reaches DRAM is partial sums evicted before their tile
 # was complete.  (With a separate reduction launch the partial sums took 1.8 GB.)
 PAIR_KERNEL_TRAFFIC = {(262144, "128x4"): 64656640 + 138696448}

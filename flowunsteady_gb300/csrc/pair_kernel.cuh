@@ -837,11 +837,10 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 // Fixed-order sum of the partial slots.  A block holds 32 targets (x) and
 // reduce_rows(NV) value rows (y): thread (x, y) sums rows y, y + rows, ... of
 // its target over the chunks in chunk order, loading kReduceLoads chunks ahead
-// (the same FP64 additions in the same order as one thread per target walking
-// every row, so the result is bitwise that one), and one warp then forms the
-// final values from shared memory.  The sum is latency-bound: at N = 7,600 (60
-// chunks) two rows per thread with four loads in flight took 20.5 µs per U/J
-// reduction with warm caches.
+// (the same additions in the same order as one thread per target walking every
+// row, so the result is bitwise that one), and one warp then forms the final
+// values from shared memory.  F2: the FP32 passes' float-pair slots, summed
+// with PairSum; otherwise FP64 slots and FP64 additions.
 __host__ __device__ constexpr int reduce_rows(int nv) { return nv <= 16 ? nv : (nv + 1) / 2; }
 constexpr int kReduceLoads = 8;
 
