@@ -2,9 +2,9 @@
 
 When a target tile's source range is split into chunks, the chunks either
 write their partial sums (FP32C: the (hi, lo) float pairs) into scratch rows
-that a second launch sums in fixed order (partial slots), or run as one thread-block cluster whose CTAs sum each
-other's compensated (hi, lo) pairs through distributed shared memory in rank
-order.  Partial slots are the default (measured faster on GB300);
+that a second launch sums in fixed order (partial slots), or run as one
+thread-block cluster whose CTAs sum each other's compensated (hi, lo) pairs
+through distributed shared memory in rank order.  Partial slots are the default (measured faster on GB300);
 VPM_CLUSTER=1 takes clusters wherever a cluster size fits.
 
 Checked here, with each form forced in its own process: the cluster form is
