@@ -179,8 +179,8 @@ static int plan_cluster(int device, const PairCall& pc, Shape sh, int64_t n_tb,
   return best_nc;
 }
 
-// Waves of work items the plain U/J pass is split into: with fewer target tiles
-// than resident CTAs, and with more.
+// Waves of work items a pass is split into: with fewer target tiles than
+// resident CTAs, and with more.
 constexpr int kSmallWaves = 8;
 constexpr int kLargeWaves = 64;
 constexpr int64_t kLargeField = 131072;
@@ -220,15 +220,19 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
       chunk = cchunk;
     }
   }
-  // Plain U/J pass with fewer target tiles than one wave: split the sources
-  // into about eight waves of work items.  The items' costs differ (close
-  // pairs take the general form), and more, shorter CTAs let the block
-  // scheduler balance them; one wave of equal-length items waits for its
-  // slowest.  Measured (helical wake and the two rings, FP32C U/J, 128x2,
-  // pass and reduction): N = 7,600 170.9 -> 152.5 µs, 20,000 729.6 -> 620.2
-  // µs, 40,000 2,100 -> 2,010 µs, 65,536 5,182 -> 5,136 µs, 131,072
-  // unchanged.  The ζ and α-derivative passes did not get faster, while
-  // their reductions read the extra partial sums, so they keep the wave plan.
+  // Fewer target tiles than one wave: split the sources into about eight
+  // waves of work items.  The items' costs differ (close pairs take the
+  // general form), and more, shorter CTAs let the block scheduler balance
+  // them; one wave of equal-length items waits for its slowest.  Measured
+  // (helical wake and the two rings, FP32C U/J, 128x2, pass and reduction):
+  // N = 7,600 170.9 -> 152.5 µs, 20,000 729.6 -> 620.2 µs, 40,000 2,100 ->
+  // 2,010 µs, 65,536 5,182 -> 5,136 µs, 131,072 unchanged.  The ζ and
+  // α-derivative passes took it too once their reductions summed float pairs
+  // and the items ran near chunks first (they had kept one wave of items
+  // before): a ring step 0.567 -> 0.541 ms (analytic ∂/∂σ), an analytic SFS
+  // evaluation at 20,000 / 40,000 / 65,536 particles 1.09 / 3.51 / 7.74 ->
+  // 1.02 / 3.27 / 7.06 ms; four waves for them measured in between, two
+  // slower.
   // With a wave of tiles or more, every pass is split still finer, about
   // kLargeWaves waves of items: measured at N = 262,144 (128x4) the plain U/J
   // pass took 74.4 ms with whole waves of whole tiles (only the last wave
@@ -242,7 +246,7 @@ cudaError_t run_pair(const PairCall& pc, int device, int num_sms, const Shape* p
   // too: the ζ pass at 262,144 (128x4, fewer tiles than its resident CTAs)
   // measured 1.7 ms faster with 4,608-source chunks.
   const bool large = n_tb >= resident || pc.ns >= kLargeField;
-  if (cluster <= 1 && pc.chunk <= 0 && (pc.pass == PASS_UJ || large)) {
+  if (cluster <= 1 && pc.chunk <= 0) {
     const int waves = large ? kLargeWaves : kSmallWaves;
     const int64_t cc = ceil_div(int64_t(waves) * resident, n_tb);
     chunk = round_up(std::max<int64_t>(ceil_div(pc.ns, cc), 1), sh.block);
