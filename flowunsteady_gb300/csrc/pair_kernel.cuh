@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(BLOCK, (min_blocks<PASS, PREC, BLOCK, T>()))
 // row, so the result is bitwise that one), and one warp then forms the final
 // values from shared memory.  F2: the FP32 passes' float-pair slots, summed
 // with PairSum; otherwise FP64 slots and FP64 additions.
-__host__ __device__ constexpr int reduce_rows(int nv) { return nv <= 16 ? nv : (nv + 1) / 2; }
+__host__ __device__ constexpr int reduce_rows(int nv) { return nv <= 32 ? nv : (nv + 1) / 2; }
 constexpr int kReduceLoads = 8;
 
 template <int PASS, int KERNEL, bool F2>
